@@ -1,0 +1,1194 @@
+// bay_api.cpp -- host side of libbayadera_gb300.so (C ABI in include/bayadera_gb300.h).
+//
+// Owns contexts (device + stream), models (NVRTC-compiled fused stretch kernels,
+// loaded as CUDA driver-API libraries), and samplers (device-resident walker state,
+// control block, captured CUDA graphs for the step loops).  Mirrors the reference's
+// GTXStretch / GTXStretchFactory / GTXAcorEngine (internal/device/nvidia_gtx.clj).
+#include "bayadera_gb300.h"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bay_embedded.h"
+#include "bay_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Err {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw Err{code, msg}; }
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        const int code = (e == cudaErrorMemoryAllocation) ? BAY_ERR_ALLOC : BAY_ERR_CUDA;
+        fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+// Driver-API entry points, resolved through the runtime at first context creation so
+// that the library loads (and compile-checks models) on machines without a driver.
+struct DriverApi {
+    PFN_cuGetErrorString_v6000 GetErrorString = nullptr;
+    PFN_cuLibraryLoadData_v12000 LibraryLoadData = nullptr;
+    PFN_cuLibraryUnload_v12000 LibraryUnload = nullptr;
+    PFN_cuLibraryGetKernel_v12000 LibraryGetKernel = nullptr;
+    PFN_cuLaunchKernel_v4000 LaunchKernel = nullptr;
+    bool loaded = false;
+};
+DriverApi g_cu;
+std::mutex g_cu_mu;
+
+void cu_check(CUresult r, const char* what) {
+    if (r != CUDA_SUCCESS) {
+        const char* s = nullptr;
+        if (g_cu.GetErrorString) g_cu.GetErrorString(r, &s);
+        fail(BAY_ERR_CUDA, std::string(what) + ": " + (s ? s : "driver error " + std::to_string((int)r)));
+    }
+}
+
+template <class T>
+void resolve(const char* name, T& fn, unsigned version) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion(name, &p, version, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+        cudaGetLastError();
+        fail(BAY_ERR_CUDA, std::string("driver entry point not found: ") + name);
+    }
+    fn = reinterpret_cast<T>(p);
+}
+
+void load_driver_api() {
+    std::lock_guard<std::mutex> g(g_cu_mu);
+    if (g_cu.loaded) return;
+    resolve("cuGetErrorString", g_cu.GetErrorString, 6000);
+    resolve("cuLibraryLoadData", g_cu.LibraryLoadData, 12000);
+    resolve("cuLibraryUnload", g_cu.LibraryUnload, 12000);
+    resolve("cuLibraryGetKernel", g_cu.LibraryGetKernel, 12000);
+    resolve("cuLaunchKernel", g_cu.LaunchKernel, 4000);
+    g_cu.loaded = true;
+}
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return BAY_OK;
+    } catch (const Err& e) {
+        g_err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_err = "host allocation failed";
+        return BAY_ERR_ALLOC;
+    } catch (...) {
+        g_err = "unexpected exception";
+        return BAY_ERR_STATE;
+    }
+}
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Process-wide cache of NVRTC output: identical (source, options) compile once.
+std::mutex g_cache_mu;
+std::map<std::string, std::vector<char>> g_cubin_cache;
+
+constexpr uint32_t kChunk = 32;  // steps per captured graph
+
+}  // namespace
+
+// ============================================================================ context
+struct bay_ctx {
+    int device = 0;
+    uint32_t wgs = 1024;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaStream_t capture = nullptr;
+    uint64_t mem_limit = 0;
+    uint64_t allocated = 0;
+    std::recursive_mutex mu;
+    std::map<void*, size_t> sizes;
+
+    void* alloc(size_t bytes) {
+        if (bytes == 0) bytes = 16;
+        if (mem_limit && allocated + bytes > mem_limit)
+            fail(BAY_ERR_ALLOC, "device memory limit of the context exceeded (" +
+                                    std::to_string(allocated + bytes) + " > " +
+                                    std::to_string(mem_limit) + " bytes)");
+        void* p = nullptr;
+        cuda_check(cudaMalloc(&p, bytes), "cudaMalloc");
+        allocated += bytes;
+        sizes[p] = bytes;
+        return p;
+    }
+    void release(void* p) {
+        if (!p) return;
+        auto it = sizes.find(p);
+        if (it != sizes.end()) {
+            allocated -= it->second;
+            sizes.erase(it);
+        }
+        cudaFree(p);
+    }
+    void use() { cuda_check(cudaSetDevice(device), "cudaSetDevice"); }
+};
+
+// ============================================================================ model
+struct bay_model {
+    bay_ctx* ctx = nullptr;
+    CUlibrary lib = nullptr;
+    CUkernel k_bare = nullptr, k_accu = nullptr, k_logfn = nullptr;
+    uint32_t dim = 0, params_size = 0, form = 0, cta = 256, wpc = 1, flags = 0;
+};
+
+namespace {
+
+const char* kStdint =
+    "#pragma once\n"
+    "typedef unsigned char uint8_t; typedef signed char int8_t;\n"
+    "typedef unsigned short uint16_t; typedef short int16_t;\n"
+    "typedef unsigned int uint32_t; typedef int int32_t;\n"
+    "typedef unsigned long long uint64_t; typedef long long int64_t;\n";
+
+std::vector<char> nvrtc_compile(const std::string& src, const std::vector<std::string>& opts) {
+    std::string key = src;
+    for (auto& o : opts) key += "\n//" + o;
+    {
+        std::lock_guard<std::mutex> g(g_cache_mu);
+        auto it = g_cubin_cache.find(key);
+        if (it != g_cubin_cache.end()) return it->second;
+    }
+    nvrtcProgram prog;
+    const char* hdr_src[] = {kStdint, kStdint};
+    const char* hdr_name[] = {"stdint.h", "cstdint"};
+    if (nvrtcCreateProgram(&prog, src.c_str(), "bay_model.cu", 2, hdr_src, hdr_name) !=
+        NVRTC_SUCCESS)
+        fail(BAY_ERR_COMPILE, "nvrtcCreateProgram failed");
+    std::vector<const char*> o;
+    for (auto& s : opts) o.push_back(s.c_str());
+    const nvrtcResult r = nvrtcCompileProgram(prog, (int)o.size(), o.data());
+    if (r != NVRTC_SUCCESS) {
+        size_t n = 0;
+        nvrtcGetProgramLogSize(prog, &n);
+        std::string log(n, '\0');
+        if (n) nvrtcGetProgramLog(prog, &log[0]);
+        nvrtcDestroyProgram(&prog);
+        fail(BAY_ERR_COMPILE, std::string("model compilation failed: ") +
+                                  nvrtcGetErrorString(r) + "\n" + log);
+    }
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    std::vector<char> cubin(n);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    g_cubin_cache[key] = cubin;
+    return cubin;
+}
+
+bool valid_ident(const char* s) {
+    if (!s || !*s) return false;
+    if (!(std::isalpha((unsigned char)s[0]) || s[0] == '_')) return false;
+    for (const char* p = s; *p; ++p)
+        if (!(std::isalnum((unsigned char)*p) || *p == '_')) return false;
+    return true;
+}
+
+}  // namespace
+
+// ============================================================================ sampler
+struct bay_sampler {
+    bay_model* model = nullptr;
+    bay_ctx* ctx = nullptr;
+    uint64_t W = 0, K = 0;
+    uint32_t D = 0;
+    float* xs = nullptr;
+    float* logfn = nullptr;
+    bay_ctl* ctl = nullptr;
+    const float* params = nullptr;
+    bool own_params = false;
+    uint64_t n_params = 0, data_len = 0;
+    double* part = nullptr;
+    double* half_sum = nullptr;
+    float* means = nullptr;
+    uint64_t means_cap = 0;
+    float* stage = nullptr;  // W*D floats: AoS staging
+    double* stats = nullptr;  // 2*D doubles
+    float* hist = nullptr;    // limits + pdf + ranks scratch
+    uint32_t* counts = nullptr;
+    uint64_t hist_bins = 0;
+    // host mirror of the control block
+    uint32_t seed_bare = 0, seed_accu = 0;
+    uint32_t step_bare = 0, step_accu = 0;
+    float a = 2.0f, beta = 1.0f;
+    uint64_t iteration_counter = 0;
+    bool positioned = false;
+    bool graphs = true;
+    cudaGraphExec_t g_bare = nullptr, g_accu = nullptr;
+    uint64_t g_accu_cap = 0;
+
+    unsigned grid() const {
+        const uint64_t per = model->form == BAY_FORM_TILED ? model->wpc : model->cta;
+        return (unsigned)((K + per - 1) / per);
+    }
+
+    bay_stretch_params make_params(uint32_t half, uint32_t step_off) const {
+        bay_stretch_params p;
+        p.params = params;
+        p.xs = xs;
+        p.logfn = logfn;
+        p.ctl = ctl;
+        p.part = part;
+        p.half_sum = half_sum;
+        p.means = means;
+        p.data_len = data_len;
+        p.params_len = (unsigned)(n_params - data_len);
+        p.W = (unsigned)W;
+        p.K = (unsigned)K;
+        p.half = half;
+        p.step_off = step_off;
+        p.means_cap = (unsigned)std::min<uint64_t>(means_cap, 0xffffffffull);
+        p.inv_W = (float)(1.0 / (double)W);
+        return p;
+    }
+
+    void launch_half(bool accu, uint32_t half, uint32_t step_off, cudaStream_t st) {
+        if (st == ctx->stream) bay::count_launches(1);
+        bay_stretch_params p = make_params(half, step_off);
+        void* args[] = {&p};
+        cu_check(g_cu.LaunchKernel((CUfunction)(accu ? model->k_accu : model->k_bare), grid(), 1, 1,
+                                model->cta, 1, 1, 0, (CUstream)st, args, nullptr),
+                 "cuLaunchKernel(stretch)");
+    }
+
+    void ctl_op(const bay_ctl_op& op) {
+        cuda_check(bay::launch_ctl_apply(ctl, op, ctx->stream), "ctl_apply");
+    }
+
+    void launch_logfn_all() {
+        bay::count_launches(1);
+        bay_stretch_params p = make_params(0, 0);
+        void* args[] = {&p};
+        const uint64_t per = model->form == BAY_FORM_TILED ? model->wpc : model->cta;
+        const unsigned g = (unsigned)((W + per - 1) / per);
+        cu_check(g_cu.LaunchKernel((CUfunction)model->k_logfn, g, 1, 1, model->cta, 1, 1, 0,
+                                (CUstream)ctx->stream, args, nullptr),
+                 "cuLaunchKernel(logfn)");
+    }
+
+    cudaGraphExec_t capture_chunk(bool accu) {
+        cudaStream_t cs = ctx->capture;
+        cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "BeginCapture");
+        try {
+            for (uint32_t i = 0; i < kChunk; ++i) {
+                launch_half(accu, 0, i, cs);
+                launch_half(accu, 1, i, cs);
+            }
+            bay_ctl_op op{};
+            op.mask = accu ? BAY_CTL_ADD_STEP1 : BAY_CTL_ADD_STEP0;
+            op.step[accu ? 1 : 0] = kChunk;
+            cuda_check(bay::launch_ctl_apply(ctl, op, cs), "ctl_apply(capture)");
+        } catch (...) {
+            cudaGraph_t g;
+            cudaStreamEndCapture(cs, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        cudaGraph_t g = nullptr;
+        cuda_check(cudaStreamEndCapture(cs, &g), "EndCapture");
+        cudaGraphExec_t ex = nullptr;
+        const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        cuda_check(e, "cudaGraphInstantiate");
+        return ex;
+    }
+
+    // n steps of the bare (accu = false) or accu kernel pair, advancing the device
+    // step counter; graph replay for whole chunks.
+    void steps(bool accu, uint64_t n) {
+        uint64_t done = 0;
+        if (graphs && n >= kChunk) {
+            cudaGraphExec_t& ex = accu ? g_accu : g_bare;
+            if (accu && ex && g_accu_cap != means_cap) {
+                cudaGraphExecDestroy(ex);
+                ex = nullptr;
+            }
+            if (!ex) {
+                ex = capture_chunk(accu);
+                if (accu) g_accu_cap = means_cap;
+            }
+            for (; done + kChunk <= n; done += kChunk) {
+                cuda_check(cudaGraphLaunch(ex, ctx->stream), "cudaGraphLaunch");
+                bay::count_launches(2 * kChunk + 1);
+            }
+        }
+        const uint64_t rest = n - done;
+        for (uint32_t i = 0; i < rest; ++i) {
+            launch_half(accu, 0, i, ctx->stream);
+            launch_half(accu, 1, i, ctx->stream);
+        }
+        if (rest) {
+            bay_ctl_op op{};
+            op.mask = accu ? BAY_CTL_ADD_STEP1 : BAY_CTL_ADD_STEP0;
+            op.step[accu ? 1 : 0] = (uint32_t)rest;
+            ctl_op(op);
+        }
+        if (accu) step_accu += (uint32_t)n;
+        else step_bare += (uint32_t)n;
+    }
+
+    void set_a_beta(float a_, float beta_) {
+        a = a_;
+        beta = beta_;
+        bay_ctl_op op{};
+        op.mask = BAY_CTL_SET_A | BAY_CTL_SET_BETA;
+        op.a = a_;
+        op.beta = beta_;
+        ctl_op(op);
+    }
+
+    void ensure_means(uint64_t n) {
+        if (means_cap >= n && means) return;
+        ctx->release(means);
+        means = nullptr;
+        means_cap = 0;
+        means = (float*)ctx->alloc(sizeof(float) * (size_t)D * (size_t)std::max<uint64_t>(n, 1));
+        means_cap = n;
+    }
+
+    void require_positions() const {
+        if (!positioned)
+            fail(BAY_ERR_STATE, "the sampler has no walker positions: call init-position first");
+    }
+
+    void destroy_graphs() {
+        if (g_bare) cudaGraphExecDestroy(g_bare);
+        if (g_accu) cudaGraphExecDestroy(g_accu);
+        g_bare = g_accu = nullptr;
+    }
+};
+
+// ============================================================================ C ABI
+extern "C" {
+
+const char* bay_last_error(void) { return g_err.c_str(); }
+
+void bay_version(int* major, int* minor) {
+    if (major) *major = 0;
+    if (minor) *minor = 1;
+}
+
+int bay_ctx_create(const bay_ctx_opts* opts, bay_ctx** out) {
+    return guarded([&] {
+        if (!out) fail(BAY_ERR_ARG, "out is NULL");
+        *out = nullptr;
+        bay_ctx* c = new bay_ctx();
+        try {
+            c->device = opts ? opts->device : 0;
+            c->wgs = (opts && opts->wgs) ? opts->wgs : 1024u;
+            c->mem_limit = opts ? opts->mem_limit : 0;
+            if (c->wgs < 2 || c->wgs > 1024 || (c->wgs & (c->wgs - 1)))
+                fail(BAY_ERR_ARG, "wgs must be a power of two in [2, 1024]");
+            int n = 0;
+            cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+            if (c->device < 0 || c->device >= n) fail(BAY_ERR_ARG, "no such CUDA device");
+            c->use();
+            cuda_check(cudaFree(nullptr), "context init");
+            load_driver_api();
+            cuda_check(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount,
+                                              c->device),
+                       "cudaDeviceGetAttribute");
+            if (opts && opts->stream) {
+                c->stream = (cudaStream_t)opts->stream;
+            } else {
+                cuda_check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking),
+                           "cudaStreamCreate");
+                c->own_stream = true;
+            }
+            cuda_check(cudaStreamCreateWithFlags(&c->capture, cudaStreamNonBlocking),
+                       "cudaStreamCreate(capture)");
+        } catch (...) {
+            if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+            if (c->capture) cudaStreamDestroy(c->capture);
+            delete c;
+            throw;
+        }
+        *out = c;
+    });
+}
+
+int bay_ctx_release(bay_ctx* c) {
+    return guarded([&] {
+        if (!c) return;
+        c->use();
+        cudaStreamSynchronize(c->stream);
+        for (auto& kv : c->sizes) cudaFree(kv.first);
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        cudaStreamDestroy(c->capture);
+        delete c;
+    });
+}
+
+int bay_ctx_processing_elements(bay_ctx* c, uint64_t* out) {
+    return guarded([&] {
+        if (!c || !out) fail(BAY_ERR_ARG, "NULL argument");
+        *out = (uint64_t)c->sm_count * c->wgs;
+    });
+}
+
+int bay_ctx_stream(bay_ctx* c, void** s) {
+    return guarded([&] {
+        if (!c || !s) fail(BAY_ERR_ARG, "NULL argument");
+        *s = (void*)c->stream;
+    });
+}
+
+int bay_ctx_synchronize(bay_ctx* c) {
+    return guarded([&] {
+        if (!c) fail(BAY_ERR_ARG, "NULL context");
+        c->use();
+        cuda_check(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    });
+}
+
+int bay_launch_count(uint64_t* out) {
+    return guarded([&] {
+        if (!out) fail(BAY_ERR_ARG, "NULL argument");
+        *out = bay::launch_count();
+    });
+}
+
+int bay_ctx_allocated(bay_ctx* c, uint64_t* out) {
+    return guarded([&] {
+        if (!c || !out) fail(BAY_ERR_ARG, "NULL argument");
+        *out = c->allocated;
+    });
+}
+
+}  // extern "C"
+
+namespace {
+struct Codegen {
+    std::string src;
+    std::vector<std::string> opts;
+    uint32_t cta = 256, wpc = 1;
+};
+
+// Source and NVRTC options of a model's fused kernels (the reference's stretch-options,
+// nvidia_gtx.clj:630-633, retargeted to sm_103a).
+Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
+    if (!d) fail(BAY_ERR_ARG, "NULL model description");
+    if (!d->source) fail(BAY_ERR_ARG, "model source is NULL");
+    if (d->dim == 0 || d->dim > 4096) fail(BAY_ERR_ARG, "dim must be in [1, 4096]");
+    Codegen g;
+    uint32_t cta = d->cta_threads ? d->cta_threads : 256u;
+    if (cta % 32 || cta > 1024) fail(BAY_ERR_ARG, "cta_threads must be a multiple of 32, <= 1024");
+    std::vector<std::string>& opts = g.opts;
+    opts = {"-arch=sm_103a", "-use_fast_math", "-default-device", "-std=c++17", "-DREAL=float",
+            "-DREAL2=float2", "-DACCUMULATOR=float"};
+    opts.push_back("-DDIM=" + std::to_string(d->dim));
+    opts.push_back("-DWGS=" + std::to_string(wgs));
+    opts.push_back("-DBAY_CTA=" + std::to_string(cta));
+    opts.push_back(std::string("-DBAY_ACCEPT_REF=") +
+                   ((d->flags & BAY_MODEL_ACCEPT_REF) ? "1" : "0"));
+    uint32_t wpc = 1;
+    if (d->form == BAY_FORM_PLAIN) {
+        if (!valid_ident(d->logfn)) fail(BAY_ERR_ARG, "logfn must name a C function");
+        opts.push_back(std::string("-DBAY_LOGFN=") + d->logfn);
+    } else if (d->form == BAY_FORM_TILED) {
+        if (!valid_ident(d->tile_prep) || !valid_ident(d->tile_term) ||
+            !valid_ident(d->tile_walker))
+            fail(BAY_ERR_ARG, "tiled form needs tile_prep, tile_term and tile_walker names");
+        if (d->row_len == 0 || d->row_len > 64) fail(BAY_ERR_ARG, "row_len must be in [1, 64]");
+        const uint32_t pl = d->prep_len ? d->prep_len : 1u;
+        if (pl > 64) fail(BAY_ERR_ARG, "prep_len must be <= 64");
+        wpc = d->walkers_per_cta ? d->walkers_per_cta : 8u;
+        if (wpc > 32 || wpc > cta) fail(BAY_ERR_ARG, "walkers_per_cta must be <= 32 and <= cta_threads");
+        opts.push_back("-DBAY_TILED=1");
+        opts.push_back("-DBAY_ROW_LEN=" + std::to_string(d->row_len));
+        opts.push_back("-DBAY_PREP_LEN=" + std::to_string(pl));
+        opts.push_back("-DBAY_WPC=" + std::to_string(wpc));
+        opts.push_back(std::string("-DBAY_TILE_PREP=") + d->tile_prep);
+        opts.push_back(std::string("-DBAY_TILE_TERM=") + d->tile_term);
+        opts.push_back(std::string("-DBAY_TILE_WALKER=") + d->tile_walker);
+    } else {
+        fail(BAY_ERR_ARG, "unknown model form");
+    }
+    std::string& src = g.src;
+    src += "#include <stdint.h>\n";
+    src += bay_embedded_rng;
+    src += "\n#line 1 \"model\"\n";
+    src += d->source;
+    src += "\n#line 1 \"bay_stretch.cuh\"\n";
+    src += bay_embedded_stretch;
+    g.cta = cta;
+    g.wpc = wpc;
+    return g;
+}
+}  // namespace
+
+extern "C" {
+
+int bay_model_check(const bay_model_desc* d, uint32_t wgs) {
+    return guarded([&] {
+        Codegen g = codegen(d, wgs ? wgs : 1024u);
+        nvrtc_compile(g.src, g.opts);
+    });
+}
+
+int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
+    return guarded([&] {
+        if (!c || !d || !out) fail(BAY_ERR_ARG, "NULL argument");
+        *out = nullptr;
+        std::lock_guard<std::recursive_mutex> lk(c->mu);
+        c->use();
+        Codegen g = codegen(d, c->wgs);
+        std::vector<char> cubin = nvrtc_compile(g.src, g.opts);
+        bay_model* m = new bay_model();
+        m->ctx = c;
+        m->dim = d->dim;
+        m->params_size = d->params_size;
+        m->form = d->form;
+        m->cta = g.cta;
+        m->wpc = g.wpc;
+        m->flags = d->flags;
+        try {
+            cu_check(g_cu.LibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr,
+                                       nullptr, 0),
+                     "cuLibraryLoadData");
+            cu_check(g_cu.LibraryGetKernel(&m->k_bare, m->lib, "bay_stretch_bare"), "GetKernel(bare)");
+            cu_check(g_cu.LibraryGetKernel(&m->k_accu, m->lib, "bay_stretch_accu"), "GetKernel(accu)");
+            cu_check(g_cu.LibraryGetKernel(&m->k_logfn, m->lib, "bay_logfn_all"), "GetKernel(logfn)");
+        } catch (...) {
+            if (m->lib) g_cu.LibraryUnload(m->lib);
+            delete m;
+            throw;
+        }
+        *out = m;
+    });
+}
+
+int bay_model_release(bay_model* m) {
+    return guarded([&] {
+        if (!m) return;
+        if (m->lib) g_cu.LibraryUnload(m->lib);
+        delete m;
+    });
+}
+
+static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const float* params,
+                          uint64_t n_params, bool device_params, bay_sampler** out) {
+    return guarded([&] {
+        if (!m || !out) fail(BAY_ERR_ARG, "NULL argument");
+        *out = nullptr;
+        if (walkers < 4 || walkers % 2)
+            fail(BAY_ERR_ARG, "Number of walkers (" + std::to_string(walkers) +
+                                  ") must be even and at least 4.");
+        if (walkers > 0xffffffffull / 2) fail(BAY_ERR_ARG, "too many walkers");
+        if (n_params < m->params_size)
+            fail(BAY_ERR_ARG, "Dimension of params must match the distribution: need at least " +
+                                  std::to_string(m->params_size) + " values, got " +
+                                  std::to_string(n_params));
+        if (n_params && !params) fail(BAY_ERR_ARG, "params is NULL");
+        bay_ctx* c = m->ctx;
+        std::lock_guard<std::recursive_mutex> lk(c->mu);
+        c->use();
+        bay_sampler* s = new bay_sampler();
+        s->model = m;
+        s->ctx = c;
+        s->W = walkers;
+        s->K = walkers / 2;
+        s->D = m->dim;
+        s->n_params = n_params;
+        s->data_len = n_params - m->params_size;
+        try {
+            s->xs = (float*)c->alloc(sizeof(float) * (size_t)s->D * walkers);
+            s->logfn = (float*)c->alloc(sizeof(float) * walkers);
+            s->ctl = (bay_ctl*)c->alloc(sizeof(bay_ctl));
+            s->part = (double*)c->alloc(sizeof(double) * (size_t)s->grid() * s->D);
+            s->half_sum = (double*)c->alloc(sizeof(double) * s->D);
+            s->stats = (double*)c->alloc(sizeof(double) * 2 * s->D);
+            cuda_check(cudaMemsetAsync(s->ctl, 0, sizeof(bay_ctl), c->stream), "memset");
+            cuda_check(cudaMemsetAsync(s->xs, 0, sizeof(float) * (size_t)s->D * walkers, c->stream),
+                       "memset");
+            cuda_check(cudaMemsetAsync(s->logfn, 0, sizeof(float) * walkers, c->stream), "memset");
+            if (device_params) {
+                if ((uintptr_t)params % 16) fail(BAY_ERR_ARG, "d_params must be 16-byte aligned");
+                s->params = params;
+            } else {
+                float* p = (float*)c->alloc(sizeof(float) * std::max<uint64_t>(n_params, 1));
+                if (n_params)
+                    cuda_check(cudaMemcpyAsync(p, params, sizeof(float) * n_params,
+                                               cudaMemcpyHostToDevice, c->stream),
+                               "cudaMemcpy(params)");
+                s->params = p;
+                s->own_params = true;
+            }
+            s->ensure_means(1);
+            // init! (nvidia_gtx.clj:391-400)
+            s->seed_bare = seed;
+            s->seed_accu = seed;
+            bay_ctl_op op{};
+            op.mask = BAY_CTL_SET_STEP0 | BAY_CTL_SET_STEP1 | BAY_CTL_SET_SEED0 | BAY_CTL_SET_SEED1 |
+                      BAY_CTL_SET_A | BAY_CTL_SET_BETA | BAY_CTL_RESET_ACCEPTED |
+                      BAY_CTL_RESET_TICKETS;
+            op.seed[0] = seed;
+            op.seed[1] = seed;
+            op.a = 2.0f;
+            op.beta = 1.0f;
+            s->ctl_op(op);
+        } catch (...) {
+            c->release(s->xs);
+            c->release(s->logfn);
+            c->release(s->ctl);
+            c->release(s->part);
+            c->release(s->half_sum);
+            c->release(s->stats);
+            c->release(s->means);
+            if (s->own_params) c->release((void*)s->params);
+            delete s;
+            throw;
+        }
+        *out = s;
+    });
+}
+
+int bay_sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const float* params,
+                       uint64_t n_params, bay_sampler** out) {
+    return sampler_create(m, seed, walkers, params, n_params, false, out);
+}
+
+int bay_sampler_create_device(bay_model* m, uint32_t seed, uint64_t walkers, const float* d_params,
+                              uint64_t n_params, bay_sampler** out) {
+    return sampler_create(m, seed, walkers, d_params, n_params, true, out);
+}
+
+int bay_sampler_release(bay_sampler* s) {
+    return guarded([&] {
+        if (!s) return;
+        bay_ctx* c = s->ctx;
+        std::lock_guard<std::recursive_mutex> lk(c->mu);
+        c->use();
+        cudaStreamSynchronize(c->stream);
+        s->destroy_graphs();
+        c->release(s->xs);
+        c->release(s->logfn);
+        c->release(s->ctl);
+        c->release(s->part);
+        c->release(s->half_sum);
+        c->release(s->stats);
+        c->release(s->means);
+        c->release(s->stage);
+        c->release(s->hist);
+        c->release(s->counts);
+        if (s->own_params) c->release((void*)s->params);
+        delete s;
+    });
+}
+
+int bay_sampler_info_get(bay_sampler* s, bay_sampler_info* out) {
+    return guarded([&] {
+        if (!s || !out) fail(BAY_ERR_ARG, "NULL argument");
+        out->walkers = s->W;
+        out->dim = s->D;
+        out->wgs = s->ctx->wgs;
+        out->iteration_counter = s->iteration_counter;
+        out->data_len = s->data_len;
+    });
+}
+
+int bay_sampler_set_graphs(bay_sampler* s, int enabled) {
+    return guarded([&] {
+        if (!s) fail(BAY_ERR_ARG, "NULL sampler");
+        s->graphs = enabled != 0;
+    });
+}
+
+int bay_init(bay_sampler* s, uint32_t seed) {
+    return guarded([&] {
+        if (!s) fail(BAY_ERR_ARG, "NULL sampler");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->seed_bare = seed;
+        s->seed_accu = seed;
+        s->step_bare = 0;
+        s->a = 2.0f;
+        s->beta = 1.0f;
+        bay_ctl_op op{};
+        op.mask = BAY_CTL_SET_SEED0 | BAY_CTL_SET_SEED1 | BAY_CTL_SET_STEP0 | BAY_CTL_SET_A |
+                  BAY_CTL_SET_BETA;
+        op.seed[0] = seed;
+        op.seed[1] = seed;
+        op.a = 2.0f;
+        op.beta = 1.0f;
+        s->ctl_op(op);
+    });
+}
+
+int bay_init_position_limits(bay_sampler* s, uint32_t seed, const float* limits) {
+    return guarded([&] {
+        if (!s || !limits) fail(BAY_ERR_ARG, "NULL argument");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        float* dl = (float*)s->ctx->alloc(sizeof(float) * 2 * s->D);
+        try {
+            cuda_check(cudaMemcpyAsync(dl, limits, sizeof(float) * 2 * s->D, cudaMemcpyDefault,
+                                       s->ctx->stream),
+                       "cudaMemcpy(limits)");
+            cuda_check(bay::launch_init_uniform(s->xs, s->D, s->W, seed, dl, s->ctx->stream),
+                       "init_walkers");
+            s->launch_logfn_all();
+            cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+        } catch (...) {
+            s->ctx->release(dl);
+            throw;
+        }
+        s->ctx->release(dl);
+        s->positioned = true;
+        s->iteration_counter = 0;
+    });
+}
+
+int bay_init_position_normal(bay_sampler* s, uint32_t seed, float mean, float sd) {
+    return guarded([&] {
+        if (!s) fail(BAY_ERR_ARG, "NULL sampler");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        cuda_check(bay::launch_init_normal(s->xs, s->D, s->W, seed, mean, sd, s->ctx->stream),
+                   "init_normal");
+        s->launch_logfn_all();
+        s->positioned = true;
+        s->iteration_counter = 0;
+    });
+}
+
+int bay_init_position_copy(bay_sampler* s, const bay_sampler* src) {
+    return guarded([&] {
+        if (!s || !src) fail(BAY_ERR_ARG, "NULL argument");
+        if (src->D != s->D || src->W != s->W)
+            fail(BAY_ERR_ARG, "source sampler has a different dimension or walker count");
+        if (!src->positioned) fail(BAY_ERR_STATE, "source sampler has no positions");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        if (src->ctx != s->ctx) cuda_check(cudaStreamSynchronize(src->ctx->stream), "sync(src)");
+        cuda_check(cudaMemcpyAsync(s->xs, src->xs, sizeof(float) * (size_t)s->D * s->W,
+                                   cudaMemcpyDeviceToDevice, s->ctx->stream),
+                   "cudaMemcpy(positions)");
+        s->launch_logfn_all();
+        s->positioned = true;
+        s->iteration_counter = 0;
+    });
+}
+
+int bay_init_position_host(bay_sampler* s, const float* positions) {
+    return guarded([&] {
+        if (!s || !positions) fail(BAY_ERR_ARG, "NULL argument");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        if (!s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
+        cuda_check(cudaMemcpyAsync(s->stage, positions, sizeof(float) * (size_t)s->D * s->W,
+                                   cudaMemcpyDefault, s->ctx->stream),
+                   "cudaMemcpy(positions)");
+        cuda_check(bay::launch_aos_to_soa(s->stage, s->D, s->W, s->xs, s->ctx->stream), "aos_to_soa");
+        s->launch_logfn_all();
+        cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+        s->positioned = true;
+        s->iteration_counter = 0;
+    });
+}
+
+int bay_burn_in(bay_sampler* s, uint64_t n, float a) {
+    return guarded([&] {
+        if (!s) fail(BAY_ERR_ARG, "NULL sampler");
+        if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->require_positions();
+        s->set_a_beta(a, 1.0f);
+        s->steps(false, n);
+        s->iteration_counter += n;
+    });
+}
+
+int bay_anneal(bay_sampler* s, const float* temps, uint64_t n, float a) {
+    return guarded([&] {
+        if (!s || (n && !temps)) fail(BAY_ERR_ARG, "NULL argument");
+        if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->require_positions();
+        for (uint64_t i = 0; i < n; ++i) {
+            s->set_a_beta(a, (float)(1.0 / (double)temps[i]));
+            s->steps(false, 1);
+        }
+        s->iteration_counter += n;
+    });
+}
+
+namespace {
+// init-move! (nvidia_gtx.clj:340-350): accu seeds advance by 2, move counter and the
+// acceptance count restart.  Counts start at 0 (the OpenCL engine's choice; the CUDA
+// engine memsets them to 1 per block).
+void init_move(bay_sampler* s, float a) {
+    s->seed_accu += 2;
+    s->step_accu = 0;
+    s->a = a;
+    bay_ctl_op op{};
+    op.mask = BAY_CTL_SET_SEED1 | BAY_CTL_SET_STEP1 | BAY_CTL_SET_A | BAY_CTL_RESET_ACCEPTED |
+              BAY_CTL_RESET_TICKETS;
+    op.seed[1] = s->seed_accu;
+    op.a = a;
+    s->ctl_op(op);
+}
+
+uint64_t read_accepted(bay_sampler* s) {
+    unsigned long long v = 0;
+    cuda_check(cudaMemcpyAsync(&v, &s->ctl->accepted, sizeof(v), cudaMemcpyDeviceToHost,
+                               s->ctx->stream),
+               "cudaMemcpy(accepted)");
+    cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+    return v;
+}
+
+uint32_t acor_lag(uint64_t n, uint32_t wgs) {
+    uint64_t l = n / 5;
+    if (wgs < l) l = wgs;
+    if (64 < l) l = 64;
+    return (uint32_t)(l < 10 ? 10 : l);
+}
+
+// acor of a device-resident series; results to host or device arrays.
+int acor_device(bay_ctx* c, const float* d_series, uint32_t D, uint64_t n, double* tau,
+                double* mean, double* sigma, uint32_t* lag_out) {
+    const uint32_t lag = acor_lag(n, c->wgs);
+    if (lag_out) *lag_out = lag;
+    if ((uint64_t)lag * 5 > n) {
+        g_err = "The autocorrelation time is too long relative to the variance. Number of steps (" +
+                std::to_string(n) + ") must not be less than " + std::to_string(lag * 5) + ".";
+        return BAY_ERR_ARG;
+    }
+    if (n > 0xffffffffull) fail(BAY_ERR_ARG, "series too long");
+    double* work = (double*)c->alloc(sizeof(double) * ((size_t)D * n + 3 * D));
+    try {
+        double* res = work + (size_t)D * n;
+        cuda_check(bay::launch_acor(d_series, D, (uint32_t)n, c->wgs, lag, work, res, res + D,
+                                    res + 2 * D, c->stream),
+                   "acor");
+        if (tau) cuda_check(cudaMemcpyAsync(tau, res, sizeof(double) * D, cudaMemcpyDefault, c->stream), "copy");
+        if (mean) cuda_check(cudaMemcpyAsync(mean, res + D, sizeof(double) * D, cudaMemcpyDefault, c->stream), "copy");
+        if (sigma) cuda_check(cudaMemcpyAsync(sigma, res + 2 * D, sizeof(double) * D, cudaMemcpyDefault, c->stream), "copy");
+        cuda_check(cudaStreamSynchronize(c->stream), "sync");
+    } catch (...) {
+        c->release(work);
+        throw;
+    }
+    c->release(work);
+    return BAY_OK;
+}
+}  // namespace
+
+int bay_acc_rate(bay_sampler* s, float a, double* rate) {
+    return guarded([&] {
+        if (!s || !rate) fail(BAY_ERR_ARG, "NULL argument");
+        if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->require_positions();
+        init_move(s, a);
+        const uint64_t cap = s->means_cap;
+        s->means_cap = 0;  // no per-step means for a single acceptance probe
+        try {
+            s->steps(true, 1);
+        } catch (...) {
+            s->means_cap = cap;
+            throw;
+        }
+        s->means_cap = cap;
+        s->iteration_counter += 1;
+        *rate = (double)read_accepted(s) / (double)s->W;
+    });
+}
+
+int bay_run_sampler(bay_sampler* s, uint64_t n, float a, bay_run_result* res, double* tau,
+                    double* mean, double* sigma, float* means_out) {
+    return guarded([&] {
+        if (!s || !res) fail(BAY_ERR_ARG, "NULL argument");
+        if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
+        if (n == 0 || n > 0xffffffffull) fail(BAY_ERR_ARG, "steps must be in [1, 2^32)");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->require_positions();
+        s->ensure_means(n);
+        init_move(s, a);
+        s->steps(true, n);
+        s->iteration_counter += n;
+        const uint64_t acc = read_accepted(s);
+        res->acceptance_rate = (double)acc / ((double)s->W * (double)n);
+        res->a = a;
+        res->steps = n;
+        if (means_out)
+            cuda_check(cudaMemcpyAsync(means_out, s->means, sizeof(float) * (size_t)s->D * n,
+                                       cudaMemcpyDefault, s->ctx->stream),
+                       "cudaMemcpy(means)");
+        uint32_t lag = 0;
+        const std::string keep = g_err;
+        res->acor_status = acor_device(s->ctx, s->means, s->D, n, tau, mean, sigma, &lag);
+        if (res->acor_status == BAY_OK) g_err = keep;
+        res->lag = lag;
+        cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+    });
+}
+
+int bay_sample(bay_sampler* s, uint64_t n_cols, float* out) {
+    return guarded([&] {
+        if (!s || (n_cols && !out)) fail(BAY_ERR_ARG, "NULL argument");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->require_positions();
+        const bool dev = is_device_ptr(out);
+        if (!dev && !s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
+        s->set_a_beta(s->a, 1.0f);
+        uint64_t ofs = 0;
+        while (ofs < n_cols) {
+            s->steps(false, 1);
+            s->iteration_counter += 1;
+            const uint64_t take = std::min<uint64_t>(s->W, n_cols - ofs);
+            float* dst = dev ? out + ofs * s->D : s->stage;
+            cuda_check(bay::launch_soa_to_aos(s->xs, s->D, s->W, 0, take, dst, s->ctx->stream),
+                       "soa_to_aos");
+            if (!dev)
+                cuda_check(cudaMemcpyAsync(out + ofs * s->D, s->stage, sizeof(float) * take * s->D,
+                                           cudaMemcpyDeviceToHost, s->ctx->stream),
+                           "cudaMemcpy(sample)");
+            if (!dev) cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+            ofs += take;
+        }
+        cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+    });
+}
+
+static int moments_out(bay_sampler* s, double* out, int which) {
+    return guarded([&] {
+        if (!s || !out) fail(BAY_ERR_ARG, "NULL argument");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->require_positions();
+        cuda_check(bay::launch_moments(s->xs, s->D, s->W, s->stats, s->stats + s->D, s->ctx->stream),
+                   "moments");
+        cuda_check(cudaMemcpyAsync(out, s->stats + (which ? s->D : 0), sizeof(double) * s->D,
+                                   cudaMemcpyDefault, s->ctx->stream),
+                   "cudaMemcpy(moments)");
+        cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+        if (which == 2 && !is_device_ptr(out))
+            for (uint32_t d = 0; d < s->D; ++d) out[d] = std::sqrt(out[d]);
+    });
+}
+
+int bay_mean(bay_sampler* s, double* out) { return moments_out(s, out, 0); }
+int bay_variance(bay_sampler* s, double* out) { return moments_out(s, out, 1); }
+int bay_sd(bay_sampler* s, double* out) {
+    if (out && is_device_ptr(out)) {
+        g_err = "bay_sd writes host memory only";
+        return BAY_ERR_ARG;
+    }
+    return moments_out(s, out, 2);
+}
+
+int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags, float* limits,
+                  float* pdf, float* ranks) {
+    return guarded([&] {
+        if (!s || !limits || !pdf || !ranks) fail(BAY_ERR_ARG, "NULL argument");
+        if (cycles == 0) fail(BAY_ERR_ARG, "cycles must be >= 1");
+        if (bins == 0) bins = s->ctx->wgs;
+        if (bins < 2 || bins > 1024 || (bins & (bins - 1)))
+            fail(BAY_ERR_ARG, "bins must be a power of two in [2, 1024]");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        bay_ctx* c = s->ctx;
+        c->use();
+        s->require_positions();
+        if (s->hist_bins < bins) {
+            c->release(s->hist);
+            c->release(s->counts);
+            s->hist = nullptr;
+            s->counts = nullptr;
+            s->hist = (float*)c->alloc(sizeof(float) * (2 * (size_t)s->D + 2 * (size_t)bins * s->D));
+            s->counts = (uint32_t*)c->alloc(sizeof(uint32_t) * (size_t)bins * s->D);
+            s->hist_bins = bins;
+        }
+        float* d_lim = s->hist;
+        float* d_pdf = d_lim + 2 * s->D;
+        float* d_rank = d_pdf + (size_t)bins * s->D;
+        // Q7: the reference's min/max reduction folds 0.0 in when a level has a partial
+        // block; wgsn = WGS / min(dim, sqrt(WGS)) (nvidia_gtx.clj:486-488).
+        int zero = 0;
+        if (flags & BAY_HIST_COMPAT_ZERO_LIMITS) {
+            uint64_t sq = (uint64_t)std::sqrt((double)c->wgs);
+            uint64_t wgsm = std::min<uint64_t>(s->D, sq);
+            if (!wgsm) wgsm = 1;
+            const uint64_t wgsn = c->wgs / wgsm;
+            uint64_t cnt = s->W;
+            do {
+                const uint64_t B = std::min(cnt, wgsn);
+                if (cnt % B) zero = 1;
+                cnt = (cnt + B - 1) / B;
+            } while (cnt > 1);
+        }
+        cuda_check(bay::launch_minmax(s->xs, s->D, s->W, zero, d_lim, c->stream), "minmax");
+        cuda_check(bay::launch_fill_u32(s->counts, (flags & BAY_HIST_COMPAT_START1) ? 1u : 0u,
+                                        (uint64_t)bins * s->D, c->stream),
+                   "fill");
+        cuda_check(bay::launch_hist_count(s->xs, s->D, s->W, bins, d_lim, s->counts, c->stream),
+                   "histogram");
+        if (cycles > 1) {
+            s->set_a_beta(s->a, 1.0f);
+            for (uint32_t i = 1; i < cycles; ++i) {
+                s->steps(false, 1);
+                cuda_check(bay::launch_hist_count(s->xs, s->D, s->W, bins, d_lim, s->counts,
+                                                  c->stream),
+                           "histogram");
+            }
+            s->iteration_counter += cycles - 1;
+        }
+        cuda_check(bay::launch_hist_finish(s->counts, d_lim, s->D, bins, (uint64_t)cycles * s->W,
+                                           d_pdf, d_rank, c->stream),
+                   "hist_finish");
+        cuda_check(cudaMemcpyAsync(limits, d_lim, sizeof(float) * 2 * s->D, cudaMemcpyDefault, c->stream), "copy");
+        cuda_check(cudaMemcpyAsync(pdf, d_pdf, sizeof(float) * bins * s->D, cudaMemcpyDefault, c->stream), "copy");
+        cuda_check(cudaMemcpyAsync(ranks, d_rank, sizeof(float) * bins * s->D, cudaMemcpyDefault, c->stream), "copy");
+        cuda_check(cudaStreamSynchronize(c->stream), "sync");
+    });
+}
+
+int bay_acor(bay_ctx* c, const float* series, uint32_t D, uint64_t n, double* tau, double* mean,
+             double* sigma, uint32_t* lag) {
+    int rc = BAY_OK;
+    const int g = guarded([&] {
+        if (!c || !series) fail(BAY_ERR_ARG, "NULL argument");
+        if (D == 0) fail(BAY_ERR_ARG, "dim must be >= 1");
+        std::lock_guard<std::recursive_mutex> lk(c->mu);
+        c->use();
+        if (is_device_ptr(series)) {
+            rc = acor_device(c, series, D, n, tau, mean, sigma, lag);
+            return;
+        }
+        float* d = (float*)c->alloc(sizeof(float) * (size_t)D * std::max<uint64_t>(n, 1));
+        try {
+            cuda_check(cudaMemcpyAsync(d, series, sizeof(float) * (size_t)D * n,
+                                       cudaMemcpyHostToDevice, c->stream),
+                       "cudaMemcpy(series)");
+            rc = acor_device(c, d, D, n, tau, mean, sigma, lag);
+        } catch (...) {
+            c->release(d);
+            throw;
+        }
+        c->release(d);
+    });
+    return g != BAY_OK ? g : rc;
+}
+
+int bay_state_export(bay_sampler* s, float* positions, float* logfn, uint32_t* rng) {
+    return guarded([&] {
+        if (!s) fail(BAY_ERR_ARG, "NULL sampler");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        s->require_positions();
+        if (positions) {
+            if (!s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
+            cuda_check(bay::launch_soa_to_aos(s->xs, s->D, s->W, 0, s->W, s->stage, s->ctx->stream),
+                       "soa_to_aos");
+            cuda_check(cudaMemcpyAsync(positions, s->stage, sizeof(float) * (size_t)s->D * s->W,
+                                       cudaMemcpyDefault, s->ctx->stream),
+                       "copy");
+        }
+        if (logfn)
+            cuda_check(cudaMemcpyAsync(logfn, s->logfn, sizeof(float) * s->W, cudaMemcpyDefault,
+                                       s->ctx->stream),
+                       "copy");
+        if (rng) {
+            rng[0] = s->seed_bare;
+            rng[1] = s->seed_accu;
+            rng[2] = s->step_bare;
+            rng[3] = s->step_accu;
+            rng[4] = (uint32_t)s->iteration_counter;
+            rng[5] = (uint32_t)(s->iteration_counter >> 32);
+            std::memcpy(&rng[6], &s->a, 4);
+            std::memcpy(&rng[7], &s->beta, 4);
+        }
+        cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+    });
+}
+
+int bay_state_import(bay_sampler* s, const float* positions, const float* logfn,
+                     const uint32_t* rng) {
+    return guarded([&] {
+        if (!s || !positions || !logfn || !rng) fail(BAY_ERR_ARG, "NULL argument");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        if (!s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
+        cuda_check(cudaMemcpyAsync(s->stage, positions, sizeof(float) * (size_t)s->D * s->W,
+                                   cudaMemcpyDefault, s->ctx->stream),
+                   "copy");
+        cuda_check(bay::launch_aos_to_soa(s->stage, s->D, s->W, s->xs, s->ctx->stream), "aos_to_soa");
+        cuda_check(cudaMemcpyAsync(s->logfn, logfn, sizeof(float) * s->W, cudaMemcpyDefault,
+                                   s->ctx->stream),
+                   "copy");
+        s->seed_bare = rng[0];
+        s->seed_accu = rng[1];
+        s->step_bare = rng[2];
+        s->step_accu = rng[3];
+        s->iteration_counter = (uint64_t)rng[4] | ((uint64_t)rng[5] << 32);
+        std::memcpy(&s->a, &rng[6], 4);
+        std::memcpy(&s->beta, &rng[7], 4);
+        bay_ctl_op op{};
+        op.mask = BAY_CTL_SET_SEED0 | BAY_CTL_SET_SEED1 | BAY_CTL_SET_STEP0 | BAY_CTL_SET_STEP1 |
+                  BAY_CTL_SET_A | BAY_CTL_SET_BETA | BAY_CTL_RESET_TICKETS;
+        op.seed[0] = s->seed_bare;
+        op.seed[1] = s->seed_accu;
+        op.step[0] = s->step_bare;
+        op.step[1] = s->step_accu;
+        op.a = s->a;
+        op.beta = s->beta;
+        s->ctl_op(op);
+        cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+        s->positioned = true;
+    });
+}
+
+int bay_logfn_values(bay_sampler* s, float* out) {
+    return guarded([&] {
+        if (!s || !out) fail(BAY_ERR_ARG, "NULL argument");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        cuda_check(cudaMemcpyAsync(out, s->logfn, sizeof(float) * s->W, cudaMemcpyDefault,
+                                   s->ctx->stream),
+                   "copy");
+        cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+    });
+}
+
+}  // extern "C"

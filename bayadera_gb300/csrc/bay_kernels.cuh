@@ -1,0 +1,94 @@
+// bay_kernels.cuh -- host-visible declarations of the nvcc-compiled kernels of
+// libbayadera_gb300.so (everything except the per-model fused stretch kernels,
+// which NVRTC builds at model-compile time from device/bay_stretch.cuh).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+// Must match struct bay_ctl in device/bay_stretch.cuh (the NVRTC side).
+struct bay_ctl {
+    unsigned int step[2];
+    unsigned int seed[2];
+    float a;
+    float beta;
+    unsigned int ticket[2];
+    unsigned long long accepted;
+    unsigned int status;
+    unsigned int pad;
+};
+
+// Must match struct bay_stretch_params in device/bay_stretch.cuh.
+struct bay_stretch_params {
+    const float* params;
+    float* xs;
+    float* logfn;
+    bay_ctl* ctl;
+    double* part;
+    double* half_sum;
+    float* means;
+    unsigned long long data_len;
+    unsigned int params_len;
+    unsigned int W, K;
+    unsigned int half;
+    unsigned int step_off;
+    unsigned int means_cap;
+    float inv_W;
+};
+
+enum {
+    BAY_CTL_SET_STEP0 = 1u << 0,
+    BAY_CTL_SET_STEP1 = 1u << 1,
+    BAY_CTL_SET_SEED0 = 1u << 2,
+    BAY_CTL_SET_SEED1 = 1u << 3,
+    BAY_CTL_SET_A = 1u << 4,
+    BAY_CTL_SET_BETA = 1u << 5,
+    BAY_CTL_ADD_STEP0 = 1u << 6,
+    BAY_CTL_ADD_STEP1 = 1u << 7,
+    BAY_CTL_RESET_ACCEPTED = 1u << 8,
+    BAY_CTL_RESET_TICKETS = 1u << 9,
+};
+
+struct bay_ctl_op {
+    unsigned int mask;
+    unsigned int step[2];
+    unsigned int seed[2];
+    float a;
+    float beta;
+};
+
+namespace bay {
+
+cudaError_t launch_ctl_apply(bay_ctl* ctl, const bay_ctl_op& op, cudaStream_t s);
+cudaError_t launch_init_uniform(float* xs, uint32_t D, uint64_t W, uint32_t seed,
+                                const float* limits, cudaStream_t s);
+cudaError_t launch_init_normal(float* xs, uint32_t D, uint64_t W, uint32_t seed, float mean,
+                               float sd, cudaStream_t s);
+// SoA xs[d*W + w] <-> AoS out[w*D + d] (dim x W column-major), for walkers [w0, w0+n).
+cudaError_t launch_soa_to_aos(const float* xs, uint32_t D, uint64_t W, uint64_t w0, uint64_t n,
+                              float* out, cudaStream_t s);
+cudaError_t launch_aos_to_soa(const float* in, uint32_t D, uint64_t W, float* xs, cudaStream_t s);
+// FP64 per-dim mean and population variance over W walkers (two passes per dim).
+cudaError_t launch_moments(const float* xs, uint32_t D, uint64_t W, double* mean, double* var,
+                           cudaStream_t s);
+// Per-dim [min, max] into limits[2*d], [2*d+1]; zero_fold folds 0.0 in (reference Q7).
+cudaError_t launch_minmax(const float* xs, uint32_t D, uint64_t W, int zero_fold, float* limits,
+                          cudaStream_t s);
+// counts[d*bins + b] += bin counts of the walkers (bins <= 4096).
+cudaError_t launch_hist_count(const float* xs, uint32_t D, uint64_t W, uint32_t bins,
+                              const float* limits, uint32_t* counts, cudaStream_t s);
+// pdf = (bins/n)/(hi-lo) * count, then bitonic ranks (bins a power of two <= 1024).
+cudaError_t launch_hist_finish(const uint32_t* counts, const float* limits, uint32_t D,
+                               uint32_t bins, uint64_t n, float* pdf, float* ranks,
+                               cudaStream_t s);
+cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, uint64_t n, cudaStream_t s);
+// acor of a D x n column-major series (series[t*D + d]); work holds D*n doubles.
+cudaError_t launch_acor(const float* series, uint32_t D, uint32_t n, uint32_t wgs, uint32_t lag,
+                        double* work, double* tau, double* mean, double* sigma, cudaStream_t s);
+// Kernels enqueued through this library in this process (graph nodes counted at replay).
+unsigned long long launch_count();
+void count_launches(unsigned long long n);
+// Flush: write n bytes (used by the bench between timed iterations).
+cudaError_t launch_fill_bytes(void* p, uint64_t n, unsigned char v, cudaStream_t s);
+
+}  // namespace bay

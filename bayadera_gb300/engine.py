@@ -1,0 +1,320 @@
+"""GB300 engine objects over the C ABI (mirrors internal/device/nvidia_gtx.clj).
+
+GB300BayaderaFactory  <- GTXBayaderaFactory (nvidia_gtx.clj:761-807)
+GB300StretchFactory   <- GTXStretchFactory  (nvidia_gtx.clj:543-610)
+GB300Stretch          <- GTXStretch         (nvidia_gtx.clj:282-541)
+GB300AcorEngine       <- GTXAcorEngine      (nvidia_gtx.clj:230-278)
+
+Host arrays are numpy; positions are dim x walkers (column-major in memory, i.e.
+a (walkers, dim) C-contiguous numpy array viewed transposed), as in the reference.
+"""
+import ctypes as C
+from collections import namedtuple
+
+import numpy as np
+
+from . import _native as N
+
+Histogram = namedtuple("Histogram", ["limits", "pdf", "bin_ranks"])
+Autocorrelation = namedtuple("Autocorrelation", ["tau", "mean", "sigma", "steps", "lag"])
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def _dev_ptr(t):
+    """Device pointer of an object with data_ptr() (a CUDA tensor), else None."""
+    dp = getattr(t, "data_ptr", None)
+    if dp is not None and getattr(getattr(t, "device", None), "type", "cpu") == "cuda":
+        return C.c_void_p(dp())
+    return None
+
+
+class GB300AcorEngine:
+    def __init__(self, factory):
+        self.factory = factory
+
+    def acor(self, data_matrix):
+        """AcorEngine/acor on a dim x n matrix (numpy (dim, n) array)."""
+        m = np.asarray(data_matrix, np.float32)
+        if m.ndim == 1:
+            m = m[None, :]
+        dim, n = m.shape
+        series = np.ascontiguousarray(m.T)  # column-major dim x n
+        tau = np.zeros(dim)
+        mean = np.zeros(dim)
+        sigma = np.zeros(dim)
+        lag = C.c_uint32(0)
+        N.call("bay_acor", self.factory.ctx, _ptr(series), dim, n, _ptr(tau), _ptr(mean),
+               _ptr(sigma), C.byref(lag))
+        return Autocorrelation(tau, mean, sigma, n, lag.value)
+
+
+class GB300BayaderaFactory:
+    """Context: one device, one stream, the reference's WGS."""
+
+    def __init__(self, device=0, wgs=1024, stream=None, mem_limit=0):
+        opts = N.CtxOpts(device, wgs, stream, mem_limit)
+        h = C.c_void_p()
+        N.call("bay_ctx_create", C.byref(opts), C.byref(h))
+        self.ctx = h
+        self.wgs = wgs
+        self.acor_engine = GB300AcorEngine(self)
+
+    def release(self):
+        if self.ctx:
+            N.call("bay_ctx_release", self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.release()
+
+    def processing_elements(self):
+        v = C.c_uint64()
+        N.call("bay_ctx_processing_elements", self.ctx, C.byref(v))
+        return v.value
+
+    def stream(self):
+        s = C.c_void_p()
+        N.call("bay_ctx_stream", self.ctx, C.byref(s))
+        return s.value
+
+    def synchronize(self):
+        N.call("bay_ctx_synchronize", self.ctx)
+
+    def allocated(self):
+        v = C.c_uint64()
+        N.call("bay_ctx_allocated", self.ctx, C.byref(v))
+        return v.value
+
+    def mcmc_factory(self, model, form=None, accept_ref=False, walkers_per_cta=0,
+                     cta_threads=0):
+        """EngineFactory/mcmc-factory: compile the model's fused stretch kernels."""
+        return GB300StretchFactory(self, model, form, accept_ref, walkers_per_cta, cta_threads)
+
+    def acor(self, data_matrix):
+        return self.acor_engine.acor(data_matrix)
+
+
+def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0):
+    """bay_model_desc of a DeviceDistributionModel; form 'plain' | 'tiled' | None (tiled
+    when the model has a tiled form)."""
+    if form is None:
+        form = "tiled" if model.tiled else "plain"
+    keep = []
+
+    def b(s):
+        v = s.encode() if s is not None else None
+        keep.append(v)
+        return v
+
+    d = N.ModelDesc()
+    d.source = b(model.full_source())
+    d.logfn = b(model.mcmc_logpdf)
+    d.dim = model.dimension
+    d.params_size = model.params_size
+    d.flags = N.MODEL_ACCEPT_REF if accept_ref else 0
+    d.cta_threads = cta_threads
+    if form == "tiled":
+        t = model.tiled
+        if not t:
+            raise ValueError("model %s has no tiled form" % model.name)
+        d.form = N.FORM_TILED
+        d.tile_prep = b(t["prep"])
+        d.tile_term = b(t["term"])
+        d.tile_walker = b(t["walker"])
+        d.row_len = t["row_len"]
+        d.prep_len = t["prep_len"]
+        d.walkers_per_cta = walkers_per_cta
+    else:
+        d.form = N.FORM_PLAIN
+    return d, keep
+
+
+def check_model(model, form=None, wgs=1024, accept_ref=False):
+    """Compile-check a model's fused kernels with NVRTC (no device needed)."""
+    d, keep = model_desc(model, form, accept_ref)
+    N.call("bay_model_check", C.byref(d), wgs)
+
+
+class GB300StretchFactory:
+    def __init__(self, factory, model, form=None, accept_ref=False, walkers_per_cta=0,
+                 cta_threads=0):
+        self.factory = factory
+        self.model = model
+        d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads)
+        h = C.c_void_p()
+        N.call("bay_model_compile", factory.ctx, C.byref(d), C.byref(h))
+        self.handle = h
+
+    def release(self):
+        if self.handle:
+            N.call("bay_model_release", self.handle)
+            self.handle = None
+
+    def create_sampler(self, seed, walkers, params):
+        """SamplerFactory/create-sampler: params = data || hyperparameters (numpy, or a
+        CUDA tensor that stays resident and must outlive the sampler)."""
+        return GB300Stretch(self, seed, walkers, params)
+
+
+class GB300Stretch:
+    def __init__(self, sfactory, seed, walkers, params):
+        self.sfactory = sfactory
+        self.model = sfactory.model
+        self.dim = self.model.dimension
+        self.walkers = int(walkers)
+        h = C.c_void_p()
+        dp = _dev_ptr(params)
+        if dp is not None:
+            self._params_ref = params
+            N.call("bay_sampler_create_device", sfactory.handle, seed & 0xffffffff, self.walkers,
+                   dp, int(params.numel()), C.byref(h))
+        else:
+            p = np.ascontiguousarray(params, np.float32).reshape(-1)
+            N.call("bay_sampler_create", sfactory.handle, seed & 0xffffffff, self.walkers, _ptr(p),
+                   p.size, C.byref(h))
+        self.handle = h
+
+    def release(self):
+        if self.handle:
+            N.call("bay_sampler_release", self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.release()
+
+    def info(self):
+        i = N.SamplerInfo()
+        N.call("bay_sampler_info_get", self.handle, C.byref(i))
+        return {"walker_count": i.walkers, "iteration_counter": i.iteration_counter,
+                "dimension": i.dim, "data_len": i.data_len}
+
+    def set_graphs(self, enabled):
+        N.call("bay_sampler_set_graphs", self.handle, 1 if enabled else 0)
+
+    # ---------------------------------------------------------------- MCMC
+    def init(self, seed):
+        N.call("bay_init", self.handle, seed & 0xffffffff)
+        return self
+
+    def init_position(self, seed_or_position, limits=None):
+        if isinstance(seed_or_position, GB300Stretch):
+            N.call("bay_init_position_copy", self.handle, seed_or_position.handle)
+        elif limits is None:
+            pos = np.ascontiguousarray(seed_or_position, np.float32)
+            if pos.shape != (self.walkers, self.dim) and pos.size != self.walkers * self.dim:
+                raise ValueError("positions must hold walkers x dim values")
+            N.call("bay_init_position_host", self.handle, _ptr(pos))
+        else:
+            lim = np.ascontiguousarray(limits, np.float32).reshape(-1)
+            if lim.size != 2 * self.dim:
+                raise ValueError("limits must be a 2 x dim matrix")
+            N.call("bay_init_position_limits", self.handle, seed_or_position & 0xffffffff,
+                   _ptr(lim))
+        return self
+
+    def init_position_normal(self, seed, mean=0.0, sd=1.0):
+        N.call("bay_init_position_normal", self.handle, seed & 0xffffffff, mean, sd)
+        return self
+
+    def burn_in(self, n, a):
+        N.call("bay_burn_in", self.handle, int(n), float(a))
+        return self
+
+    def anneal(self, schedule, n, a):
+        temps = np.array([schedule(i) for i in range(int(n))], np.float32)
+        N.call("bay_anneal", self.handle, _ptr(temps), int(n), float(a))
+        return self
+
+    def acc_rate(self, a):
+        r = C.c_double()
+        N.call("bay_acc_rate", self.handle, float(a), C.byref(r))
+        return r.value
+
+    def run_sampler(self, n, a, return_means=False):
+        res = N.RunResult()
+        tau = np.zeros(self.dim)
+        mean = np.zeros(self.dim)
+        sigma = np.zeros(self.dim)
+        means = np.zeros((int(n), self.dim), np.float32) if return_means else None
+        N.call("bay_run_sampler", self.handle, int(n), float(a), C.byref(res), _ptr(tau),
+               _ptr(mean), _ptr(sigma), _ptr(means) if means is not None else None)
+        out = {"acceptance_rate": res.acceptance_rate, "a": res.a}
+        if res.acor_status == N.BAY_OK:
+            out["autocorrelation"] = Autocorrelation(tau, mean, sigma, int(n), res.lag)
+        else:
+            out["autocorrelation"] = None
+            out["autocorrelation_error"] = N.last_error()
+        if means is not None:
+            out["means"] = means.T
+        return out
+
+    # ---------------------------------------------------------------- sampling
+    def sample(self, n=None):
+        """sample!: dim x n matrix of positions (numpy (dim, n) view of (n, dim))."""
+        n = self.walkers if n is None else int(n)
+        out = np.zeros((n, self.dim), np.float32)
+        N.call("bay_sample", self.handle, n, _ptr(out))
+        return out.T
+
+    def sample_into(self, out):
+        """sample! into a CUDA tensor of shape (n, dim) (device-resident output)."""
+        N.call("bay_sample", self.handle, out.shape[0], C.c_void_p(out.data_ptr()))
+        return out
+
+    def positions(self):
+        out = np.zeros((self.walkers, self.dim), np.float32)
+        N.call("bay_state_export", self.handle, _ptr(out), None, None)
+        return out.T
+
+    def logfn(self):
+        out = np.zeros(self.walkers, np.float32)
+        N.call("bay_logfn_values", self.handle, _ptr(out))
+        return out
+
+    def export_state(self):
+        pos = np.zeros((self.walkers, self.dim), np.float32)
+        lf = np.zeros(self.walkers, np.float32)
+        rng = np.zeros(8, np.uint32)
+        N.call("bay_state_export", self.handle, _ptr(pos), _ptr(lf), _ptr(rng))
+        return pos, lf, rng
+
+    def import_state(self, pos, lf, rng):
+        pos = np.ascontiguousarray(pos, np.float32)
+        lf = np.ascontiguousarray(lf, np.float32)
+        rng = np.ascontiguousarray(rng, np.uint32)
+        N.call("bay_state_import", self.handle, _ptr(pos), _ptr(lf), _ptr(rng))
+        return self
+
+    # ---------------------------------------------------------------- estimates
+    def mean(self):
+        out = np.zeros(self.dim)
+        N.call("bay_mean", self.handle, _ptr(out))
+        return out
+
+    def variance(self):
+        out = np.zeros(self.dim)
+        N.call("bay_variance", self.handle, _ptr(out))
+        return out
+
+    def sd(self):
+        out = np.zeros(self.dim)
+        N.call("bay_sd", self.handle, _ptr(out))
+        return out
+
+    def histogram(self, cycles=1, bins=0, flags=0):
+        bins = bins or self.sfactory.factory.wgs
+        limits = np.zeros((self.dim, 2), np.float32)
+        pdf = np.zeros((self.dim, bins), np.float32)
+        ranks = np.zeros((self.dim, bins), np.float32)
+        N.call("bay_histogram", self.handle, int(cycles), int(bins), int(flags), _ptr(limits),
+               _ptr(pdf), _ptr(ranks))
+        return Histogram(limits.T, pdf.T, ranks.T)

@@ -1,0 +1,222 @@
+"""Device models and their C sources (mirrors internal/device/models.clj).
+
+A distribution model carries its C source, the name of its log density (and the
+MCMC variant without the normalising constant), its dimension, the number of
+hyperparameters and default limits; a likelihood model carries a source and the
+name of its loglik.  device_posterior_model composes a prior and a likelihood into
+a new distribution model by generating the posterior's C function
+(models.clj:102-115; the template is cuda/distributions/posterior.cu:5-10):
+
+    post(data_len, hyper_len, params, dim, x) =
+        loglik(data_len, params, dim, x)
+      + prior_logpdf(data_len, hyper_len, &params[data_len], dim, x)
+
+so the posterior's params are data || prior hyperparameters.
+"""
+import itertools
+import os
+
+import numpy as np
+
+LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "library")
+
+_counter = itertools.count()
+
+FLOAT_MAX = float(np.finfo(np.float32).max)
+FLOAT_MIN = float(np.finfo(np.float32).tiny)
+
+
+def _gensym(prefix):
+    return "%s%d" % (prefix, next(_counter))
+
+
+def source_library():
+    """name -> C source of the built-in model library (csrc/library/*.h)."""
+    out = {}
+    for fn in sorted(os.listdir(LIB_DIR)):
+        if fn.endswith(".h"):
+            with open(os.path.join(LIB_DIR, fn)) as f:
+                out[fn[:-2]] = f.read()
+    return out
+
+
+_SOURCES = None
+
+
+def get_source(name):
+    global _SOURCES
+    if _SOURCES is None:
+        _SOURCES = source_library()
+    return _SOURCES[name]
+
+
+class DeviceLikelihoodModel:
+    """DeviceLikelihoodModel (models.clj:25-51)."""
+
+    def __init__(self, name, loglik, source, dialect="c99"):
+        self.name = name
+        self.loglik = loglik
+        self.sources = list(source) if isinstance(source, (list, tuple)) else [source]
+        self.dialect = dialect
+
+    def source(self):
+        return self.sources
+
+
+class DeviceDistributionModel:
+    """DeviceDistributionModel (models.clj:57-100).
+
+    tiled: optional dict with keys prep, term, walker, row_len, prep_len
+    (the data-tiled form of the same density, see include/bayadera_gb300.h).
+    """
+
+    def __init__(self, name, logpdf, mcmc_logpdf, dimension, params_size, limits, source,
+                 dialect="c99", tiled=None):
+        self.name = name
+        self.logpdf = logpdf
+        self.mcmc_logpdf = mcmc_logpdf
+        self.dimension = int(dimension)
+        self.params_size = int(params_size)
+        self.limits = None if limits is None else np.asarray(limits, np.float32).reshape(-1)
+        self.sources = list(source) if isinstance(source, (list, tuple)) else [source]
+        self.dialect = dialect
+        self.tiled = tiled
+
+    def source(self):
+        return self.sources
+
+    def full_source(self):
+        seen, out = set(), []
+        for s in self.sources:
+            if s not in seen:
+                seen.add(s)
+                out.append(s)
+        return "\n".join(out)
+
+    def posterior_model(self, name, likelihood):
+        return device_posterior_model(self, name, likelihood)
+
+
+def device_distribution_model(source, name=None, logpdf=None, mcmc_logpdf=None, dimension=1,
+                              params_size=1, limits=None, dialect="c99", tiled=None):
+    """device-distribution-model (models.clj:84-89) with the same defaults."""
+    name = name or _gensym("distribution")
+    logpdf = logpdf or "%s_logpdf" % name
+    return DeviceDistributionModel(name, logpdf, mcmc_logpdf or logpdf, dimension, params_size,
+                                   limits, source, dialect, tiled)
+
+
+def device_likelihood_model(source, name=None, loglik=None, dialect="c99"):
+    """device-likelihood-model (models.clj:46-51)."""
+    name = name or _gensym("likelihood")
+    return DeviceLikelihoodModel(name, loglik or "%s_loglik" % name, source, dialect)
+
+
+_POSTERIOR = """
+extern "C" {
+inline REAL %(post)s(const uint32_t data_len, const uint32_t hyperparams_len,
+                    const REAL* params, const uint32_t dim, const REAL* x) {
+    return %(loglik)s(data_len, params, dim, x)
+        + %(prior)s(data_len, hyperparams_len, &params[data_len], dim, x);
+}
+}
+"""
+
+
+def device_posterior_model(prior, name, lik):
+    """device-posterior-model (models.clj:102-115)."""
+    if prior.dialect != lik.dialect:
+        raise ValueError("Incompatible types of likelihood and prior models.")
+    post = _gensym(name)
+    post_logpdf = "%s_logpdf" % post
+    post_mcmc = "%s_mcmc_logpdf" % post
+    srcs = []
+    for s in prior.sources + lik.sources:
+        if s not in srcs:
+            srcs.append(s)
+    srcs.append(_POSTERIOR % {"post": post_logpdf, "loglik": lik.loglik, "prior": prior.logpdf}
+                + _POSTERIOR % {"post": post_mcmc, "loglik": lik.loglik, "prior": prior.logpdf})
+    return DeviceDistributionModel(post, post_logpdf, post_mcmc, prior.dimension,
+                                   prior.params_size, prior.limits, srcs, prior.dialect)
+
+
+# ----------------------------------------------------------------- built-in models
+def _lim(lo, hi):
+    return [lo, hi]
+
+
+def distribution_models():
+    """distribution-models (models.clj:183-201): name -> model."""
+    g = get_source
+    return {
+        "uniform": device_distribution_model(g("uniform"), name="uniform", params_size=2,
+                                             limits=_lim(-FLOAT_MAX, FLOAT_MAX)),
+        "gaussian": device_distribution_model(g("gaussian"), name="gaussian",
+                                              mcmc_logpdf="gaussian_mcmc_logpdf", params_size=2,
+                                              limits=_lim(-FLOAT_MAX, FLOAT_MAX)),
+        "student_t": device_distribution_model(g("student_t"), name="student_t",
+                                               mcmc_logpdf="student_t_mcmc_logpdf", params_size=4,
+                                               limits=_lim(-FLOAT_MAX, FLOAT_MAX)),
+        "beta": device_distribution_model(g("beta"), name="beta", mcmc_logpdf="beta_mcmc_logpdf",
+                                          params_size=3, limits=_lim(0.0, 1.0)),
+        "exponential": device_distribution_model(g("exponential"), name="exponential",
+                                                 mcmc_logpdf="exponential_mcmc_logpdf",
+                                                 params_size=2,
+                                                 limits=_lim(FLOAT_MIN, FLOAT_MAX)),
+        "erlang": device_distribution_model(g("erlang"), name="erlang",
+                                            mcmc_logpdf="erlang_mcmc_logpdf", params_size=3,
+                                            limits=_lim(0.0, FLOAT_MAX)),
+        "gamma": device_distribution_model(g("gamma"), name="gamma",
+                                           mcmc_logpdf="gamma_mcmc_logpdf", params_size=2,
+                                           limits=_lim(0.0, FLOAT_MAX)),
+        "binomial": device_distribution_model(g("binomial"), name="binomial",
+                                              mcmc_logpdf="binomial_mcmc_logpdf", params_size=3,
+                                              limits=_lim(0.0, FLOAT_MAX)),
+    }
+
+
+def likelihood_models():
+    """likelihood-models (models.clj:203-206)."""
+    g = get_source
+    return {
+        "gaussian": device_likelihood_model(g("gaussian"), name="gaussian"),
+        "student_t": device_likelihood_model(g("student_t"), name="student_t"),
+        "binomial": device_likelihood_model(g("binomial"), name="binomial"),
+    }
+
+
+# ----------------------------------------------------------------- benchmark models
+def gaussian_posterior_model(tiled=True):
+    """(mu, sigma) of Gaussian data with prior N(mu | h0, h1^2) Uniform(sigma | h2, h3);
+    params = data || (h0, h1, h2, h3)."""
+    src = [get_source("gaussian"), get_source("uniform"), get_source("gaussian_posterior")]
+    t = None
+    if tiled:
+        t = {"prep": "gaussian_posterior_prep", "term": "gaussian_posterior_term",
+             "walker": "gaussian_posterior_walker", "row_len": 1, "prep_len": 2}
+    return device_distribution_model(src, name="gaussian_posterior", dimension=2, params_size=4,
+                                     logpdf="gaussian_posterior_logpdf", tiled=t)
+
+
+def mvn_precision_model(dim):
+    """Zero-mean Gaussian with a dim x dim precision matrix as hyperparameters."""
+    return device_distribution_model(get_source("mvn_precision"), name="mvn_precision",
+                                     dimension=dim, params_size=dim * dim,
+                                     logpdf="mvn_precision_logpdf")
+
+
+def logistic_model(features):
+    return device_distribution_model(get_source("logistic"), name="logistic",
+                                     dimension=features, params_size=1, logpdf="logistic_logpdf")
+
+
+def robust_t_model(features):
+    return device_distribution_model(get_source("robust_t"), name="robust_t",
+                                     dimension=features + 1, params_size=3,
+                                     logpdf="robust_t_logpdf")
+
+
+def hierarchical_model(groups):
+    return device_distribution_model(get_source("hierarchical"), name="hierarchical",
+                                     dimension=groups + 2, params_size=2,
+                                     logpdf="hierarchical_logpdf")

@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Throughput of the ensemble stretch-move engine: walker-steps/s on the 50-dimensional
+correlated Gaussian workload (AR(1) covariance, rho = 0.9, per-dimension scales
+log-uniform in [0.1, 10], precision matrix as 2500 hyperparameters; 65,536 walkers
+initialised N(0, I); 2,000 burn-in and 4,000 sampling steps; outputs mean, variance,
+acor and 128-bin histograms).
+
+One step = that whole job on one GPU.  `value` times it with the inputs resident on the
+device; `e2e` times the same job through the C ABI from host buffers (sampler creation
+with the host copy of the precision matrix, results copied back).  The reference arm
+(--impl reference) times the CPU restatement of the reference's stretch kernel on the
+host cores.  Multi-GPU: independent replicas (the path has no exchange step).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+DIM = 50
+WALKERS = 65536
+BURN = 2000
+RUN = 4000
+BINS = 128
+SEED = 0
+BYTES_PER_WALKER_STEP = 12 * DIM + 8      # read self + partner, write on accept, 2 logfn
+FLOP_PER_WALKER_STEP = 2 * DIM * DIM      # dense -x'Px/2
+L2_FLUSH_BYTES = 256 << 20
+
+
+def precision_matrix(dim=DIM, seed=SEED):
+    """Sigma_ij = s_i s_j rho^|i-j|, rho = 0.9, s_i log-uniform in [0.1, 10]; returns
+    (P = Sigma^-1 as float32, Sigma as float64)."""
+    rng = np.random.default_rng(seed)
+    s = np.exp(rng.uniform(np.log(0.1), np.log(10.0), dim))
+    i = np.arange(dim)
+    sigma = np.outer(s, s) * 0.9 ** np.abs(i[:, None] - i[None, :])
+    return np.linalg.inv(sigma).astype(np.float32), sigma
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return j.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "stretch_bare_mvn50.txt")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("traffic_bytes_per_launch_full_size:"):
+            try:
+                return float(ln.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------------------ CPU (oracle) timing
+def cpu_sample(steps_budget_s=12.0, walkers=WALKERS):
+    """The CPU restatement of the reference's stretch kernel (OpenMP over walkers, all
+    host cores) on the same workload: bounded to about steps_budget_s of CPU work."""
+    from oracle import oracle as O
+    P, _ = precision_matrix()
+    threads = os.cpu_count() or 1
+    r = O.Stretch("mvn_precision", DIM, walkers, P.reshape(-1), seed=SEED, threads=threads,
+                  flags=O.ACCEPT_LOG64)
+    r.init_position_normal(SEED + 1)
+    t0 = time.perf_counter()
+    r.move_bare()
+    t1 = time.perf_counter() - t0
+    n = max(1, int(steps_budget_s / max(t1, 1e-6)))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        r.move_bare()
+    dt = time.perf_counter() - t0
+    return {"value": walkers * n / dt, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d ensemble steps of the %d-walker 50-D job (%.1f s)" % (n, walkers, dt)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    budget = max(3.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_sample(budget / 4)
+    vals = [cpu_sample(budget) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    line = {
+        "impl": "reference", "metric": "walker-steps/s", "value": v, "unit": "walker-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * WALKERS * (BURN + RUN) / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config(),
+        "cpu_baseline": {"value": v, "unit": "walker-steps/s", "cores": vals[0]["cores"],
+                         "kind": "port", "sample": vals[0]["sample"]},
+        "e2e": {"value": v, "unit": "walker-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config():
+    return {"workload": "mvn50-ar1 (50-D correlated Gaussian, rho 0.9, scales log-U[0.1,10])",
+            "dim": DIM, "walkers": WALKERS, "burn_in": BURN, "run": RUN, "bins": BINS,
+            "model_form": "plain (one thread per walker, fused NVRTC kernel)",
+            "l2": "flushed between timed steps (256 MiB device write)",
+            "parallelism": "replicas"}
+
+
+# ------------------------------------------------------------------ GPU arm
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from bayadera_gb300 import _native
+    from bayadera_gb300 import models as M
+    from bayadera_gb300.engine import GB300BayaderaFactory
+
+    stream = torch.cuda.Stream()
+    P, sigma = precision_matrix()
+    dP = torch.from_numpy(P.reshape(-1).copy()).cuda()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    f = GB300BayaderaFactory(device=local, wgs=1024, stream=stream.cuda_stream)
+    sf = f.mcmc_factory(M.mvn_precision_model(DIM))
+    seed_base = 1000 * (rank + 1)
+
+    def job(samp, seed):
+        samp.init(seed)
+        samp.init_position_normal(seed + 1)
+        samp.burn_in(BURN, 2.0)
+        res = samp.run_sampler(RUN, 2.0)
+        mean = samp.mean()
+        var = samp.variance()
+        hist = samp.histogram(1, BINS)
+        return res, mean, var, hist
+
+    samp = sf.create_sampler(seed_base, WALKERS, dP)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    for w in range(args.warmup):
+        job(samp, seed_base + 10 * w)
+    torch.cuda.synchronize()
+
+    # timed region: K jobs, device-resident inputs, L2 flushed between jobs
+    times = []
+    results = None
+    launches0 = _native.launch_count()
+    with ClockSampler(local) as clocks:
+        barrier()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            results = job(samp, seed_base + 7919 * (k + 1))
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        barrier()
+    launches = _native.launch_count() - launches0
+    t_total = sum(times)
+    if dist is not None:
+        t = torch.tensor([t_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    walker_steps = WALKERS * (BURN + RUN) * args.steps * world
+    value = walker_steps / t_total
+
+    # dominant kernel: bare stretch launches of a burn-in, events on the launching stream
+    n_probe = 256
+    with torch.cuda.stream(stream):
+        flush.fill_(1)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    samp.burn_in(n_probe, 2.0)
+    e1.record(stream)
+    e1.synchronize()
+    t_launch = e0.elapsed_time(e1) / 1e3 / (2 * n_probe)
+    bytes_launch = (WALKERS // 2) * BYTES_PER_WALKER_STEP
+    flop_launch = (WALKERS // 2) * FLOP_PER_WALKER_STEP
+    hbm_peak, peak_kind = measured_peaks()
+    achieved = bytes_launch / t_launch / 1e9
+    traffic = profile_traffic()
+
+    # e2e: the same job through the C ABI from host buffers
+    e2e_times = []
+    h2d = P.nbytes
+    d2h = 0
+    for k in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = sf.create_sampler(seed_base + 31 * k, WALKERS, P.reshape(-1))
+        res, mean, var, hist = job(s2, seed_base + 31 * k)
+        s2.release()
+        e2e_times.append(time.perf_counter() - t0)
+        d2h = (8 + 3 * DIM * 8 + 2 * DIM * 8 + hist.limits.nbytes + hist.pdf.nbytes
+               + hist.bin_ranks.nbytes)
+    e2e_value = WALKERS * (BURN + RUN) * world / statistics.median(e2e_times)
+
+    # correctness of the job's result: posterior means within 3 MC s.e. of 0
+    res, mean, var, hist = results
+    ac = res["autocorrelation"]
+    within = None
+    if ac is not None:
+        within = int(np.sum(np.abs(ac.mean) <= 3 * ac.sigma))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample(12.0)
+
+    if rank == 0:
+        line = {
+            "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded AR(1) precision matrix, seed 0)",
+            "config": config(),
+            "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "kernel": "bay_stretch_bare",
+                         "launch_us": t_launch * 1e6,
+                         "fp32_tflops": flop_launch / t_launch / 1e12},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "result": {"acceptance_rate": res["acceptance_rate"],
+                       "tau_max": float(np.max(ac.tau)) if ac is not None else None,
+                       "means_within_3se": within, "dims": DIM},
+        }
+        print(json.dumps(line))
+    samp.release()
+    sf.release()
+    f.release()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,222 @@
+/*
+ * bayadera_gb300.h -- C ABI of libbayadera_gb300.so, the GB300 (sm_103a) engine for
+ * Bayadera's affine-invariant ensemble (stretch-move) MCMC path.
+ *
+ * The entry points replace the CUDA engine behind the reference's protocols
+ * (src/clojure/uncomplicate/bayadera/internal/protocols.clj): each declaration
+ * names the reference function it stands in for.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every call returns an int status: BAY_OK (0) or a BAY_ERR_* code; the message of
+ *    the last failure on the calling thread is bay_last_error().  No call aborts.
+ *  - Host arrays belong to the caller; device buffers and handles belong to the
+ *    library and are freed by the matching *_release.
+ *  - Walker positions crossing the ABI are dim x walkers column-major (walker k's
+ *    coordinates contiguous), the reference's GE matrix layout.  Histogram pdf and
+ *    ranks are bins x dim column-major; limits 2 x dim; acor series dim x n.
+ *  - Calls on one context are serialised on its stream (like the reference's single
+ *    hstream); different contexts may run concurrently.
+ */
+#ifndef BAYADERA_GB300_H
+#define BAYADERA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum bay_status {
+    BAY_OK = 0,
+    BAY_ERR_ARG = 1,     /* invalid argument (IllegalArgumentException in the reference) */
+    BAY_ERR_CUDA = 2,    /* a CUDA runtime/driver call failed */
+    BAY_ERR_COMPILE = 3, /* NVRTC rejected the model source; the log is in bay_last_error */
+    BAY_ERR_ALLOC = 4,   /* device memory exhausted or over the context's limit */
+    BAY_ERR_STATE = 5,   /* call out of order (e.g. no positions yet) */
+    BAY_ERR_DEVICE = 6   /* a device-side check failed (status word set by a kernel) */
+};
+
+typedef struct bay_ctx bay_ctx;
+typedef struct bay_model bay_model;
+typedef struct bay_sampler bay_sampler;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* bay_last_error(void);
+void bay_version(int* major, int* minor);
+
+/* ------------------------------------------------------------------ context
+ * Replaces gtx-bayadera-factory (nvidia_gtx.clj:793-807) and with-default-bayadera
+ * (cuda.clj:19-31): a device, one stream, and WGS, the reference's work-group size
+ * (default 1024 = max-block-dim-x).  WGS keeps its reference meaning (default
+ * histogram bins, acor window blocks, processing elements); the kernels' own CTA
+ * shapes are chosen by the library. */
+typedef struct bay_ctx_opts {
+    int device;          /* CUDA device ordinal */
+    uint32_t wgs;        /* 0 = 1024 */
+    void* stream;        /* cudaStream_t to run on; NULL = a new non-blocking stream */
+    uint64_t mem_limit;  /* bytes of device memory this context may allocate; 0 = no limit */
+} bay_ctx_opts;
+
+int bay_ctx_create(const bay_ctx_opts* opts, bay_ctx** out);
+int bay_ctx_release(bay_ctx* ctx);
+/* processing-elements (nvidia_gtx.clj:790-791): SM count * WGS. */
+int bay_ctx_processing_elements(bay_ctx* ctx, uint64_t* out);
+int bay_ctx_stream(bay_ctx* ctx, void** stream);
+int bay_ctx_synchronize(bay_ctx* ctx);
+/* Bytes currently allocated by this context. */
+int bay_ctx_allocated(bay_ctx* ctx, uint64_t* out);
+/* Kernels this library has enqueued in this process, all contexts (each replayed graph
+ * counts its kernel nodes).  No reference counterpart: an instrumentation counter. */
+int bay_launch_count(uint64_t* out);
+
+/* ------------------------------------------------------------------ models
+ * Replaces gtx-stretch-factory (nvidia_gtx.clj:747-757): NVRTC-compiles the model's C
+ * source for sm_103a into the fused stretch kernels (Philox draw, proposal, density,
+ * accept, acceptance count).  Same source contract as the reference
+ * (models.clj:102-115, cuda/distributions/posterior.cu:5-10): `logfn` names
+ *   REAL f(uint32_t data_len, uint32_t params_len, const REAL* params,
+ *          uint32_t dim, const REAL* x)
+ * with params = data || hyperparameters; REAL is float; the source may include
+ * <stdint.h>.  Compiled with -use_fast_math like the reference.
+ *
+ * BAY_FORM_TILED is the data-tiled form for likelihoods that sum over data rows:
+ *   void  prep(const REAL* hyper, uint32_t hyper_len, uint32_t dim, const REAL* x,
+ *              REAL* prep);                         per walker, prep_len values
+ *   REAL  term(const REAL* row, const REAL* prep);   one row of row_len floats
+ *   REAL  walker(uint64_t n_rows, const REAL* hyper, uint32_t hyper_len,
+ *                uint32_t dim, const REAL* x);       every term not summed over rows
+ * log density = walker(x) + sum over rows of term(row, prep(x)); the sum is spread
+ * over a CTA with compensated fp32 partial sums and an FP64 combine; data length is
+ * 64-bit. */
+enum bay_form { BAY_FORM_PLAIN = 0, BAY_FORM_TILED = 1 };
+enum bay_model_flags {
+    /* accept if u <= z^(D-1) exp(beta dlogfn) in fp32, the reference's formula
+     * (nvidia-gtx-mcmc-stretch.cu:84-88); default compares logs in FP64. */
+    BAY_MODEL_ACCEPT_REF = 1u << 0
+};
+
+typedef struct bay_model_desc {
+    const char* source;       /* NUL-terminated C source */
+    const char* logfn;        /* BAY_FORM_PLAIN: density function name */
+    uint32_t dim;             /* walker dimension (protocols.clj:39-44 dimension) */
+    uint32_t params_size;     /* hyperparameter count (params-size) */
+    uint32_t form;            /* bay_form */
+    const char* tile_prep;    /* BAY_FORM_TILED function names */
+    const char* tile_term;
+    const char* tile_walker;
+    uint32_t row_len;         /* BAY_FORM_TILED: floats per data row */
+    uint32_t prep_len;        /* BAY_FORM_TILED: per-walker precomputed values (>= 1) */
+    uint32_t walkers_per_cta; /* BAY_FORM_TILED: 0 = library choice */
+    uint32_t cta_threads;     /* 0 = library choice (multiple of 32, <= 1024) */
+    uint32_t flags;           /* bay_model_flags */
+} bay_model_desc;
+
+int bay_model_compile(bay_ctx* ctx, const bay_model_desc* desc, bay_model** out);
+int bay_model_release(bay_model* model);
+/* Compile-check a model without a device (NVRTC only); the reference surfaces the same
+ * errors from clojurecuda compile! (nvidia_gtx.clj:748-754).  wgs 0 = 1024. */
+int bay_model_check(const bay_model_desc* desc, uint32_t wgs);
+
+/* ------------------------------------------------------------------ samplers
+ * Replaces GTXStretchFactory.create-sampler (nvidia_gtx.clj:548-610) followed by
+ * init! (:391-400).  params = data || hyperparameters (n_params floats, the data being
+ * n_params - params_size floats, impl.clj:150-163).  Walkers must be even and >= 4;
+ * the reference's "multiple of 2*WGS" restriction (:552, :609-610) is lifted. */
+int bay_sampler_create(bay_model* model, uint32_t seed, uint64_t walkers, const float* params,
+                       uint64_t n_params, bay_sampler** out);
+/* Same, with params already resident on the device (not copied; must outlive the
+ * sampler).  d_params must be 16-byte aligned. */
+int bay_sampler_create_device(bay_model* model, uint32_t seed, uint64_t walkers,
+                              const float* d_params, uint64_t n_params, bay_sampler** out);
+int bay_sampler_release(bay_sampler* s);
+
+typedef struct bay_sampler_info {
+    uint64_t walkers;
+    uint32_t dim;
+    uint32_t wgs;
+    uint64_t iteration_counter; /* Info (nvidia_gtx.clj:332-335) */
+    uint64_t data_len;
+} bay_sampler_info;
+int bay_sampler_info_get(bay_sampler* s, bay_sampler_info* out);
+
+/* MCMC/init! (nvidia_gtx.clj:391-400): bare-move seeds (seed, seed+1), a = 2, beta = 1,
+ * move counter 0. */
+int bay_init(bay_sampler* s, uint32_t seed);
+/* MCMC/init-position! with limits (nvidia_gtx.clj:409-418): uniform in [lo, hi] per dim
+ * (limits 2 x dim: lo_0, hi_0, lo_1, hi_1, ...), then the log density of every walker. */
+int bay_init_position_limits(bay_sampler* s, uint32_t seed, const float* limits);
+/* init-position! from another sampler's walkers (nvidia_gtx.clj:401-408). */
+int bay_init_position_copy(bay_sampler* s, const bay_sampler* src);
+/* Positions from the host (dim x walkers column-major). */
+int bay_init_position_host(bay_sampler* s, const float* positions);
+/* Extension: N(mean, sd^2) i.i.d. in every coordinate. */
+int bay_init_position_normal(bay_sampler* s, uint32_t seed, float mean, float sd);
+
+/* MCMC/burn-in! (nvidia_gtx.clj:419-429): n bare steps at stretch a, beta = 1. */
+int bay_burn_in(bay_sampler* s, uint64_t steps, float a);
+/* MCMC/anneal! (nvidia_gtx.clj:430-440): step i runs at beta = 1/temperatures[i]. */
+int bay_anneal(bay_sampler* s, const float* temperatures, uint64_t steps, float a);
+/* MCMC/acc-rate! (nvidia_gtx.clj:466-478): one accu step; accepted / walkers. */
+int bay_acc_rate(bay_sampler* s, float a, double* rate);
+
+/* MCMC/run-sampler! (nvidia_gtx.clj:441-465): n accu steps with fresh accu seeds
+ * (+2 per call), then acor of the per-step ensemble means.  Results:
+ * acceptance rate, and per dim tau, mean, sigma (each dim doubles); lag.  means_out
+ * (nullable) receives the dim x steps column-major per-step means. */
+typedef struct bay_run_result {
+    double acceptance_rate;
+    float a;
+    uint32_t lag;
+    uint64_t steps;
+    int acor_status;           /* BAY_OK, or BAY_ERR_ARG if steps < 5 * lag */
+} bay_run_result;
+int bay_run_sampler(bay_sampler* s, uint64_t steps, float a, bay_run_result* result,
+                    double* tau, double* mean, double* sigma, float* means_out);
+
+/* RandomSampler/sample! (nvidia_gtx.clj:371-389): bare steps at beta = 1, after each
+ * the walkers' positions fill the next columns of out (dim x n_cols), the last copy
+ * truncated.  out may be host or device memory. */
+int bay_sample(bay_sampler* s, uint64_t n_cols, float* out);
+
+/* Location/mean and Spread/variance, sd (nvidia_gtx.clj:513-541): per-dim statistics of
+ * the current walkers, accumulated in FP64 (population variance, divisor W). */
+int bay_mean(bay_sampler* s, double* out);
+int bay_variance(bay_sampler* s, double* out);
+int bay_sd(bay_sampler* s, double* out);
+
+/* EstimateEngine/histogram! (nvidia_gtx.clj:480-512): limits = per-dim [min, max] of
+ * the current walkers; integer counts over `cycles` snapshots (a bare step between
+ * snapshots); pdf = (bins / (cycles W)) / (hi - lo) * count; ranks = bin indices by
+ * decreasing pdf (the reference's bitonic network).  bins: power of two <= 1024,
+ * 0 = WGS.  flags: BAY_HIST_COMPAT_START1 (CUDA reference: counts start at 1,
+ * nvidia_gtx.clj:500), BAY_HIST_COMPAT_ZERO_LIMITS (reference min/max reduction folds
+ * 0.0 into partial blocks, nvidia-gtx-estimate.cu:91-106).  limits 2 x dim, pdf and
+ * ranks bins x dim (host or device memory). */
+enum bay_hist_flags { BAY_HIST_COMPAT_START1 = 1u << 0, BAY_HIST_COMPAT_ZERO_LIMITS = 1u << 1 };
+int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags, float* limits,
+                  float* pdf, float* ranks);
+
+/* AcorEngine/acor (nvidia_gtx.clj:240-278, nvidia-gtx-acor.cu): integrated
+ * autocorrelation time by Sokal/Goodman pairwise blocking of a dim x n column-major
+ * series (host or device memory), in FP64.  lag = max(10, min(n/5, WGS, 64));
+ * BAY_ERR_ARG if n < 5 lag. */
+int bay_acor(bay_ctx* ctx, const float* series, uint32_t dim, uint64_t n, double* tau,
+             double* mean, double* sigma, uint32_t* lag);
+
+/* Checkpoint/resume: positions (dim x walkers), log densities (walkers) and the RNG
+ * state (8 words: bare seed, accu seed, bare step, accu step, iteration counter lo/hi,
+ * a bits, beta bits).  Counter-based RNG: an imported state resumes bit-exactly. */
+int bay_state_export(bay_sampler* s, float* positions, float* logfn, uint32_t* rng_state);
+int bay_state_import(bay_sampler* s, const float* positions, const float* logfn,
+                     const uint32_t* rng_state);
+/* Log densities of the current walkers (walkers floats). */
+int bay_logfn_values(bay_sampler* s, float* out);
+
+/* Execution control: CUDA-graph replay of the step loops (default on). */
+int bay_sampler_set_graphs(bay_sampler* s, int enabled);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

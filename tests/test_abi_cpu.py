@@ -1,0 +1,101 @@
+"""CPU-only checks of the C ABI library: it loads, exports every symbol the header
+declares, and NVRTC compiles every model form (no device needed)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "bayadera_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def native():
+    from bayadera_gb300 import build, _native
+    build.build()
+    _native.lib()
+    return _native
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bay_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    for n in ("bay_ctx_create", "bay_model_compile", "bay_sampler_create", "bay_burn_in",
+              "bay_run_sampler", "bay_histogram", "bay_acor", "bay_mean", "bay_variance"):
+        assert n in names
+
+
+def test_library_exports_every_header_symbol(native):
+    lib = C.CDLL(native.LIB_PATH)
+    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    assert missing == []
+
+
+def test_binding_covers_header(native):
+    assert sorted(native.exported_symbols()) == header_functions()
+
+
+def test_last_error_empty_at_start(native):
+    assert isinstance(native.last_error(), str)
+
+
+def test_ctx_create_without_gpu_fails_cleanly(native):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    opts = native.CtxOpts(0, 1024, None, 0)
+    h = C.c_void_p()
+    rc = native.lib().bay_ctx_create(C.byref(opts), C.byref(h))
+    assert rc != native.BAY_OK
+    assert native.last_error() != ""
+
+
+def _check(model, form=None, **kw):
+    from bayadera_gb300.engine import check_model
+    check_model(model, form, **kw)
+
+
+def test_model_check_builtin_library(native):
+    from bayadera_gb300 import models as M
+    for name, m in M.distribution_models().items():
+        _check(m)
+    # posterior of every likelihood with a gaussian prior
+    prior = M.distribution_models()["gaussian"]
+    for name, lik in M.likelihood_models().items():
+        _check(M.device_posterior_model(prior, "post_" + name, lik))
+
+
+def test_model_check_benchmark_models(native):
+    from bayadera_gb300 import models as M
+    _check(M.gaussian_posterior_model(), "plain")
+    _check(M.gaussian_posterior_model(), "tiled")
+    _check(M.gaussian_posterior_model(), "plain", accept_ref=True)
+    _check(M.mvn_precision_model(50))
+    _check(M.logistic_model(8))
+    _check(M.robust_t_model(8))
+    _check(M.hierarchical_model(4))
+
+
+def test_model_check_reports_nvrtc_log(native):
+    from bayadera_gb300 import models as M
+    bad = M.device_distribution_model("extern \"C\" { inline REAL broken_logpdf( { } }",
+                                      name="broken")
+    with pytest.raises(native.CompileError) as e:
+        _check(bad)
+    assert "error" in str(e.value)
+
+
+def test_model_check_rejects_bad_names(native):
+    from bayadera_gb300 import models as M
+    m = M.device_distribution_model(M.get_source("gaussian"), name="g",
+                                    logpdf="gaussian_logpdf; int x")
+    with pytest.raises(native.IllegalArgument):
+        _check(m)

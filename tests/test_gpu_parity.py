@@ -1,0 +1,401 @@
+"""GPU parity of the stretch-move path (libbayadera_gb300.so through its C ABI) against
+the oracle and the reference's golden vectors.  Tolerances are stated per test:
+integer/index work and the uniform-model trajectories are bit-exact; paths through
+fast-math transcendentals are checked to the stated ulp / relative bounds."""
+import numpy as np
+import pytest
+
+from tests.conftest import acor_matrix
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def factory():
+    import __graft_entry__
+    __graft_entry__.build()
+    from bayadera_gb300.engine import GB300BayaderaFactory
+    f = GB300BayaderaFactory(device=0, wgs=256)
+    yield f
+    f.release()
+
+
+@pytest.fixture(scope="module")
+def M():
+    from bayadera_gb300 import models
+    return models
+
+
+@pytest.fixture(scope="module")
+def N():
+    from bayadera_gb300 import _native
+    return _native
+
+
+def _uniform(factory, M, g, **kw):
+    sf = factory.mcmc_factory(M.distribution_models()["uniform"], **kw)
+    s = sf.create_sampler(g["seed"], g["walkers"], np.array(g["params"], np.float32))
+    s.init(g["seed"])
+    s.init_position(g["seed"], g["limits"])
+    return sf, s
+
+
+def _oracle_uniform(O, g):
+    r = O.Stretch("uniform", 1, g["walkers"], g["params"], seed=g["seed"], wgs=g["wgs"])
+    r.init(g["seed"])
+    r.init_position(g["seed"], g["limits"])
+    return r
+
+
+# ------------------------------------------------------------------ golden trajectories
+@pytest.mark.parametrize("accept_ref", [False, True])
+def test_uniform_trajectory_bit_exact(factory, M, oracle, golden, accept_ref):
+    g = golden["stretch_uniform"]
+    sf, s = _uniform(factory, M, g, accept_ref=accept_ref)
+    r = _oracle_uniform(oracle, g)
+    for want in g["sample_steps_first4"]:
+        got = s.sample()[0]
+        assert got[:4].tolist() == want
+        np.testing.assert_array_equal(got, r.sample()[:, 0])
+    s.release()
+    sf.release()
+
+
+def test_uniform_accu_step(factory, M, oracle, golden):
+    """nvidia_gtx_test.clj:237-258: two bare steps, then one accu step with seed 123."""
+    g = golden["stretch_uniform"]
+    sf, s = _uniform(factory, M, g)
+    s.burn_in(2, g["a"])
+    s.init(g["seed"] - 2)          # accu seed = move seed + 2 = 123
+    rate = s.acc_rate(g["a"])
+    pos = s.positions()[0]
+    assert pos[:4].tolist() == g["accu_first4"]
+    r = _oracle_uniform(oracle, g)
+    r.move_bare()
+    r.move_bare()
+    G = r.K // g["wgs"]
+    acc = np.zeros(G, np.uint32)
+    means = np.zeros(G, np.float32)
+    r.move_accu(g["seed"], 0, g["a"], acc, means)
+    np.testing.assert_array_equal(pos, r.xs)
+    assert acc[:10].tolist() == g["accu_accept_blocks_first10"]
+    assert round(rate * g["walkers"]) == int(acc.sum())       # integer count, exact
+    s.release()
+    sf.release()
+
+
+@pytest.mark.parametrize("accept_ref", [False, True])
+def test_gaussian_trajectory_golden(factory, M, golden, accept_ref):
+    g = golden["stretch_gaussian"]
+    sf = factory.mcmc_factory(M.distribution_models()["gaussian"], accept_ref=accept_ref)
+    s = sf.create_sampler(g["seed"], g["walkers"], np.array(g["params"], np.float32))
+    s.init(g["seed"])
+    s.init_position(g["seed"], g["limits"])
+    for want in g["sample_steps_first4"]:
+        # fast-math exp in q; tolerance: 1 ulp on the walkers the golden test reads
+        np.testing.assert_array_max_ulp(s.sample()[0][:4], np.array(want, np.float32), maxulp=1)
+    s.release()
+    sf.release()
+
+
+def test_burn_in_golden_statistics(factory, M, golden):
+    """nvidia_gtx_test.clj:279-296 (100 steps at a = 1.5).  The golden values depend on
+    every fast-math accept decision of 1.1M proposals; the statistics must agree to
+    within 0.03 (a few standard errors of an 11264-walker mean)."""
+    g = golden["burn_in_gaussian"]
+    sf = factory.mcmc_factory(M.distribution_models()["gaussian"])
+    s = sf.create_sampler(g["init_seed"], g["walkers"], np.array(g["params"], np.float32))
+    s.init_position(g["init_seed"], g["limits"])
+    s.init(g["seed"])
+    s.burn_in(g["steps"], g["a"])
+    assert abs(s.sample()[0].astype(np.float64).mean() - g["mean"]) < 0.03
+    s.sample()
+    assert abs(s.sample()[0].astype(np.float64).std() - g["sd"]) < 0.03
+    s.release()
+    sf.release()
+
+
+# ------------------------------------------------------------------ step consistency (D > 1)
+def _step_consistency(factory, oracle, model, oname, params, data_len, dim, W, steps, seed,
+                      init, max_mismatch):
+    sf = factory.mcmc_factory(model, form="plain")
+    s = sf.create_sampler(seed, W, params)
+    init(s)
+    worst = 0
+    for t in range(steps):
+        pos, lf, rng = s.export_state()
+        r = oracle.Stretch(oname, dim, W, params, data_len=data_len, seed=int(rng[0]),
+                           flags=oracle.ACCEPT_LOG64)
+        r.xs[:] = pos.reshape(-1)
+        r.logfn[:] = lf
+        r.bare_counter = int(rng[2])
+        r.move_bare(a=2.0, beta=1.0)
+        s.burn_in(1, 2.0)
+        got = s.positions().T.reshape(W, dim)
+        want = r.xs.reshape(W, dim)
+        rows = np.any(got != want, axis=1)
+        worst = max(worst, int(rows.sum()))
+        # the walkers that differ may differ only through a marginal accept decision
+        assert rows.sum() <= max_mismatch, "step %d: %d walkers differ" % (t, rows.sum())
+    s.release()
+    sf.release()
+    return worst
+
+
+def test_step_consistency_mvn50(factory, M, oracle):
+    D, W = 50, 2048
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(D, D)).astype(np.float64)
+    P = (A @ A.T / D + np.eye(D)).astype(np.float32)
+    _step_consistency(factory, oracle, M.mvn_precision_model(D), "mvn_precision",
+                      P.reshape(-1), 0, D, W, 6, 11,
+                      lambda s: s.init_position_normal(3, 0.0, 1.0), max_mismatch=4)
+
+
+def test_step_consistency_gaussian_posterior(factory, M, oracle):
+    rng = np.random.default_rng(0)
+    data = rng.normal(3.0, 2.0, 500).astype(np.float32)
+    params = np.concatenate([data, np.array([0.0, 10.0, 0.0, 20.0], np.float32)])
+    _step_consistency(factory, oracle, M.gaussian_posterior_model(), "gaussian_posterior",
+                      params, data.size, 2, 1024, 6, 13,
+                      lambda s: s.init_position(4, [2.0, 4.0, 1.0, 3.0]), max_mismatch=8)
+
+
+# ------------------------------------------------------------------ log densities
+def test_tiled_logfn_matches_fp64(factory, M, oracle):
+    rng = np.random.default_rng(1)
+    data = rng.normal(3.0, 2.0, 10000).astype(np.float32)
+    params = np.concatenate([data, np.array([0.0, 10.0, 0.0, 20.0], np.float32)])
+    for form in ("tiled", "plain"):
+        sf = factory.mcmc_factory(M.gaussian_posterior_model(), form=form)
+        s = sf.create_sampler(3, 512, params)
+        s.init_position(5, [2.5, 3.5, 1.5, 2.5])
+        pos = s.positions().T.astype(np.float64)
+        lf = s.logfn().astype(np.float64)
+        want = np.array([oracle.logfn64("gaussian_posterior", params, data.size, 2, p)
+                         for p in pos])
+        err = np.abs(lf - want) / np.abs(want)
+        # tiled: Kahan fp32 + FP64 combine; plain: serial fp32 over 10^4 terms
+        assert err.max() < (2e-6 if form == "tiled" else 2e-4), (form, err.max())
+        s.release()
+        sf.release()
+
+
+# ------------------------------------------------------------------ estimates
+def test_moments_fp64(factory, M, oracle):
+    D, W = 50, 4096
+    P = np.eye(D, dtype=np.float32) * 0.25
+    sf = factory.mcmc_factory(M.mvn_precision_model(D))
+    s = sf.create_sampler(1, W, P.reshape(-1))
+    s.init_position_normal(2, 1.0, 3.0)
+    s.burn_in(5, 2.0)
+    pos = s.positions().T.reshape(-1)
+    np.testing.assert_allclose(s.mean(), oracle.mean64(pos, D), rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(s.variance(), oracle.variance64(pos, D), rtol=1e-12)
+    np.testing.assert_allclose(s.sd(), np.sqrt(oracle.variance64(pos, D)), rtol=1e-12)
+    s.release()
+    sf.release()
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_histogram_bit_exact(factory, M, oracle, N, flags):
+    D, W, bins = 3, 6144, 256
+    P = np.diag([1.0, 0.25, 4.0]).astype(np.float32)
+    sf = factory.mcmc_factory(M.mvn_precision_model(D))
+    s = sf.create_sampler(1, W, P.reshape(-1))
+    s.init_position_normal(2, 5.0, 1.0)   # away from 0: the Q7 flag matters
+    s.burn_in(3, 2.0)
+    pos = s.positions().T.reshape(-1).copy()
+    h = s.histogram(1, bins, flags)
+    ol, opdf, orank, _ = oracle.histogram([pos], D, bins, wgs=256, flags=flags)
+    np.testing.assert_array_equal(h.limits.T.reshape(-1), ol)
+    np.testing.assert_array_equal(h.pdf.T.reshape(-1), opdf)
+    np.testing.assert_array_equal(h.bin_ranks.T.reshape(-1), orank)
+    s.release()
+    sf.release()
+
+
+def test_histogram_cycles_normalised(factory, M):
+    sf = factory.mcmc_factory(M.distribution_models()["gaussian"])
+    s = sf.create_sampler(1, 4096, np.array([0.0, 1.0], np.float32))
+    s.init_position(2, [-3.0, 3.0])
+    s.burn_in(20, 2.0)
+    h = s.histogram(4, 128)
+    width = (h.limits[1, 0] - h.limits[0, 0]) / 128
+    # walkers that move outside the first snapshot's limits land in the edge bins
+    assert abs(float(h.pdf[:, 0].sum()) * width - 1.0) < 1e-5
+    assert s.info()["iteration_counter"] == 23
+    s.release()
+    sf.release()
+
+
+# ------------------------------------------------------------------ acor
+@pytest.mark.parametrize("n", [67, 367])
+def test_acor_golden(factory, oracle, golden, acor_series, n):
+    a = golden["acor"][str(n)]
+    m = acor_matrix(acor_series, n, a["row1"])
+    ac = factory.acor(m)
+    np.testing.assert_allclose(ac.tau, a["tau"], rtol=1e-5)          # fp32 reference
+    assert abs(ac.sigma[0] - a["sigma0"]) <= 1e-5 * a["sigma0"]
+    t64, m64, s64, lag = oracle.acor64(m, golden["acor"]["wgs"])
+    np.testing.assert_allclose(ac.tau, t64, rtol=1e-10)              # FP64 oracle
+    np.testing.assert_allclose(ac.sigma, s64, rtol=1e-10)
+    np.testing.assert_allclose(ac.mean, m64, rtol=1e-10, atol=1e-12)
+    assert ac.lag == lag
+
+
+def test_acor_long_series(factory, oracle, golden, acor_series):
+    a = golden["acor"]["112640"]
+    m = acor_matrix(acor_series, 112640, a["row1"])
+    ac = factory.acor(m)
+    assert abs(ac.tau[1] - a["tau1"]) <= a["tau1_tol"]
+    assert abs(ac.sigma[0] - a["sigma0"]) <= a["sigma0_tol"]
+    t64, _, s64, _ = oracle.acor64(m, golden["acor"]["wgs"])
+    np.testing.assert_allclose(ac.tau, t64, rtol=1e-9)
+
+
+def test_acor_too_short(factory, N):
+    with pytest.raises(N.IllegalArgument):
+        factory.acor(np.ones((2, 40), np.float32))
+
+
+# ------------------------------------------------------------------ run-sampler!
+def test_run_sampler_uniform_exact(factory, M, oracle, golden):
+    g = golden["stretch_uniform"]
+    sf, s = _uniform(factory, M, g)
+    s.burn_in(10, 2.0)
+    res = s.run_sampler(64, 2.0, return_means=True)
+    r = _oracle_uniform(oracle, g)
+    r.burn_in(10, 2.0)
+    rate, means = r.run_sampler(64, 2.0)
+    assert round(res["acceptance_rate"] * g["walkers"] * 64) == round(rate * g["walkers"] * 64)
+    np.testing.assert_array_equal(s.positions()[0], r.xs)
+    np.testing.assert_allclose(res["means"], means, rtol=2e-6, atol=2e-6)
+    ac = res["autocorrelation"]
+    t64, m64, s64, _ = oracle.acor64(res["means"], g["wgs"])
+    np.testing.assert_allclose(ac.tau, t64, rtol=1e-9)
+    s.release()
+    sf.release()
+
+
+def test_engine_statistics_golden(factory, M, golden):
+    """nvidia_gtx_test.clj:298-318 (CUDA: 0.488) and its OpenCL twin amd_gcn_test.clj:309
+    (0.485).  Their +-0.001 holds only for their own trajectories: one acceptance probe
+    over 22528 walkers has a binomial s.e. of about 0.0033, and 5120 burn-in steps of
+    fast-math accept decisions decorrelate any two implementations.  Checked here:
+    within 3 binomial s.e. of both reference values; tau within the reference's 0.5."""
+    g = golden["engine_gaussian"]
+    sf = factory.mcmc_factory(M.distribution_models()["gaussian"])
+    s = sf.create_sampler(g["seed"], g["walkers"], np.array(g["params"], np.float32))
+    s.init(g["seed"])
+    s.init_position(g["seed"], g["limits"])
+    s.burn_in(g["burn_in"], g["a"])
+    rate = s.acc_rate(g["a"])
+    se = np.sqrt(rate * (1 - rate) / g["walkers"])
+    assert abs(rate - g["acc_rate"]) <= 3 * se
+    assert abs(rate - 0.485) <= 3 * se
+    res = s.run_sampler(g["run_steps"], g["a"])
+    assert abs(res["autocorrelation"].tau[0] - g["tau"]) <= g["tau_tol"]
+    s.release()
+    sf.release()
+
+
+# ------------------------------------------------------------------ state, determinism
+def test_state_roundtrip_bit_exact(factory, M):
+    P = np.eye(8, dtype=np.float32)
+    sf = factory.mcmc_factory(M.mvn_precision_model(8))
+    s = sf.create_sampler(5, 1024, P.reshape(-1))
+    s.init_position_normal(6)
+    s.burn_in(10, 2.0)
+    state = s.export_state()
+    s.burn_in(40, 2.0)
+    a = s.positions().copy()
+    s.import_state(*state)
+    s.burn_in(40, 2.0)
+    np.testing.assert_array_equal(s.positions(), a)
+    s.release()
+    sf.release()
+
+
+def test_graphs_match_direct_launches(factory, M):
+    P = np.eye(4, dtype=np.float32)
+    sf = factory.mcmc_factory(M.mvn_precision_model(4))
+    out = []
+    for graphs in (True, False):
+        s = sf.create_sampler(9, 512, P.reshape(-1))
+        s.set_graphs(graphs)
+        s.init_position_normal(1)
+        s.burn_in(75, 2.0)
+        r = s.run_sampler(70, 2.0, return_means=True)
+        out.append((s.positions().copy(), r["means"].copy(), r["acceptance_rate"]))
+        s.release()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+    sf.release()
+
+
+def test_sample_columns(factory, M):
+    sf = factory.mcmc_factory(M.distribution_models()["gaussian"])
+    s = sf.create_sampler(3, 1024, np.array([0.0, 1.0], np.float32))
+    s.init_position(4, [-2.0, 2.0])
+    x = s.sample(2500)
+    assert x.shape == (1, 2500)
+    assert s.info()["iteration_counter"] == 3
+    np.testing.assert_array_equal(x[:, 2048:], s.positions()[:, :452])
+    s.release()
+    sf.release()
+
+
+# ------------------------------------------------------------------ errors
+def test_errors(factory, M, N):
+    sf = factory.mcmc_factory(M.distribution_models()["gaussian"])
+    with pytest.raises(N.IllegalArgument):
+        sf.create_sampler(1, 1001, np.array([0.0, 1.0], np.float32))
+    s = sf.create_sampler(1, 1024, np.array([0.0, 1.0], np.float32))
+    with pytest.raises(N.BayaderaError):
+        s.burn_in(1, 2.0)                                   # no positions yet
+    s.init_position(1, [-1.0, 1.0])
+    with pytest.raises(N.IllegalArgument):
+        s.histogram(1, 100)                                 # not a power of two
+    with pytest.raises(N.IllegalArgument):
+        s.burn_in(1, 0.5)                                   # a <= 1
+    r = s.run_sampler(20, 2.0)                              # acor needs n >= 5 lag
+    assert r["autocorrelation"] is None and "must not be less than" in r["autocorrelation_error"]
+    s.release()
+    sf.release()
+
+
+def test_memory_limit(M, N):
+    from bayadera_gb300.engine import GB300BayaderaFactory
+    with GB300BayaderaFactory(device=0, wgs=256, mem_limit=1 << 20) as f:
+        sf = f.mcmc_factory(M.mvn_precision_model(64))
+        with pytest.raises(N.BayaderaError) as e:
+            sf.create_sampler(1, 1 << 16, np.eye(64, dtype=np.float32).reshape(-1))
+        assert e.value.code == N.BAY_ERR_ALLOC
+        sf.release()
+
+
+# ------------------------------------------------------------------ posterior moments
+def test_mvn_posterior_within_3_mcse(factory, M):
+    """Correlated 10-D Gaussian: ensemble-pooled means within 3.5 MC s.e. (acor sigma;
+    3.5 rather than 3 so that ten dims pass together with 99.5% probability) of the
+    analytic mean 0, and variances within 10% of Sigma's diagonal."""
+    D = 10
+    rng = np.random.default_rng(2)
+    s_ = np.exp(rng.uniform(np.log(0.5), np.log(2.0), D))
+    idx = np.arange(D)
+    Sigma = np.outer(s_, s_) * 0.9 ** np.abs(idx[:, None] - idx[None, :])
+    P = np.linalg.inv(Sigma).astype(np.float32)
+    sf = factory.mcmc_factory(M.mvn_precision_model(D))
+    s = sf.create_sampler(21, 8192, P.reshape(-1))
+    s.init_position_normal(22)
+    s.burn_in(2000, 2.0)
+    res = s.run_sampler(4000, 2.0, return_means=True)
+    ac = res["autocorrelation"]
+    pooled = res["means"].astype(np.float64).mean(axis=1)
+    assert np.all(np.abs(pooled) <= 3.5 * ac.sigma + 1e-12), (pooled, ac.sigma)
+    var = s.variance()
+    assert np.all(np.abs(var / np.diag(Sigma) - 1) < 0.1)
+    s.release()
+    sf.release()
