@@ -294,9 +294,20 @@ def test_engine_statistics_golden(factory, M, golden):
     se = np.sqrt(rate * (1 - rate) / g["walkers"])
     assert abs(rate - g["acc_rate"]) <= 3 * se
     assert abs(rate - 0.485) <= 3 * se
-    res = s.run_sampler(g["run_steps"], g["a"])
-    assert abs(res["autocorrelation"].tau[0] - g["tau"]) <= g["tau_tol"]
     s.release()
+    # tau-hat of one 63670-step run scatters by about +-0.6 from seed to seed (the CPU
+    # oracle gives 11.73..12.48 for three seeds): the mean over three seeds must lie within
+    # the reference's 12.5 +- 0.5, each run within 12.5 +- 1.5.
+    taus = []
+    for seed in (g["seed"], g["seed"] + 1, g["seed"] + 2):
+        s = sf.create_sampler(seed, g["walkers"], np.array(g["params"], np.float32))
+        s.init(seed)
+        s.init_position(seed, g["limits"])
+        s.burn_in(g["burn_in"], g["a"])
+        taus.append(s.run_sampler(g["run_steps"], g["a"])["autocorrelation"].tau[0])
+        s.release()
+    assert abs(np.mean(taus) - g["tau"]) <= g["tau_tol"], taus
+    assert all(abs(t - g["tau"]) <= 3 * g["tau_tol"] for t in taus), taus
     sf.release()
 
 
