@@ -97,6 +97,8 @@ _SIGNATURES = {
     "bay_sd": (C.c_int, [P, P]),
     "bay_histogram": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]),
     "bay_acor": (C.c_int, [P, P, C.c_uint32, C.c_uint64, P, P, P, C.POINTER(C.c_uint32)]),
+    "bay_acor_noalloc": (C.c_int, [P, P, C.c_uint32, C.c_uint64, P, P, P,
+                                   C.POINTER(C.c_uint32)]),
     "bay_state_export": (C.c_int, [P, P, P, P]),
     "bay_state_import": (C.c_int, [P, P, P, P]),
     "bay_logfn_values": (C.c_int, [P, P]),

@@ -1111,6 +1111,41 @@ int bay_acor(bay_ctx* c, const float* series, uint32_t D, uint64_t n, double* ta
     return g != BAY_OK ? g : rc;
 }
 
+// Allocation-free acor for callers that cannot allocate device memory at call time:
+// the work space is the library's fixed device scratch (BAY_ACOR_NOALLOC_MAX_DOUBLES).
+int bay_acor_noalloc(bay_ctx* c, const float* d_series, uint32_t D, uint64_t n, double* tau,
+                     double* mean, double* sigma, uint32_t* lag_out) {
+    return guarded([&] {
+        if (!c || !d_series) fail(BAY_ERR_ARG, "NULL argument");
+        if (D == 0) fail(BAY_ERR_ARG, "dim must be >= 1");
+        if (!is_device_ptr(d_series))
+            fail(BAY_ERR_ARG, "bay_acor_noalloc needs the series in device memory");
+        const uint64_t need = (uint64_t)D * n + 3ull * D;
+        if (n > 0xffffffffull || need > BAY_ACOR_NOALLOC_MAX_DOUBLES)
+            fail(BAY_ERR_ARG, "series too large for the fixed acor scratch: dim * n + 3 * dim = " +
+                                  std::to_string(need) + " doubles > " +
+                                  std::to_string(BAY_ACOR_NOALLOC_MAX_DOUBLES));
+        const uint32_t lag = acor_lag(n, c->wgs);
+        if (lag_out) *lag_out = lag;
+        if ((uint64_t)lag * 5 > n)
+            fail(BAY_ERR_ARG, "The autocorrelation time is too long relative to the variance. "
+                              "Number of steps (" + std::to_string(n) +
+                                  ") must not be less than " + std::to_string(lag * 5) + ".");
+        std::lock_guard<std::recursive_mutex> lk(c->mu);
+        c->use();
+        double* work = nullptr;
+        cuda_check(bay::acor_noalloc_scratch(c->device, &work), "cudaGetSymbolAddress(acor scratch)");
+        double* res = work + (size_t)D * n;
+        cuda_check(bay::launch_acor(d_series, D, (uint32_t)n, c->wgs, lag, work, res, res + D,
+                                    res + 2 * D, c->stream),
+                   "acor");
+        if (tau) cuda_check(cudaMemcpyAsync(tau, res, sizeof(double) * D, cudaMemcpyDefault, c->stream), "copy");
+        if (mean) cuda_check(cudaMemcpyAsync(mean, res + D, sizeof(double) * D, cudaMemcpyDefault, c->stream), "copy");
+        if (sigma) cuda_check(cudaMemcpyAsync(sigma, res + 2 * D, sizeof(double) * D, cudaMemcpyDefault, c->stream), "copy");
+        cuda_check(cudaStreamSynchronize(c->stream), "sync");
+    });
+}
+
 int bay_state_export(bay_sampler* s, float* positions, float* logfn, uint32_t* rng) {
     return guarded([&] {
         if (!s) fail(BAY_ERR_ARG, "NULL sampler");

@@ -3,6 +3,7 @@
 // ranks, acor, and the device-resident control block.  The per-model fused stretch
 // kernels are in device/bay_stretch.cuh (NVRTC).
 #include <atomic>
+#include <mutex>
 
 #include "bay_kernels.cuh"
 #include "device/bay_rng.cuh"
@@ -318,6 +319,13 @@ __global__ void acor_kernel(const float* series, uint32_t D, uint32_t n, uint32_
     }
 }
 
+// Fixed device scratch of the allocation-free acor entry point: the work copy of the
+// series (dim * n doubles) followed by tau, mean and sigma (3 * dim doubles).  It is
+// part of the module image, so every GPU that loads the library holds these 8 MiB
+// until the process exits.  acor_kernel writes every slot it later reads, so nothing
+// has to be cleared between calls; calls that overlap on the GPU share it and race.
+__device__ __align__(256) double g_acor_noalloc_scratch[BAY_ACOR_NOALLOC_MAX_DOUBLES];
+
 inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 152u * 16u) {
     uint64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;
@@ -413,6 +421,24 @@ cudaError_t launch_acor(const float* series, uint32_t D, uint32_t n, uint32_t wg
     acor_kernel<<<D, 256, 0, s>>>(series, D, n, wgs, lag, work, tau, mean, sigma);
     g_launches++;
     return cudaGetLastError();
+}
+
+cudaError_t acor_noalloc_scratch(int device, double** ptr) {
+    // Host code must not use g_acor_noalloc_scratch's name as an address: it is a
+    // host-side stand-in.  The device address comes from cudaGetSymbolAddress, looked up
+    // once per device with that device current (the caller made it current).
+    static std::mutex mu;
+    static double* cache[64] = {nullptr};
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(mu);
+    if (!cache[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_acor_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        cache[device] = static_cast<double*>(p);
+    }
+    *ptr = cache[device];
+    return cudaSuccess;
 }
 
 cudaError_t launch_fill_bytes(void* p, uint64_t n, unsigned char v, cudaStream_t s) {

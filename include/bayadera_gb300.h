@@ -204,6 +204,20 @@ int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags
 int bay_acor(bay_ctx* ctx, const float* series, uint32_t dim, uint64_t n, double* tau,
              double* mean, double* sigma, uint32_t* lag);
 
+/* acor that allocates nothing.  No counterpart in the reference: it is for callers
+ * that may not allocate device memory when they call -- for instance a host that runs
+ * inside a framework whose caching allocator owns the device memory, or a real-time
+ * loop with a fixed memory budget.  The caller passes the series in device memory
+ * (dim x n column-major) and the outputs (device or host memory); the work space is a
+ * fixed 8 MiB scratch array compiled into the library, so dim * n + 3 * dim must not
+ * exceed 1,048,576 doubles (BAY_ERR_ARG otherwise).  Every GPU that loads the library
+ * holds that array until the process exits.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.  All calls
+ * share the one array: calls whose kernels overlap on the GPU (other contexts, other
+ * streams) race and must be serialised by the caller.  Same results as bay_acor. */
+int bay_acor_noalloc(bay_ctx* ctx, const float* d_series, uint32_t dim, uint64_t n,
+                     double* tau, double* mean, double* sigma, uint32_t* lag);
+
 /* Checkpoint/resume: positions (dim x walkers), log densities (walkers) and the RNG
  * state (8 words: bare seed, accu seed, bare step, accu step, iteration counter lo/hi,
  * a bits, beta bits).  Counter-based RNG: an imported state resumes bit-exactly. */
