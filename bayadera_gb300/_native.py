@@ -18,6 +18,7 @@ BAY_ERR_DEVICE = 6
 
 FORM_PLAIN = 0
 FORM_TILED = 1
+FORM_GEMM = 2
 MODEL_ACCEPT_REF = 1
 HIST_COMPAT_START1 = 1
 HIST_COMPAT_ZERO_LIMITS = 2
@@ -49,7 +50,11 @@ class ModelDesc(C.Structure):
                 ("params_size", C.c_uint32), ("form", C.c_uint32), ("tile_prep", C.c_char_p),
                 ("tile_term", C.c_char_p), ("tile_walker", C.c_char_p), ("row_len", C.c_uint32),
                 ("prep_len", C.c_uint32), ("walkers_per_cta", C.c_uint32),
-                ("cta_threads", C.c_uint32), ("flags", C.c_uint32)]
+                ("cta_threads", C.c_uint32), ("flags", C.c_uint32),
+                ("gemm_features", C.c_uint32), ("gemm_coef", C.c_uint32),
+                ("gemm_block", C.c_uint32), ("gemm_ld", C.c_uint32),
+                ("gemm_offset", C.c_uint64), ("gemm_rows", C.c_uint64),
+                ("gemm_aux_col", C.c_uint32), ("gemm_aux_len", C.c_uint32)]
 
 
 class SamplerInfo(C.Structure):

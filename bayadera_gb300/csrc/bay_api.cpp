@@ -15,6 +15,7 @@
 #include <cctype>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -51,6 +52,7 @@ struct DriverApi {
     PFN_cuLibraryUnload_v12000 LibraryUnload = nullptr;
     PFN_cuLibraryGetKernel_v12000 LibraryGetKernel = nullptr;
     PFN_cuLaunchKernel_v4000 LaunchKernel = nullptr;
+    PFN_cuKernelSetAttribute_v12000 KernelSetAttribute = nullptr;
     bool loaded = false;
 };
 DriverApi g_cu;
@@ -84,6 +86,7 @@ void load_driver_api() {
     resolve("cuLibraryUnload", g_cu.LibraryUnload, 12000);
     resolve("cuLibraryGetKernel", g_cu.LibraryGetKernel, 12000);
     resolve("cuLaunchKernel", g_cu.LaunchKernel, 4000);
+    resolve("cuKernelSetAttribute", g_cu.KernelSetAttribute, 12000);
     g_cu.loaded = true;
 }
 
@@ -164,7 +167,25 @@ struct bay_model {
     CUlibrary lib = nullptr;
     CUkernel k_bare = nullptr, k_accu = nullptr, k_logfn = nullptr;
     uint32_t dim = 0, params_size = 0, form = 0, cta = 256, wpc = 1, flags = 0;
+    // GEMM form layout of A (see bay_model_desc)
+    uint32_t gemm_features = 0, gemm_block = 0, gemm_ld = 0, gemm_aux_col = 0, gemm_aux_len = 0;
+    uint64_t gemm_offset = 0, gemm_rows = 0;
 };
+
+namespace {
+constexpr uint32_t kGemmWalkers = 64;             // BAY_WT in device/bay_stretch.cuh
+constexpr size_t kGemmMaxSmem = 200 * 1024;       // dynamic shared memory cap per CTA
+
+// Dynamic shared memory of the GEMM-form kernels for `rows` rows (layout in
+// bay_stretch_gemm: A feature-major, Y tile twice, aux values).
+size_t gemm_smem_bytes(const bay_model* m, uint64_t rows) {
+    const uint64_t np = (rows + 63) & ~63ull;
+    const uint64_t dpad = m->dim | 1u;
+    const uint64_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1;
+    return sizeof(float) * (m->gemm_features * np + m->gemm_features * kGemmWalkers +
+                            kGemmWalkers * dpad + np * auxs);
+}
+}  // namespace
 
 namespace {
 
@@ -191,7 +212,17 @@ std::vector<char> nvrtc_compile(const std::string& src, const std::vector<std::s
         fail(BAY_ERR_COMPILE, "nvrtcCreateProgram failed");
     std::vector<const char*> o;
     for (auto& s : opts) o.push_back(s.c_str());
+    // BAY_PTXAS_VERBOSE=1 prints ptxas' resource report (registers, spills, shared memory)
+    const bool verbose = std::getenv("BAY_PTXAS_VERBOSE") != nullptr;
+    if (verbose) o.push_back("--ptxas-options=-v");
     const nvrtcResult r = nvrtcCompileProgram(prog, (int)o.size(), o.data());
+    if (verbose && r == NVRTC_SUCCESS) {
+        size_t n = 0;
+        nvrtcGetProgramLogSize(prog, &n);
+        std::string log(n, '\0');
+        if (n) nvrtcGetProgramLog(prog, &log[0]);
+        std::fprintf(stderr, "%s\n", log.c_str());
+    }
     if (r != NVRTC_SUCCESS) {
         size_t n = 0;
         nvrtcGetProgramLogSize(prog, &n);
@@ -233,8 +264,7 @@ struct bay_sampler {
     const float* params = nullptr;
     bool own_params = false;
     uint64_t n_params = 0, data_len = 0;
-    double* part = nullptr;
-    double* half_sum = nullptr;
+    float* part = nullptr;  // accu per-CTA sums of one chunk: kChunk x 2 x grid() x D
     float* means = nullptr;
     uint64_t means_cap = 0;
     float* stage = nullptr;  // W*D floats: AoS staging
@@ -252,10 +282,33 @@ struct bay_sampler {
     cudaGraphExec_t g_bare = nullptr, g_accu = nullptr;
     uint64_t g_accu_cap = 0;
 
-    unsigned grid() const {
-        const uint64_t per = model->form == BAY_FORM_TILED ? model->wpc : model->cta;
-        return (unsigned)((K + per - 1) / per);
+    uint64_t gemm_base = 0, gemm_rows = 0;  // GEMM form: A's row 0 and row count in params
+    uint32_t gemm_np = 0;                   // rows padded to a multiple of 64
+    float* gemm_lay = nullptr;              // the kernel's layout of A and the aux values
+    size_t smem = 0;                        // dynamic shared memory per CTA
+
+    // Dimension-major copy of the walker state (stage[d * W + w]) for the per-dimension
+    // estimate kernels (moments, limits, histogram), which read one dimension per CTA.
+    const float* dim_major() {
+        if (!stage) stage = (float*)ctx->alloc(sizeof(float) * (size_t)D * W);
+        cuda_check(bay::launch_aos_to_soa(xs, D, W, stage, ctx->stream), "transpose");
+        return stage;
     }
+
+    // A device-detected failure (a bounded wait that gave up) sets ctl->status.
+    void check_status() {
+        unsigned int st = 0;
+        cuda_check(cudaMemcpyAsync(&st, &ctl->status, sizeof(st), cudaMemcpyDeviceToHost,
+                                   ctx->stream),
+                   "cudaMemcpy(status)");
+        cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
+        if (st) fail(BAY_ERR_DEVICE, "a kernel gave up waiting for its shared-memory copy "
+                                     "(device status " + std::to_string(st) + ")");
+    }
+
+    uint64_t per_cta() const { return model->form == BAY_FORM_PLAIN ? model->cta : model->wpc; }
+
+    unsigned grid() const { return (unsigned)((K + per_cta() - 1) / per_cta()); }
 
     bay_stretch_params make_params(uint32_t half, uint32_t step_off) const {
         bay_stretch_params p;
@@ -264,7 +317,6 @@ struct bay_sampler {
         p.logfn = logfn;
         p.ctl = ctl;
         p.part = part;
-        p.half_sum = half_sum;
         p.means = means;
         p.data_len = data_len;
         p.params_len = (unsigned)(n_params - data_len);
@@ -274,6 +326,11 @@ struct bay_sampler {
         p.step_off = step_off;
         p.means_cap = (unsigned)std::min<uint64_t>(means_cap, 0xffffffffull);
         p.inv_W = (float)(1.0 / (double)W);
+        p.gemm_base = gemm_base;
+        p.gemm_rows = gemm_rows;
+        p.gemm_ld = model->gemm_ld;
+        p.gemm_np = gemm_np;
+        p.gemm_lay = gemm_lay;
         return p;
     }
 
@@ -282,7 +339,7 @@ struct bay_sampler {
         bay_stretch_params p = make_params(half, step_off);
         void* args[] = {&p};
         cu_check(g_cu.LaunchKernel((CUfunction)(accu ? model->k_accu : model->k_bare), grid(), 1, 1,
-                                model->cta, 1, 1, 0, (CUstream)st, args, nullptr),
+                                   model->cta, 1, 1, (unsigned)smem, (CUstream)st, args, nullptr),
                  "cuLaunchKernel(stretch)");
     }
 
@@ -294,25 +351,35 @@ struct bay_sampler {
         bay::count_launches(1);
         bay_stretch_params p = make_params(0, 0);
         void* args[] = {&p};
-        const uint64_t per = model->form == BAY_FORM_TILED ? model->wpc : model->cta;
-        const unsigned g = (unsigned)((W + per - 1) / per);
-        cu_check(g_cu.LaunchKernel((CUfunction)model->k_logfn, g, 1, 1, model->cta, 1, 1, 0,
-                                (CUstream)ctx->stream, args, nullptr),
+        const unsigned g = (unsigned)((W + per_cta() - 1) / per_cta());
+        cu_check(g_cu.LaunchKernel((CUfunction)model->k_logfn, g, 1, 1, model->cta, 1, 1,
+                                   (unsigned)smem, (CUstream)ctx->stream, args, nullptr),
                  "cuLaunchKernel(logfn)");
+    }
+
+    // m <= kChunk steps: the kernel pairs with step offsets 0..m-1, the per-step means
+    // of the accu steps (from the per-CTA sums), then the device step counter += m.
+    void run_chunk(bool accu, uint32_t m, cudaStream_t st) {
+        for (uint32_t i = 0; i < m; ++i) {
+            launch_half(accu, 0, i, st);
+            launch_half(accu, 1, i, st);
+        }
+        if (accu && means_cap)
+            cuda_check(bay::launch_reduce_means(ctl, part, means,
+                                                (uint32_t)std::min<uint64_t>(means_cap, 0xffffffffull),
+                                                grid(), D, m, 1.0 / (double)W, st),
+                       "reduce_means");
+        bay_ctl_op op{};
+        op.mask = accu ? BAY_CTL_ADD_STEP1 : BAY_CTL_ADD_STEP0;
+        op.step[accu ? 1 : 0] = m;
+        cuda_check(bay::launch_ctl_apply(ctl, op, st), "ctl_apply(step)");
     }
 
     cudaGraphExec_t capture_chunk(bool accu) {
         cudaStream_t cs = ctx->capture;
         cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "BeginCapture");
         try {
-            for (uint32_t i = 0; i < kChunk; ++i) {
-                launch_half(accu, 0, i, cs);
-                launch_half(accu, 1, i, cs);
-            }
-            bay_ctl_op op{};
-            op.mask = accu ? BAY_CTL_ADD_STEP1 : BAY_CTL_ADD_STEP0;
-            op.step[accu ? 1 : 0] = kChunk;
-            cuda_check(bay::launch_ctl_apply(ctl, op, cs), "ctl_apply(capture)");
+            run_chunk(accu, kChunk, cs);
         } catch (...) {
             cudaGraph_t g;
             cudaStreamEndCapture(cs, &g);
@@ -344,19 +411,13 @@ struct bay_sampler {
             }
             for (; done + kChunk <= n; done += kChunk) {
                 cuda_check(cudaGraphLaunch(ex, ctx->stream), "cudaGraphLaunch");
-                bay::count_launches(2 * kChunk + 1);
+                bay::count_launches(2 * kChunk + 1 + ((accu && means_cap) ? 1 : 0));
             }
         }
-        const uint64_t rest = n - done;
-        for (uint32_t i = 0; i < rest; ++i) {
-            launch_half(accu, 0, i, ctx->stream);
-            launch_half(accu, 1, i, ctx->stream);
-        }
-        if (rest) {
-            bay_ctl_op op{};
-            op.mask = accu ? BAY_CTL_ADD_STEP1 : BAY_CTL_ADD_STEP0;
-            op.step[accu ? 1 : 0] = (uint32_t)rest;
-            ctl_op(op);
+        while (done < n) {
+            const uint32_t m = (uint32_t)std::min<uint64_t>(kChunk, n - done);
+            run_chunk(accu, m, ctx->stream);
+            done += m;
         }
         if (accu) step_accu += (uint32_t)n;
         else step_bare += (uint32_t)n;
@@ -507,6 +568,7 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
     if (d->dim == 0 || d->dim > 4096) fail(BAY_ERR_ARG, "dim must be in [1, 4096]");
     Codegen g;
     uint32_t cta = d->cta_threads ? d->cta_threads : 256u;
+    if (d->form == BAY_FORM_GEMM) cta = 256;  // the GEMM tile assumes 16 x 16 thread groups
     if (cta % 32 || cta > 1024) fail(BAY_ERR_ARG, "cta_threads must be a multiple of 32, <= 1024");
     std::vector<std::string>& opts = g.opts;
     opts = {"-arch=sm_103a", "-use_fast_math", "-default-device", "-std=c++17", "-DREAL=float",
@@ -536,6 +598,27 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
         opts.push_back(std::string("-DBAY_TILE_PREP=") + d->tile_prep);
         opts.push_back(std::string("-DBAY_TILE_TERM=") + d->tile_term);
         opts.push_back(std::string("-DBAY_TILE_WALKER=") + d->tile_walker);
+    } else if (d->form == BAY_FORM_GEMM) {
+        if (!valid_ident(d->tile_prep) || !valid_ident(d->tile_term) ||
+            !valid_ident(d->tile_walker))
+            fail(BAY_ERR_ARG, "GEMM form needs tile_prep, tile_term and tile_walker names");
+        if (d->gemm_features == 0 || d->gemm_coef + d->gemm_features > d->dim)
+            fail(BAY_ERR_ARG, "gemm_coef + gemm_features must be within the walker dimension");
+        if (d->gemm_ld < d->gemm_features) fail(BAY_ERR_ARG, "gemm_ld must be >= gemm_features");
+        if (d->gemm_aux_len > 8 || (d->gemm_aux_len && d->gemm_aux_col + d->gemm_aux_len > d->gemm_ld))
+            fail(BAY_ERR_ARG, "aux columns must lie inside a row (at most 8)");
+        const uint32_t pl = d->prep_len ? d->prep_len : 1u;
+        if (pl > 64) fail(BAY_ERR_ARG, "prep_len must be <= 64");
+        opts.push_back("-DBAY_GEMM=1");
+        opts.push_back("-DBAY_GEMM_F=" + std::to_string(d->gemm_features));
+        opts.push_back("-DBAY_GEMM_COEF=" + std::to_string(d->gemm_coef));
+        opts.push_back("-DBAY_GEMM_AUX=" + std::to_string(d->gemm_aux_len));
+        opts.push_back("-DBAY_GEMM_AUXCOL=" + std::to_string(d->gemm_aux_col));
+        opts.push_back("-DBAY_PREP_LEN=" + std::to_string(pl));
+        opts.push_back(std::string("-DBAY_GEMM_PREP=") + d->tile_prep);
+        opts.push_back(std::string("-DBAY_GEMM_TERM=") + d->tile_term);
+        opts.push_back(std::string("-DBAY_GEMM_WALKER=") + d->tile_walker);
+        wpc = 64;
     } else {
         fail(BAY_ERR_ARG, "unknown model form");
     }
@@ -577,6 +660,15 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
         m->cta = g.cta;
         m->wpc = g.wpc;
         m->flags = d->flags;
+        if (d->form == BAY_FORM_GEMM) {
+            m->gemm_features = d->gemm_features;
+            m->gemm_block = d->gemm_block;
+            m->gemm_ld = d->gemm_ld;
+            m->gemm_aux_col = d->gemm_aux_col;
+            m->gemm_aux_len = d->gemm_aux_len;
+            m->gemm_offset = d->gemm_offset;
+            m->gemm_rows = d->gemm_rows;
+        }
         try {
             cu_check(g_cu.LibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr,
                                        nullptr, 0),
@@ -584,6 +676,13 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
             cu_check(g_cu.LibraryGetKernel(&m->k_bare, m->lib, "bay_stretch_bare"), "GetKernel(bare)");
             cu_check(g_cu.LibraryGetKernel(&m->k_accu, m->lib, "bay_stretch_accu"), "GetKernel(accu)");
             cu_check(g_cu.LibraryGetKernel(&m->k_logfn, m->lib, "bay_logfn_all"), "GetKernel(logfn)");
+            if (d->form == BAY_FORM_GEMM) {
+                CUdevice dev = (CUdevice)c->device;
+                for (CUkernel k : {m->k_bare, m->k_accu, m->k_logfn})
+                    cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                     (int)kGemmMaxSmem, k, dev),
+                             "cuKernelSetAttribute(smem)");
+            }
         } catch (...) {
             if (m->lib) g_cu.LibraryUnload(m->lib);
             delete m;
@@ -626,12 +725,36 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
         s->D = m->dim;
         s->n_params = n_params;
         s->data_len = n_params - m->params_size;
+        if (m->form == BAY_FORM_GEMM) {
+            const uint64_t block = m->gemm_block ? s->data_len : 0;
+            const uint64_t block_len = m->gemm_block ? m->params_size : s->data_len;
+            if (m->gemm_offset > block_len) {
+                delete s;
+                fail(BAY_ERR_ARG, "gemm_offset lies past the end of its params block");
+            }
+            s->gemm_base = block + m->gemm_offset;
+            s->gemm_rows = m->gemm_rows ? m->gemm_rows : (block_len - m->gemm_offset) / m->gemm_ld;
+            const uint64_t row_need = std::max<uint64_t>(m->gemm_features,
+                                                         m->gemm_aux_col + m->gemm_aux_len);
+            if (s->gemm_rows == 0 ||
+                m->gemm_offset + (s->gemm_rows - 1) * m->gemm_ld + row_need > block_len) {
+                delete s;
+                fail(BAY_ERR_ARG, "the GEMM matrix does not fit its params block");
+            }
+            s->smem = gemm_smem_bytes(m, s->gemm_rows);
+            if (s->smem > kGemmMaxSmem) {
+                delete s;
+                fail(BAY_ERR_ARG, "GEMM matrix of " + std::to_string(s->gemm_rows) + " x " +
+                                      std::to_string(m->gemm_features) +
+                                      " does not fit in shared memory (the resident GEMM form holds "
+                                      "up to about 40960 values)");
+            }
+        }
         try {
             s->xs = (float*)c->alloc(sizeof(float) * (size_t)s->D * walkers);
             s->logfn = (float*)c->alloc(sizeof(float) * walkers);
             s->ctl = (bay_ctl*)c->alloc(sizeof(bay_ctl));
-            s->part = (double*)c->alloc(sizeof(double) * (size_t)s->grid() * s->D);
-            s->half_sum = (double*)c->alloc(sizeof(double) * s->D);
+            s->part = (float*)c->alloc(sizeof(float) * kChunk * 2 * (size_t)s->grid() * s->D);
             s->stats = (double*)c->alloc(sizeof(double) * 2 * s->D);
             cuda_check(cudaMemsetAsync(s->ctl, 0, sizeof(bay_ctl), c->stream), "memset");
             cuda_check(cudaMemsetAsync(s->xs, 0, sizeof(float) * (size_t)s->D * walkers, c->stream),
@@ -648,6 +771,17 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                                "cudaMemcpy(params)");
                 s->params = p;
                 s->own_params = true;
+            }
+            if (m->form == BAY_FORM_GEMM) {
+                s->gemm_np = (uint32_t)((s->gemm_rows + 63) & ~63ull);
+                const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
+                s->gemm_lay = (float*)c->alloc(
+                    sizeof(float) * ((size_t)m->gemm_features * s->gemm_np + (size_t)s->gemm_np * auxs));
+                cuda_check(bay::launch_gemm_layout(s->params + s->gemm_base, m->gemm_ld,
+                                                   (uint32_t)s->gemm_rows, m->gemm_features,
+                                                   s->gemm_np, m->gemm_aux_col, m->gemm_aux_len,
+                                                   auxs, s->gemm_lay, c->stream),
+                           "gemm_layout");
             }
             s->ensure_means(1);
             // init! (nvidia_gtx.clj:391-400)
@@ -667,9 +801,9 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
             c->release(s->logfn);
             c->release(s->ctl);
             c->release(s->part);
-            c->release(s->half_sum);
             c->release(s->stats);
             c->release(s->means);
+            c->release(s->gemm_lay);
             if (s->own_params) c->release((void*)s->params);
             delete s;
             throw;
@@ -700,12 +834,12 @@ int bay_sampler_release(bay_sampler* s) {
         c->release(s->logfn);
         c->release(s->ctl);
         c->release(s->part);
-        c->release(s->half_sum);
         c->release(s->stats);
         c->release(s->means);
         c->release(s->stage);
         c->release(s->hist);
         c->release(s->counts);
+        c->release(s->gemm_lay);
         if (s->own_params) c->release((void*)s->params);
         delete s;
     });
@@ -810,11 +944,9 @@ int bay_init_position_host(bay_sampler* s, const float* positions) {
         if (!s || !positions) fail(BAY_ERR_ARG, "NULL argument");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
         s->ctx->use();
-        if (!s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
-        cuda_check(cudaMemcpyAsync(s->stage, positions, sizeof(float) * (size_t)s->D * s->W,
+        cuda_check(cudaMemcpyAsync(s->xs, positions, sizeof(float) * (size_t)s->D * s->W,
                                    cudaMemcpyDefault, s->ctx->stream),
                    "cudaMemcpy(positions)");
-        cuda_check(bay::launch_aos_to_soa(s->stage, s->D, s->W, s->xs, s->ctx->stream), "aos_to_soa");
         s->launch_logfn_all();
         cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
         s->positioned = true;
@@ -872,6 +1004,7 @@ uint64_t read_accepted(bay_sampler* s) {
                                s->ctx->stream),
                "cudaMemcpy(accepted)");
     cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+    s->check_status();
     return v;
 }
 
@@ -970,22 +1103,16 @@ int bay_sample(bay_sampler* s, uint64_t n_cols, float* out) {
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
         s->ctx->use();
         s->require_positions();
-        const bool dev = is_device_ptr(out);
-        if (!dev && !s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
         s->set_a_beta(s->a, 1.0f);
         uint64_t ofs = 0;
         while (ofs < n_cols) {
             s->steps(false, 1);
             s->iteration_counter += 1;
             const uint64_t take = std::min<uint64_t>(s->W, n_cols - ofs);
-            float* dst = dev ? out + ofs * s->D : s->stage;
-            cuda_check(bay::launch_soa_to_aos(s->xs, s->D, s->W, 0, take, dst, s->ctx->stream),
-                       "soa_to_aos");
-            if (!dev)
-                cuda_check(cudaMemcpyAsync(out + ofs * s->D, s->stage, sizeof(float) * take * s->D,
-                                           cudaMemcpyDeviceToHost, s->ctx->stream),
-                           "cudaMemcpy(sample)");
-            if (!dev) cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+            // the walker state is the reference's dim x walkers column-major layout
+            cuda_check(cudaMemcpyAsync(out + ofs * s->D, s->xs, sizeof(float) * take * s->D,
+                                       cudaMemcpyDefault, s->ctx->stream),
+                       "cudaMemcpy(sample)");
             ofs += take;
         }
         cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
@@ -998,12 +1125,14 @@ static int moments_out(bay_sampler* s, double* out, int which) {
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
         s->ctx->use();
         s->require_positions();
-        cuda_check(bay::launch_moments(s->xs, s->D, s->W, s->stats, s->stats + s->D, s->ctx->stream),
+        cuda_check(bay::launch_moments(s->dim_major(), s->D, s->W, s->stats, s->stats + s->D,
+                                       s->ctx->stream),
                    "moments");
         cuda_check(cudaMemcpyAsync(out, s->stats + (which ? s->D : 0), sizeof(double) * s->D,
                                    cudaMemcpyDefault, s->ctx->stream),
                    "cudaMemcpy(moments)");
         cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+        s->check_status();
         if (which == 2 && !is_device_ptr(out))
             for (uint32_t d = 0; d < s->D; ++d) out[d] = std::sqrt(out[d]);
     });
@@ -1058,18 +1187,19 @@ int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags
                 cnt = (cnt + B - 1) / B;
             } while (cnt > 1);
         }
-        cuda_check(bay::launch_minmax(s->xs, s->D, s->W, zero, d_lim, c->stream), "minmax");
+        const float* dm = s->dim_major();
+        cuda_check(bay::launch_minmax(dm, s->D, s->W, zero, d_lim, c->stream), "minmax");
         cuda_check(bay::launch_fill_u32(s->counts, (flags & BAY_HIST_COMPAT_START1) ? 1u : 0u,
                                         (uint64_t)bins * s->D, c->stream),
                    "fill");
-        cuda_check(bay::launch_hist_count(s->xs, s->D, s->W, bins, d_lim, s->counts, c->stream),
+        cuda_check(bay::launch_hist_count(dm, s->D, s->W, bins, d_lim, s->counts, c->stream),
                    "histogram");
         if (cycles > 1) {
             s->set_a_beta(s->a, 1.0f);
             for (uint32_t i = 1; i < cycles; ++i) {
                 s->steps(false, 1);
-                cuda_check(bay::launch_hist_count(s->xs, s->D, s->W, bins, d_lim, s->counts,
-                                                  c->stream),
+                cuda_check(bay::launch_hist_count(s->dim_major(), s->D, s->W, bins, d_lim,
+                                                  s->counts, c->stream),
                            "histogram");
             }
             s->iteration_counter += cycles - 1;
@@ -1152,14 +1282,10 @@ int bay_state_export(bay_sampler* s, float* positions, float* logfn, uint32_t* r
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
         s->ctx->use();
         s->require_positions();
-        if (positions) {
-            if (!s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
-            cuda_check(bay::launch_soa_to_aos(s->xs, s->D, s->W, 0, s->W, s->stage, s->ctx->stream),
-                       "soa_to_aos");
-            cuda_check(cudaMemcpyAsync(positions, s->stage, sizeof(float) * (size_t)s->D * s->W,
+        if (positions)
+            cuda_check(cudaMemcpyAsync(positions, s->xs, sizeof(float) * (size_t)s->D * s->W,
                                        cudaMemcpyDefault, s->ctx->stream),
                        "copy");
-        }
         if (logfn)
             cuda_check(cudaMemcpyAsync(logfn, s->logfn, sizeof(float) * s->W, cudaMemcpyDefault,
                                        s->ctx->stream),
@@ -1184,11 +1310,9 @@ int bay_state_import(bay_sampler* s, const float* positions, const float* logfn,
         if (!s || !positions || !logfn || !rng) fail(BAY_ERR_ARG, "NULL argument");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
         s->ctx->use();
-        if (!s->stage) s->stage = (float*)s->ctx->alloc(sizeof(float) * (size_t)s->D * s->W);
-        cuda_check(cudaMemcpyAsync(s->stage, positions, sizeof(float) * (size_t)s->D * s->W,
+        cuda_check(cudaMemcpyAsync(s->xs, positions, sizeof(float) * (size_t)s->D * s->W,
                                    cudaMemcpyDefault, s->ctx->stream),
                    "copy");
-        cuda_check(bay::launch_aos_to_soa(s->stage, s->D, s->W, s->xs, s->ctx->stream), "aos_to_soa");
         cuda_check(cudaMemcpyAsync(s->logfn, logfn, sizeof(float) * s->W, cudaMemcpyDefault,
                                    s->ctx->stream),
                    "copy");

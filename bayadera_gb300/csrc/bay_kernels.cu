@@ -51,14 +51,13 @@ __global__ void ctl_apply(bay_ctl* c, bay_ctl_op op) {
 // init_walkers (nvidia-gtx-mcmc-stretch.cu:158-195): element e = w*D + d (the
 // reference's AoS index) takes word e%4 of Philox(ctr {e/4, 0xf00dcafe, 0xdeadbeef,
 // 0xbeeff00d}, key {seed, 0xdecafaaa}); x = u*hi + (1-u)*lo, first product fused.
-// Written here straight into the SoA slot xs[d*W + w] (coalesced).
+// The walker state is walker-major, so element e is written at xs[e] (coalesced).
 __global__ void init_uniform(float* xs, uint32_t D, uint64_t W, uint32_t seed,
                              const float* limits) {
     const uint64_t n = (uint64_t)D * W;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t d = i / W, w = i % W;
-        const uint64_t e = w * D + d;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t d = e % D;
         bay_u4 c;
         c.x = (unsigned)(e >> 2);
         c.y = 0xf00dcafeu;
@@ -68,7 +67,7 @@ __global__ void init_uniform(float* xs, uint32_t D, uint64_t W, uint32_t seed,
         const unsigned word = (e & 3) == 0 ? r.x : (e & 3) == 1 ? r.y : (e & 3) == 2 ? r.z : r.w;
         const float u = bay_u01(word);
         const float lo = limits[2 * d], hi = limits[2 * d + 1];
-        xs[i] = __fmaf_rn(u, hi, __fmul_rn(__fsub_rn(1.0f, u), lo));
+        xs[e] = __fmaf_rn(u, hi, __fmul_rn(__fsub_rn(1.0f, u), lo));
     }
 }
 
@@ -77,10 +76,8 @@ __global__ void init_uniform(float* xs, uint32_t D, uint64_t W, uint32_t seed,
 __global__ void init_normal(float* xs, uint32_t D, uint64_t W, uint32_t seed, float mean,
                             float sd) {
     const uint64_t n = (uint64_t)D * W;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t d = i / W, w = i % W;
-        const uint64_t e = w * D + d;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+         e += (uint64_t)gridDim.x * blockDim.x) {
         bay_u4 c;
         c.x = (unsigned)(e >> 1);
         c.y = 0x6e6f726du;
@@ -90,7 +87,7 @@ __global__ void init_normal(float* xs, uint32_t D, uint64_t W, uint32_t seed, fl
         const double rr = sqrt(-2.0 * log((double)bay_u01(r.y)));
         const double t = 6.283185307179586 * (double)bay_u01(r.x);
         const double z = (e & 1) ? rr * sin(t) : rr * cos(t);
-        xs[i] = (float)((double)mean + (double)sd * z);
+        xs[e] = (float)((double)mean + (double)sd * z);
     }
 }
 
@@ -236,6 +233,42 @@ __global__ void hist_finish(const uint32_t* counts, const float* limits, uint32_
         }
     }
     ranks[(uint64_t)d * bins + lid] = v.x;
+}
+
+// One CTA per (step, dim): the 2 x G per-CTA sums part[((t*2 + h)*D + d)*G + b] read
+// coalesced along b, summed in FP64 in a fixed order.
+__global__ void reduce_means(const bay_ctl* ctl, const float* part, float* means,
+                             uint32_t means_cap, uint32_t G, uint32_t D, double inv_W) {
+    __shared__ double red[33];
+    const uint32_t t = blockIdx.x, d = blockIdx.y;
+    const uint32_t step = ctl->step[1] + t;
+    double s = 0.0;
+    for (uint32_t h = 0; h < 2; ++h) {
+        const float* p = part + (((size_t)t * 2 + h) * D + d) * G;
+        for (uint32_t b = threadIdx.x; b < G; b += blockDim.x) s += (double)p[b];
+    }
+    s = block_sum_d(s, red);
+    if (threadIdx.x == 0 && step < means_cap) means[(size_t)step * D + d] = (float)(s * inv_W);
+}
+
+// The GEMM form's matrix laid out once per sampler: lay[f*NP + r] = A[r][f] (rows past
+// `rows` zero), then lay[F*NP + r*auxs + c] = A[r][aux_col + c].
+__global__ void gemm_layout(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t NP,
+                            uint32_t aux_col, uint32_t aux_len, uint32_t auxs, float* lay) {
+    const uint64_t nA = (uint64_t)F * NP;
+    const uint64_t n = nA + (uint64_t)NP * auxs;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        float v = 0.0f;
+        if (i < nA) {
+            const uint64_t f = i / NP, r = i % NP;
+            if (r < rows) v = A[r * ld + f];
+        } else {
+            const uint64_t e = i - nA, r = e / auxs, c = e % auxs;
+            if (r < rows && c < aux_len) v = A[r * ld + aux_col + c];
+        }
+        lay[i] = v;
+    }
 }
 
 __global__ void fill_u32(uint32_t* p, uint32_t v, uint64_t n) {
@@ -405,6 +438,25 @@ cudaError_t launch_hist_finish(const uint32_t* counts, const float* limits, uint
                                cudaStream_t s) {
     const float alpha = (float)((double)bins / (double)n);
     hist_finish<<<D, bins, bins * sizeof(float2), s>>>(counts, limits, bins, alpha, pdf, ranks);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_means(const bay_ctl* ctl, const float* part, float* means,
+                                uint32_t means_cap, uint32_t G, uint32_t D, uint32_t nsteps,
+                                double inv_W, cudaStream_t s) {
+    if (nsteps == 0) return cudaSuccess;
+    dim3 grid(nsteps, D);
+    reduce_means<<<grid, 128, 0, s>>>(ctl, part, means, means_cap, G, D, inv_W);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_layout(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t NP,
+                               uint32_t aux_col, uint32_t aux_len, uint32_t auxs, float* lay,
+                               cudaStream_t s) {
+    const uint64_t n = (uint64_t)F * NP + (uint64_t)NP * auxs;
+    gemm_layout<<<grid_for(n, 256), 256, 0, s>>>(A, ld, rows, F, NP, aux_col, aux_len, auxs, lay);
     g_launches++;
     return cudaGetLastError();
 }

@@ -24,8 +24,7 @@ struct bay_stretch_params {
     float* xs;
     float* logfn;
     bay_ctl* ctl;
-    double* part;
-    double* half_sum;
+    float* part;
     float* means;
     unsigned long long data_len;
     unsigned int params_len;
@@ -34,6 +33,11 @@ struct bay_stretch_params {
     unsigned int step_off;
     unsigned int means_cap;
     float inv_W;
+    unsigned long long gemm_base;
+    unsigned long long gemm_rows;
+    unsigned int gemm_ld;
+    unsigned int gemm_np;
+    const float* gemm_lay;
 };
 
 enum {
@@ -82,6 +86,17 @@ cudaError_t launch_hist_finish(const uint32_t* counts, const float* limits, uint
                                uint32_t bins, uint64_t n, float* pdf, float* ranks,
                                cudaStream_t s);
 cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, uint64_t n, cudaStream_t s);
+// The GEMM form's matrix (rows x F at A, row stride ld, aux values at column aux_col)
+// laid out feature-major with rows zero-padded to NP, then the aux values [NP][auxs].
+cudaError_t launch_gemm_layout(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t NP,
+                               uint32_t aux_col, uint32_t aux_len, uint32_t auxs, float* lay,
+                               cudaStream_t s);
+// Per-step ensemble means of `nsteps` accu steps from the stretch kernels' per-CTA sums
+// part[((t*2 + half)*D + d)*G + cta]: means[(ctl->step[1] + t)*D + d] = sum / W, summed
+// in FP64 in (half, cta) order; steps at or past means_cap are dropped.
+cudaError_t launch_reduce_means(const bay_ctl* ctl, const float* part, float* means,
+                                uint32_t means_cap, uint32_t G, uint32_t D, uint32_t nsteps,
+                                double inv_W, cudaStream_t s);
 // acor of a D x n column-major series (series[t*D + d]); work holds D*n doubles.
 cudaError_t launch_acor(const float* series, uint32_t D, uint32_t n, uint32_t wgs, uint32_t lag,
                         double* work, double* tau, double* mean, double* sigma, cudaStream_t s);

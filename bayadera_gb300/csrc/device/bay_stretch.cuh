@@ -11,7 +11,7 @@
 // {k, step, stream, 0xbeeff00d}; stream 3333/4444 (bare) and 1111/2222 (accu) for
 // halves 0/1; seed_h = seed (half 0) or seed + 1 (half 1).
 //
-// Layout (both forms): positions structure-of-arrays, xs[d * W + w] (W walkers,
+// Layout (all forms): positions walker-major, xs[w * DIM + d] (W walkers,
 // half h = walkers [h*K, h*K + K)); logfn contiguous, logfn[w].
 //
 // Macros supplied by the host when it compiles a model:
@@ -36,6 +36,9 @@
 #ifndef BAY_TILED
 #define BAY_TILED 0
 #endif
+#ifndef BAY_GEMM
+#define BAY_GEMM 0
+#endif
 
 // Sampler control block, resident in device memory so that captured CUDA graphs
 // replay without parameter patching.
@@ -52,12 +55,11 @@ struct bay_ctl {
 
 struct bay_stretch_params {
     const float* params;            // data || hyperparameters
-    float* xs;                      // SoA positions
+    float* xs;                      // positions, walker-major xs[w * DIM + d]
     float* logfn;                   // W log densities
     bay_ctl* ctl;
-    double* part;                   // accu: per-CTA partial sums [gridDim.x][DIM]
-    double* half_sum;               // accu: [DIM] sums of half 0, consumed by half 1
-    float* means;                   // accu: per-step ensemble means, means[step*DIM + d]
+    float* part;                    // accu: per-CTA sums [step_off][half][DIM][cta]
+    float* means;                   // unused by the stretch kernels (reduce_means writes it)
     unsigned long long data_len;    // floats of data in params
     unsigned int params_len;        // hyperparameters after the data
     unsigned int W, K;
@@ -65,6 +67,14 @@ struct bay_stretch_params {
     unsigned int step_off;          // added to the device step counter
     unsigned int means_cap;         // steps the means buffer holds
     float inv_W;
+    // GEMM form: matrix rows at params + gemm_base + r * gemm_ld, r < gemm_rows; the
+    // sampler's copy laid out for the kernel: gemm_lay = [F][NP] feature-major, rows
+    // zero-padded to NP (a multiple of 64), then [NP][aux] row-major
+    unsigned long long gemm_base;
+    unsigned long long gemm_rows;
+    unsigned int gemm_ld;
+    unsigned int gemm_np;
+    const float* gemm_lay;
 };
 
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
@@ -95,54 +105,350 @@ __device__ __forceinline__ bool bay_accept(float u2, float z, float ly, float lx
 #endif
 }
 
-// Per-CTA sum of one value per thread (fp32 within warps, FP64 across warps), result
-// valid in thread 0.  Fixed order: deterministic.
-__device__ __forceinline__ double bay_cta_sum(float v, double* red) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) red[warp] = (double)v;
-    __syncthreads();
-    double s = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-    __syncthreads();
-    return s;
+// Compensated fp32 pairs (hi, lo), hi + lo the value: sums carried without FP64 (FP64
+// issue is a small fraction of FP32 on this part).  bay_cadd is symmetric in its
+// arguments (TwoSum of the highs, then the lows), so an xor-butterfly of it leaves the
+// same bits in every lane: the combine order is fixed and the result deterministic.
+struct bay_cf {
+    float hi, lo;
+};
+__device__ __forceinline__ bay_cf bay_cadd(bay_cf a, bay_cf b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+    const float hi = __fadd_rn(s, lo);
+    bay_cf r;
+    r.hi = hi;
+    r.lo = __fsub_rn(lo, __fsub_rn(hi, s));
+    return r;
+}
+__device__ __forceinline__ bay_cf bay_cf_shfl_xor(bay_cf v, int o) {
+    bay_cf r;
+    r.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    r.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    return r;
+}
+// a + (s.hi + s.lo), rounded once to fp32
+__device__ __forceinline__ float bay_cf_total(float a, bay_cf s) {
+    bay_cf t;
+    t.hi = a;
+    t.lo = 0.0f;
+    t = bay_cadd(t, s);
+    return __fadd_rn(t.hi, t.lo);
 }
 
-// Accu epilogue: per-CTA accept count and per-dim sums of the moved half, reduced
-// across CTAs by the last CTA to finish (ticket), in CTA order.  Half 0 parks its
-// sums in half_sum; half 1 adds them and writes the step's ensemble means.
+// Accu epilogue: the CTA's accept count (one 64-bit atomic, integer: deterministic) and,
+// when per-step means are wanted, the CTA's per-dim sums of the moved half: fp32 warp
+// shuffles, per-warp sums staged in shared memory (one barrier per 64 dims), combined
+// across warps with compensated fp32 in warp order, stored to part[(step_off*2 + half)][dim][cta].  The
+// per-step ensemble means are reduced from these partials by a separate kernel.
+#define BAY_SUM_CHUNK 64
 __device__ void bay_accu_epilogue(const bay_stretch_params& P, bool accepted, bool valid,
-                                  const float* mine, unsigned int step, double* red) {
+                                  const float* mine, float (*red)[BAY_SUM_CHUNK]) {
     const int n_acc = __syncthreads_count(accepted);
     if (threadIdx.x == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
-    for (int d = 0; d < DIM; ++d) {
-        const double s = bay_cta_sum(valid ? mine[d] : 0.0f, red);
-        if (threadIdx.x == 0) P.part[(size_t)blockIdx.x * DIM + d] = s;
-    }
-    __shared__ bool last;
-    __threadfence();
-    if (threadIdx.x == 0) {
-        const unsigned int t = atomicAdd(&P.ctl->ticket[P.half], 1u);
-        last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    for (int d = threadIdx.x; d < DIM; d += blockDim.x) {
-        double s = 0.0;
-        for (unsigned int b = 0; b < gridDim.x; ++b) s += ((volatile double*)P.part)[(size_t)b * DIM + d];
-        if (P.half == 0) {
-            P.half_sum[d] = s;
-        } else if (step < P.means_cap) {
-            P.means[(size_t)step * DIM + d] = (float)((P.half_sum[d] + s) * (double)P.inv_W);
+    if (P.means_cap == 0) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x + blockIdx.x;
+#pragma unroll
+    for (int d0 = 0; d0 < DIM; d0 += BAY_SUM_CHUNK) {
+#pragma unroll
+        for (int d = d0; d < DIM && d < d0 + BAY_SUM_CHUNK; ++d) {
+            float v = valid ? mine[d] : 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp][d - d0] = v;
         }
+        __syncthreads();
+        const int nd = (DIM - d0) < BAY_SUM_CHUNK ? (DIM - d0) : BAY_SUM_CHUNK;
+        for (int d = threadIdx.x; d < nd; d += blockDim.x) {
+            bay_cf s;
+            s.hi = 0.0f;
+            s.lo = 0.0f;
+            for (int w = 0; w < nwarps; ++w) {
+                bay_cf y;
+                y.hi = red[w][d];
+                y.lo = 0.0f;
+                s = bay_cadd(s, y);
+            }
+            out[(size_t)(d0 + d) * gridDim.x] = __fadd_rn(s.hi, s.lo);
+        }
+        __syncthreads();
     }
-    if (threadIdx.x == 0) P.ctl->ticket[P.half] = 0;
 }
 
-#if !BAY_TILED
+#if BAY_GEMM
+// ---------------------------------------------------------------- GEMM form
+// log density = BAY_GEMM_WALKER(rows, hyper, hyper_len, dim, x)
+//             + sum_r BAY_GEMM_TERM(eta_r, aux_r, r, x, prep),   eta = A x[COEF : COEF+F],
+// A = the rows x F matrix at params + gemm_base (row stride gemm_ld; aux values of row r
+// at column BAY_GEMM_AUXCOL).  A CTA owns BAY_WT walkers.  The matrix (feature-major,
+// rows padded to 64) and the proposal tile are staged in shared memory once; each of
+// the 256 threads accumulates a 4-walker x 4-row register tile over the F features (two
+// 16-byte shared loads per 16 FMAs), applies the row term with a Kahan sum, and the 16
+// row-group lanes of a walker combine as compensated fp32 pairs in a fixed xor order.
+#define BAY_WT 64
+#define BAY_RW 4
+#define BAY_RN 4
+#define BAY_NG 16
+#define BAY_ROWS_PER_PASS (BAY_NG * BAY_RN)
+#define BAY_DPAD (DIM | 1)
+#ifndef BAY_GEMM_AUX
+#define BAY_GEMM_AUX 0
+#endif
+#define BAY_AUXS (BAY_GEMM_AUX > 0 ? BAY_GEMM_AUX : 1)
+
+template <bool ACCU, bool LOGFN_ONLY>
+__device__ __forceinline__ void bay_stretch_gemm(const bay_stretch_params& P) {
+    extern __shared__ __align__(128) float bay_smem[];
+    const unsigned int rows = (unsigned int)P.gemm_rows;
+    const unsigned int NP = P.gemm_np;
+    float* As = bay_smem;                              // [F][NP]   (the sampler's layout,
+    float* Aux = As + (size_t)BAY_GEMM_F * NP;         // [NP][AUXS] copied as one block)
+    float* Ys = Aux + (size_t)NP * BAY_AUXS;           // [F][BAY_WT]
+    float* Yw = Ys + BAY_GEMM_F * BAY_WT;              // [BAY_WT][BAY_DPAD]
+    __shared__ float sZ[BAY_WT], sU2[BAY_WT], sW[BAY_WT];
+    __shared__ unsigned int sJ[BAY_WT];
+    __shared__ float sPrep[BAY_WT][BAY_PREP_LEN];
+    __shared__ bay_cf sSum[BAY_WT];
+    __shared__ float sLx[BAY_WT];
+    __shared__ __align__(8) unsigned long long sBar;
+
+    const unsigned int kind = ACCU ? 1u : 0u;
+    const unsigned int tid = threadIdx.x;
+    const unsigned int k0 = blockIdx.x * BAY_WT;
+    const unsigned int nk = LOGFN_ONLY ? P.W : P.K;
+    const unsigned int step = P.ctl->step[kind] + P.step_off;
+    const float* hyper = P.params + P.data_len;
+    float* X = P.xs + (LOGFN_ONLY ? 0 : (size_t)P.half * P.K * DIM);
+    const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM;
+
+    // 1. one TMA bulk copy (cp.async.bulk, completion counted on an mbarrier) brings the
+    //    laid-out matrix and aux values into shared memory; it overlaps the proposals.
+    const unsigned int lay_bytes =
+        (unsigned int)(((size_t)BAY_GEMM_F * NP + (size_t)NP * BAY_AUXS) * sizeof(float));
+    const unsigned int bar = (unsigned int)__cvta_generic_to_shared(&sBar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                     "r"(lay_bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+            ::"r"((unsigned int)__cvta_generic_to_shared(As)), "l"(P.gemm_lay), "r"(lay_bytes),
+            "r"(bar) : "memory");
+    }
+    // 2. proposals (Philox, z, partner) for the tile, then Y in both layouts; each thread
+    //    keeps all its gather loads in flight before it uses any of them
+    if (!LOGFN_ONLY && tid < BAY_WT) {
+        const unsigned int k = k0 + tid;
+        if (k < nk) {
+            const unsigned int stream = ACCU ? (P.half ? 2222u : 1111u) : (P.half ? 4444u : 3333u);
+            bay_u4 c;
+            c.x = k;
+            c.y = step;
+            c.z = stream;
+            c.w = 0xbeeff00du;
+            const bay_u4 r = bay_philox4x32_10(c, P.ctl->seed[kind] + P.half, 0xdecafbadu);
+            const float z = bay_stretch_z(P.ctl->a, bay_u01(r.y));
+            sZ[tid] = z;
+            sJ[tid] = bay_partner(bay_u01(r.x), P.K);
+            sU2[tid] = bay_u01(r.z);
+            sLx[tid] = P.logfn[(size_t)P.half * P.K + k];
+        }
+    }
+    __syncthreads();
+    {
+        // The tile's own rows are one contiguous block of BAY_WT * DIM floats; element e is
+        // (walker e / DIM, coordinate e % DIM), so a warp reads its own elements coalesced
+        // and each partner row (DIM contiguous floats) in runs of consecutive coordinates.
+        constexpr int NE = (BAY_WT * DIM + 255) / 256;   // elements per thread
+        constexpr int CH = 16;                            // loads kept in flight per batch
+        const float* Xt = X + (size_t)k0 * DIM;
+        const unsigned int n_own = (nk - k0 < BAY_WT ? nk - k0 : BAY_WT) * DIM;
+#pragma unroll
+        for (int c0 = 0; c0 < NE; c0 += CH) {
+            float xv[CH], sv[CH];
+#pragma unroll
+            for (int i = 0; i < CH; ++i) {
+                const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
+                const unsigned int w = e / DIM, d = e - w * DIM;
+                const bool ev = (c0 + i < NE) && e < n_own;
+                xv[i] = ev ? Xt[e] : 0.0f;
+                sv[i] = (!LOGFN_ONLY && ev) ? S[(size_t)sJ[w] * DIM + d] : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < CH; ++i) {
+                const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
+                if ((c0 + i < NE) && e < BAY_WT * DIM) {
+                    const unsigned int w = e / DIM, d = e - w * DIM;
+                    const float y = LOGFN_ONLY ? xv[i]
+                        : (e < n_own ? __fmaf_rn(sZ[w], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
+                    Yw[w * BAY_DPAD + d] = y;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // feature-major copy of the coefficient block for the register tiles (bank-conflict
+    // free: consecutive lanes write consecutive walkers and read rows of odd stride)
+    for (unsigned int e = tid; e < BAY_GEMM_F * BAY_WT; e += blockDim.x) {
+        const unsigned int f = e / BAY_WT, w = e - f * BAY_WT;
+        Ys[e] = Yw[w * BAY_DPAD + BAY_GEMM_COEF + f];
+    }
+    // the matrix copy: bounded wait; a CTA-uniform timeout flags the sampler and exits
+    {
+        unsigned int done = 0;
+        for (unsigned int it = 0; it < (1u << 22) && !done; ++it)
+            asm volatile(
+                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                " selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done) : "r"(bar), "r"(0u) : "memory");
+        if (__syncthreads_or(!done)) {
+            if (tid == 0) atomicOr(&P.ctl->status, 1u);
+            return;
+        }
+    }
+    // 3. per-walker precompute and the terms outside the row sum
+    if (tid < BAY_WT) {
+        float pr[BAY_PREP_LEN];
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) pr[i] = 0.0f;
+        float wt = 0.0f;
+        if (k0 + tid < nk) {
+            BAY_GEMM_PREP(hyper, P.params_len, DIM, &Yw[tid * BAY_DPAD], pr);
+            wt = BAY_GEMM_WALKER(P.gemm_rows, hyper, P.params_len, DIM, &Yw[tid * BAY_DPAD]);
+        }
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) sPrep[tid][i] = pr[i];
+        sW[tid] = wt;
+    }
+    __syncthreads();
+    // 4. eta tiles and row terms
+    const unsigned int wg = tid / BAY_NG, rg = tid - wg * BAY_NG;
+    const unsigned int w0 = wg * BAY_RW;
+    float sum[BAY_RW], cmp[BAY_RW];
+#pragma unroll
+    for (int i = 0; i < BAY_RW; ++i) {
+        sum[i] = 0.0f;
+        cmp[i] = 0.0f;
+    }
+    for (unsigned int r0 = 0; r0 < NP; r0 += BAY_ROWS_PER_PASS) {
+        const unsigned int n0 = r0 + rg * BAY_RN;
+        float acc[BAY_RW][BAY_RN];
+#pragma unroll
+        for (int i = 0; i < BAY_RW; ++i)
+#pragma unroll
+            for (int j = 0; j < BAY_RN; ++j) acc[i][j] = 0.0f;
+#pragma unroll 5
+        for (int f = 0; f < BAY_GEMM_F; ++f) {
+            const float4 y = *reinterpret_cast<const float4*>(&Ys[f * BAY_WT + w0]);
+            const float4 a = *reinterpret_cast<const float4*>(&As[(size_t)f * NP + n0]);
+            const float yv[4] = {y.x, y.y, y.z, y.w};
+            const float av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+            for (int i = 0; i < BAY_RW; ++i)
+#pragma unroll
+                for (int j = 0; j < BAY_RN; ++j) acc[i][j] = __fmaf_rn(av[j], yv[i], acc[i][j]);
+        }
+#pragma unroll
+        for (int j = 0; j < BAY_RN; ++j) {
+            const unsigned int r = n0 + j;
+            if (r < rows) {
+#pragma unroll
+                for (int i = 0; i < BAY_RW; ++i) {
+                    const float t = BAY_GEMM_TERM(acc[i][j], &Aux[(size_t)r * BAY_AUXS], (uint64_t)r,
+                                                  &Yw[(w0 + i) * BAY_DPAD], sPrep[w0 + i]);
+                    const float yk = __fsub_rn(t, cmp[i]);
+                    const float s2 = __fadd_rn(sum[i], yk);
+                    cmp[i] = __fsub_rn(__fsub_rn(s2, sum[i]), yk);
+                    sum[i] = s2;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < BAY_RW; ++i) {
+        bay_cf v;
+        v.hi = sum[i];
+        v.lo = -cmp[i];
+#pragma unroll
+        for (int o = BAY_NG / 2; o > 0; o >>= 1) v = bay_cadd(v, bay_cf_shfl_xor(v, o));
+        if (rg == 0) sSum[w0 + i] = v;
+    }
+    __syncthreads();
+    // 5. accept (one thread per walker), then the tile's rows written back cooperatively
+    //    (accepted walkers' proposals; for the accu statistics the rejected walkers' current
+    //    rows are copied into the tile), statistics
+    __shared__ unsigned char sAcc[BAY_WT];
+    const unsigned int k = k0 + tid;
+    const bool valid = tid < BAY_WT && k < nk;
+    bool accepted = false;
+    if (valid) {
+        bay_cf t;
+        t.hi = sW[tid];
+        t.lo = 0.0f;
+        t = bay_cadd(t, sSum[tid]);
+        const float ly = __fadd_rn(t.hi, t.lo);
+        if (LOGFN_ONLY) {
+            P.logfn[k] = ly;
+        } else {
+            accepted = bay_accept(sU2[tid], sZ[tid], ly, sLx[tid], ACCU ? 1.0f : P.ctl->beta);
+            if (accepted) P.logfn[(size_t)P.half * P.K + k] = ly;
+        }
+    }
+    if (LOGFN_ONLY) return;
+    if (tid < BAY_WT) sAcc[tid] = accepted ? 1 : 0;
+    const int n_acc = __syncthreads_count(accepted);
+    {
+        float* Xt = X + (size_t)k0 * DIM;
+        const unsigned int n_own = (nk - k0 < BAY_WT ? nk - k0 : BAY_WT) * DIM;
+        for (unsigned int e = tid; e < n_own; e += blockDim.x) {
+            const unsigned int w = e / DIM, d = e - w * DIM;
+            if (sAcc[w]) Xt[e] = Yw[w * BAY_DPAD + d];
+            else if (ACCU) Yw[w * BAY_DPAD + d] = Xt[e];
+        }
+    }
+    if (ACCU) {
+        __syncthreads();
+        if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
+        if (P.means_cap != 0) {
+            float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x
+                + blockIdx.x;
+            const unsigned int nv = nk - k0 < BAY_WT ? nk - k0 : BAY_WT;
+            for (unsigned int d = tid; d < DIM; d += blockDim.x) {
+                bay_cf s;
+                s.hi = 0.0f;
+                s.lo = 0.0f;
+                for (unsigned int w = 0; w < nv; ++w) {
+                    bay_cf y;
+                    y.hi = Yw[w * BAY_DPAD + d];
+                    y.lo = 0.0f;
+                    s = bay_cadd(s, y);
+                }
+                out[(size_t)d * gridDim.x] = __fadd_rn(s.hi, s.lo);
+            }
+        }
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) bay_stretch_bare(bay_stretch_params P) {
+    bay_stretch_gemm<false, false>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_stretch_accu(bay_stretch_params P) {
+    bay_stretch_gemm<true, false>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_logfn_all(bay_stretch_params P) {
+    bay_stretch_gemm<false, true>(P);
+}
+
+#elif !BAY_TILED
 // ---------------------------------------------------------------- plain form
 // One thread per walker of the moving half, the model's LOGFN evaluated per thread
 // (the reference's structure, with SoA coalesced loads and registers for Y).
@@ -156,8 +462,8 @@ __device__ __forceinline__ void bay_stretch_plain(const bay_stretch_params& P) {
     const float a = P.ctl->a;
     const float beta = ACCU ? 1.0f : P.ctl->beta;
     const unsigned int stream = ACCU ? (P.half ? 2222u : 1111u) : (P.half ? 4444u : 3333u);
-    float* X = P.xs + (size_t)P.half * P.K;
-    const float* S = P.xs + (size_t)(1u - P.half) * P.K;
+    float* X = P.xs + (size_t)P.half * P.K * DIM;
+    const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM;
     float Y[DIM];
     bool accepted = false;
     if (valid) {
@@ -172,24 +478,24 @@ __device__ __forceinline__ void bay_stretch_plain(const bay_stretch_params& P) {
         const unsigned int j = bay_partner(u0, P.K);
 #pragma unroll
         for (int i = 0; i < DIM; ++i) {
-            const float s = S[(size_t)i * P.W + j];
-            Y[i] = __fmaf_rn(z, __fsub_rn(X[(size_t)i * P.W + k], s), s);
+            const float s = S[(size_t)j * DIM + i];
+            Y[i] = __fmaf_rn(z, __fsub_rn(X[(size_t)k * DIM + i], s), s);
         }
         const float ly = BAY_LOGFN((unsigned int)P.data_len, P.params_len, P.params, DIM, Y);
         const float lx = P.logfn[(size_t)P.half * P.K + k];
         accepted = bay_accept(u2, z, ly, lx, beta);
         if (accepted) {
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) X[(size_t)i * P.W + k] = Y[i];
+            for (int i = 0; i < DIM; ++i) X[(size_t)k * DIM + i] = Y[i];
             P.logfn[(size_t)P.half * P.K + k] = ly;
         } else if (ACCU) {
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) Y[i] = X[(size_t)i * P.W + k];
+            for (int i = 0; i < DIM; ++i) Y[i] = X[(size_t)k * DIM + i];
         }
     }
     if (ACCU) {
-        __shared__ double red[BAY_CTA / 32];
-        bay_accu_epilogue(P, accepted, valid, Y, step, red);
+        __shared__ float red[BAY_CTA / 32][BAY_SUM_CHUNK];
+        bay_accu_epilogue(P, accepted, valid, Y, red);
     }
 }
 
@@ -206,7 +512,7 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
     if (k >= P.W) return;
     float x[DIM];
 #pragma unroll
-    for (int i = 0; i < DIM; ++i) x[i] = P.xs[(size_t)i * P.W + k];
+    for (int i = 0; i < DIM; ++i) x[i] = P.xs[(size_t)k * DIM + i];
     P.logfn[k] = BAY_LOGFN((unsigned int)P.data_len, P.params_len, P.params, DIM, x);
 }
 
@@ -221,7 +527,7 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
 
 __device__ __forceinline__ void bay_tiled_logfn_rows(const bay_stretch_params& P,
                                                     const float (*prep)[BAY_PREP_LEN],
-                                                    double (*red)[BAY_WPC], double* out) {
+                                                    bay_cf (*red)[BAY_WPC], bay_cf* out) {
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     float acc[BAY_WPC], cmp[BAY_WPC], pv[BAY_WPC][BAY_PREP_LEN];
 #pragma unroll
@@ -249,15 +555,17 @@ __device__ __forceinline__ void bay_tiled_logfn_rows(const bay_stretch_params& P
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int w = 0; w < BAY_WPC; ++w) {
-        double v = (double)acc[w] - (double)cmp[w];
+        bay_cf v;
+        v.hi = acc[w];
+        v.lo = -cmp[w];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        for (int o = 16; o > 0; o >>= 1) v = bay_cadd(v, bay_cf_shfl_xor(v, o));
         if (lane == 0) red[warp][w] = v;
     }
     __syncthreads();
     if (threadIdx.x < BAY_WPC) {
-        double s = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i][threadIdx.x];
+        bay_cf s = red[0][threadIdx.x];
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) s = bay_cadd(s, red[i][threadIdx.x]);
         out[threadIdx.x] = s;
     }
     __syncthreads();
@@ -269,16 +577,16 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
     __shared__ float sY[BAY_WPC][DIM];
     __shared__ float sPrep[BAY_WPC][BAY_PREP_LEN];
     __shared__ float sW[BAY_WPC], sZ[BAY_WPC], sU2[BAY_WPC];
-    __shared__ double sRed[BAY_CTA / 32][BAY_WPC];
-    __shared__ double sSum[BAY_WPC];
-    __shared__ double red1[BAY_CTA / 32];
+    __shared__ bay_cf sRed[BAY_CTA / 32][BAY_WPC];
+    __shared__ bay_cf sSum[BAY_WPC];
+    __shared__ float red1[BAY_CTA / 32][BAY_SUM_CHUNK];
     const unsigned int step = P.ctl->step[kind] + P.step_off;
     const unsigned int seed = P.ctl->seed[kind] + P.half;
     const float a = P.ctl->a;
     const float beta = ACCU ? 1.0f : P.ctl->beta;
     const unsigned int stream = ACCU ? (P.half ? 2222u : 1111u) : (P.half ? 4444u : 3333u);
-    float* X = P.xs + (size_t)P.half * P.K;
-    const float* S = P.xs + (size_t)(1u - P.half) * P.K;
+    float* X = P.xs + (size_t)P.half * P.K * DIM;
+    const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM;
     const float* hyper = P.params + P.data_len;
     const unsigned int k0 = blockIdx.x * BAY_WPC;
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
@@ -298,8 +606,8 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
             float Y[DIM];
 #pragma unroll
             for (int i = 0; i < DIM; ++i) {
-                const float s = S[(size_t)i * P.W + j];
-                Y[i] = __fmaf_rn(z, __fsub_rn(X[(size_t)i * P.W + k], s), s);
+                const float s = S[(size_t)j * DIM + i];
+                Y[i] = __fmaf_rn(z, __fsub_rn(X[(size_t)k * DIM + i], s), s);
                 sY[t][i] = Y[i];
             }
             float pr[BAY_PREP_LEN];
@@ -322,20 +630,20 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
     const bool valid = t < BAY_WPC && k < P.K;
     float mine[DIM];
     if (valid) {
-        const float ly = (float)((double)sW[t] + sSum[t]);
+        const float ly = bay_cf_total(sW[t], sSum[t]);
         const float lx = P.logfn[(size_t)P.half * P.K + k];
         accepted = bay_accept(sU2[t], sZ[t], ly, lx, beta);
         if (accepted) {
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) X[(size_t)i * P.W + k] = sY[t][i];
+            for (int i = 0; i < DIM; ++i) X[(size_t)k * DIM + i] = sY[t][i];
             P.logfn[(size_t)P.half * P.K + k] = ly;
         }
         if (ACCU) {
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) mine[i] = accepted ? sY[t][i] : X[(size_t)i * P.W + k];
+            for (int i = 0; i < DIM; ++i) mine[i] = accepted ? sY[t][i] : X[(size_t)k * DIM + i];
         }
     }
-    if (ACCU) bay_accu_epilogue(P, accepted, valid, mine, step, red1);
+    if (ACCU) bay_accu_epilogue(P, accepted, valid, mine, red1);
 }
 
 extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_stretch_bare(bay_stretch_params P) {
@@ -349,8 +657,8 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_stretch_accu(bay_stret
 extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_params P) {
     __shared__ float sPrep[BAY_WPC][BAY_PREP_LEN];
     __shared__ float sW[BAY_WPC];
-    __shared__ double sRed[BAY_CTA / 32][BAY_WPC];
-    __shared__ double sSum[BAY_WPC];
+    __shared__ bay_cf sRed[BAY_CTA / 32][BAY_WPC];
+    __shared__ bay_cf sSum[BAY_WPC];
     const float* hyper = P.params + P.data_len;
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     const unsigned int k0 = blockIdx.x * BAY_WPC;
@@ -359,7 +667,7 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
         if (k < P.W) {
             float x[DIM];
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) x[i] = P.xs[(size_t)i * P.W + k];
+            for (int i = 0; i < DIM; ++i) x[i] = P.xs[(size_t)k * DIM + i];
             float pr[BAY_PREP_LEN];
             BAY_TILE_PREP(hyper, P.params_len, DIM, x, pr);
 #pragma unroll
@@ -374,6 +682,6 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
     __syncthreads();
     bay_tiled_logfn_rows(P, sPrep, sRed, sSum);
     const unsigned int t = threadIdx.x, k = k0 + t;
-    if (t < BAY_WPC && k < P.W) P.logfn[k] = (float)((double)sW[t] + sSum[t]);
+    if (t < BAY_WPC && k < P.W) P.logfn[k] = bay_cf_total(sW[t], sSum[t]);
 }
 #endif

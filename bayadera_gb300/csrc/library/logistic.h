@@ -20,4 +20,17 @@ inline REAL logistic_logpdf(const uint32_t data_len, const uint32_t hyper_len,
     for (uint32_t f = 0; f < dim; ++f) pr = fmaf(beta[f], beta[f], pr);
     return res - pr / (2.0f * sd * sd);
 }
+// GEMM form: A = the data rows' features, aux = y.
+inline void logistic_prep(const REAL* hyper, const uint32_t hyper_len, const uint32_t dim,
+                          const REAL* beta, REAL* prep) {}
+inline REAL logistic_term(const REAL eta, const REAL* aux, const uint64_t row, const REAL* beta,
+                          const REAL* prep) {
+    return fmaf(aux[0], eta, -logistic_softplus(eta));
+}
+inline REAL logistic_walker(const uint64_t rows, const REAL* hyper, const uint32_t hyper_len,
+                            const uint32_t dim, const REAL* beta) {
+    REAL pr = 0.0f;
+    for (uint32_t f = 0; f < dim; ++f) pr = fmaf(beta[f], beta[f], pr);
+    return -pr / (2.0f * hyper[0] * hyper[0]);
+}
 }

@@ -21,4 +21,23 @@ inline REAL robust_t_logpdf(const uint32_t data_len, const uint32_t hyper_len,
     for (uint32_t f = 0; f < F; ++f) pb = fmaf(x[f], x[f], pb);
     return res - (REAL)n * ls - pb / (2.0f * h[1] * h[1]) - ls * ls / (2.0f * h[2] * h[2]);
 }
+// GEMM form: A = the data rows' features, aux = y; prep = (1/sigma, nu).
+inline void robust_t_prep(const REAL* h, const uint32_t hyper_len, const uint32_t dim,
+                          const REAL* x, REAL* prep) {
+    prep[0] = expf(-x[dim - 1]);
+    prep[1] = h[0];
+}
+inline REAL robust_t_term(const REAL eta, const REAL* aux, const uint64_t row, const REAL* x,
+                          const REAL* prep) {
+    const REAL z = (aux[0] - eta) * prep[0];
+    return -0.5f * (prep[1] + 1.0f) * log1pf(z * z / prep[1]);
+}
+inline REAL robust_t_walker(const uint64_t rows, const REAL* h, const uint32_t hyper_len,
+                            const uint32_t dim, const REAL* x) {
+    const uint32_t F = dim - 1;
+    const REAL ls = x[F];
+    REAL pb = 0.0f;
+    for (uint32_t f = 0; f < F; ++f) pb = fmaf(x[f], x[f], pb);
+    return -(REAL)rows * ls - pb / (2.0f * h[1] * h[1]) - ls * ls / (2.0f * h[2] * h[2]);
+}
 }

@@ -104,7 +104,7 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
     """bay_model_desc of a DeviceDistributionModel; form 'plain' | 'tiled' | None (tiled
     when the model has a tiled form)."""
     if form is None:
-        form = "tiled" if model.tiled else "plain"
+        form = "gemm" if model.gemm else ("tiled" if model.tiled else "plain")
     keep = []
 
     def b(s):
@@ -130,6 +130,23 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
         d.row_len = t["row_len"]
         d.prep_len = t["prep_len"]
         d.walkers_per_cta = walkers_per_cta
+    elif form == "gemm":
+        gm = model.gemm
+        if not gm:
+            raise ValueError("model %s has no GEMM form" % model.name)
+        d.form = N.FORM_GEMM
+        d.tile_prep = b(gm["prep"])
+        d.tile_term = b(gm["term"])
+        d.tile_walker = b(gm["walker"])
+        d.prep_len = gm.get("prep_len", 1)
+        d.gemm_features = gm["features"]
+        d.gemm_coef = gm.get("coef", 0)
+        d.gemm_block = 1 if gm.get("block", "data") == "hyper" else 0
+        d.gemm_ld = gm["ld"]
+        d.gemm_offset = gm.get("offset", 0)
+        d.gemm_rows = gm.get("rows", 0)
+        d.gemm_aux_col = gm.get("aux_col", 0)
+        d.gemm_aux_len = gm.get("aux_len", 0)
     else:
         d.form = N.FORM_PLAIN
     return d, keep

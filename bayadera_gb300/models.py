@@ -68,10 +68,12 @@ class DeviceDistributionModel:
 
     tiled: optional dict with keys prep, term, walker, row_len, prep_len
     (the data-tiled form of the same density, see include/bayadera_gb300.h).
+    gemm: optional dict with keys prep, term, walker, prep_len, features, coef, block
+    ("data" | "hyper"), ld, offset, rows, aux_col, aux_len (the linear-predictor form).
     """
 
     def __init__(self, name, logpdf, mcmc_logpdf, dimension, params_size, limits, source,
-                 dialect="c99", tiled=None):
+                 dialect="c99", tiled=None, gemm=None):
         self.name = name
         self.logpdf = logpdf
         self.mcmc_logpdf = mcmc_logpdf
@@ -81,6 +83,7 @@ class DeviceDistributionModel:
         self.sources = list(source) if isinstance(source, (list, tuple)) else [source]
         self.dialect = dialect
         self.tiled = tiled
+        self.gemm = gemm
 
     def source(self):
         return self.sources
@@ -98,12 +101,12 @@ class DeviceDistributionModel:
 
 
 def device_distribution_model(source, name=None, logpdf=None, mcmc_logpdf=None, dimension=1,
-                              params_size=1, limits=None, dialect="c99", tiled=None):
+                              params_size=1, limits=None, dialect="c99", tiled=None, gemm=None):
     """device-distribution-model (models.clj:84-89) with the same defaults."""
     name = name or _gensym("distribution")
     logpdf = logpdf or "%s_logpdf" % name
     return DeviceDistributionModel(name, logpdf, mcmc_logpdf or logpdf, dimension, params_size,
-                                   limits, source, dialect, tiled)
+                                   limits, source, dialect, tiled, gemm)
 
 
 def device_likelihood_model(source, name=None, loglik=None, dialect="c99"):
@@ -199,21 +202,34 @@ def gaussian_posterior_model(tiled=True):
 
 
 def mvn_precision_model(dim):
-    """Zero-mean Gaussian with a dim x dim precision matrix as hyperparameters."""
+    """Zero-mean Gaussian with a dim x dim precision matrix as hyperparameters; GEMM form
+    A = P (rows of the hyperparameter block), term -x_r eta_r / 2."""
+    g = {"prep": "mvn_precision_prep", "term": "mvn_precision_term",
+         "walker": "mvn_precision_walker", "features": dim, "coef": 0, "block": "hyper",
+         "ld": dim, "offset": 0, "rows": dim}
     return device_distribution_model(get_source("mvn_precision"), name="mvn_precision",
                                      dimension=dim, params_size=dim * dim,
-                                     logpdf="mvn_precision_logpdf")
+                                     logpdf="mvn_precision_logpdf", gemm=g)
 
 
 def logistic_model(features):
+    """Logistic regression on data rows (x_1..x_F, y); GEMM form A = the rows' features."""
+    g = {"prep": "logistic_prep", "term": "logistic_term", "walker": "logistic_walker",
+         "features": features, "coef": 0, "block": "data", "ld": features + 1, "offset": 0,
+         "aux_col": features, "aux_len": 1}
     return device_distribution_model(get_source("logistic"), name="logistic",
-                                     dimension=features, params_size=1, logpdf="logistic_logpdf")
+                                     dimension=features, params_size=1, logpdf="logistic_logpdf",
+                                     gemm=g)
 
 
 def robust_t_model(features):
+    """Student-t regression on data rows (x_1..x_F, y), x = (beta, log sigma)."""
+    g = {"prep": "robust_t_prep", "term": "robust_t_term", "walker": "robust_t_walker",
+         "prep_len": 2, "features": features, "coef": 0, "block": "data", "ld": features + 1,
+         "offset": 0, "aux_col": features, "aux_len": 1}
     return device_distribution_model(get_source("robust_t"), name="robust_t",
                                      dimension=features + 1, params_size=3,
-                                     logpdf="robust_t_logpdf")
+                                     logpdf="robust_t_logpdf", gemm=g)
 
 
 def hierarchical_model(groups):

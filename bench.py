@@ -114,7 +114,7 @@ def measured_peaks():
 
 def profile_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "stretch_bare_mvn50.txt")
+    p = os.path.join(ROOT, "profiles", "stretch_gemm_mvn50.txt")
     if not os.path.exists(p):
         return None
     for ln in open(p):
@@ -175,7 +175,7 @@ def run_reference(args):
 def config():
     return {"workload": "mvn50-ar1 (50-D correlated Gaussian, rho 0.9, scales log-U[0.1,10])",
             "dim": DIM, "walkers": WALKERS, "burn_in": BURN, "run": RUN, "bins": BINS,
-            "model_form": "plain (one thread per walker, fused NVRTC kernel)",
+            "model_form": "gemm (64-walker tiles, x'Px register-blocked from shared memory)",
             "l2": "flushed between timed steps (256 MiB device write)",
             "parallelism": "replicas"}
 
@@ -213,7 +213,9 @@ def main():
     dP = torch.from_numpy(P.reshape(-1).copy()).cuda()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     f = GB300BayaderaFactory(device=local, wgs=1024, stream=stream.cuda_stream)
-    sf = f.mcmc_factory(M.mvn_precision_model(DIM))
+    model = M.mvn_precision_model(DIM)
+    sfs = {"gemm": f.mcmc_factory(model, form="gemm"),
+           "plain": f.mcmc_factory(model, form="plain")}
     seed_base = 1000 * (rank + 1)
 
     def job(samp, seed):
@@ -226,24 +228,20 @@ def main():
         hist = samp.histogram(1, BINS)
         return res, mean, var, hist
 
-    samp = sf.create_sampler(seed_base, WALKERS, dP)
-
     def barrier():
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
 
-    for w in range(args.warmup):
-        job(samp, seed_base + 10 * w)
-    torch.cuda.synchronize()
-
-    # timed region: K jobs, device-resident inputs, L2 flushed between jobs
-    times = []
-    results = None
-    launches0 = _native.launch_count()
-    with ClockSampler(local) as clocks:
+    def timed_jobs(samp, steps, warmup):
+        """Warm-up jobs, then `steps` jobs each timed with CUDA events on the library's
+        stream, the L2 flushed by a 256 MiB write before each (outside the events)."""
+        for w in range(warmup):
+            job(samp, seed_base + 10 * w)
+        torch.cuda.synchronize()
+        times, results = [], None
         barrier()
-        for k in range(args.steps):
+        for k in range(steps):
             with torch.cuda.stream(stream):
                 flush.fill_(k & 0xff)
             e0 = torch.cuda.Event(enable_timing=True)
@@ -254,14 +252,24 @@ def main():
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
         barrier()
+        t_total = sum(times)
+        if dist is not None:
+            t = torch.tensor([t_total], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t_total = float(t.item())
+        return WALKERS * (BURN + RUN) * steps * world / t_total, t_total, results
+
+    # headline: the GEMM form (walker tiles, shared-memory register-blocked x'Px)
+    samp = sfs["gemm"].create_sampler(seed_base, WALKERS, dP)
+    launches0 = _native.launch_count()
+    with ClockSampler(local) as clocks:
+        value, t_total, results = timed_jobs(samp, args.steps, args.warmup)
     launches = _native.launch_count() - launches0
-    t_total = sum(times)
-    if dist is not None:
-        t = torch.tensor([t_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
-    walker_steps = WALKERS * (BURN + RUN) * args.steps * world
-    value = walker_steps / t_total
+
+    # the plain FP32 form (one thread per walker, the reference's kernel structure)
+    samp_plain = sfs["plain"].create_sampler(seed_base, WALKERS, dP)
+    plain_value, _, _ = timed_jobs(samp_plain, max(1, min(args.steps, 2)), 1)
+    samp_plain.release()
 
     # dominant kernel: bare stretch launches of a burn-in, events on the launching stream
     n_probe = 256
@@ -287,7 +295,7 @@ def main():
     for k in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s2 = sf.create_sampler(seed_base + 31 * k, WALKERS, P.reshape(-1))
+        s2 = sfs["gemm"].create_sampler(seed_base + 31 * k, WALKERS, P.reshape(-1))
         res, mean, var, hist = job(s2, seed_base + 31 * k)
         s2.release()
         e2e_times.append(time.perf_counter() - t0)
@@ -295,7 +303,7 @@ def main():
                + hist.bin_ranks.nbytes)
     e2e_value = WALKERS * (BURN + RUN) * world / statistics.median(e2e_times)
 
-    # correctness of the job's result: posterior means within 3 MC s.e. of 0
+    # the job's result: posterior means within 3 MC s.e. of the analytic mean 0
     res, mean, var, hist = results
     ac = res["autocorrelation"]
     within = None
@@ -319,10 +327,12 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                         "peak_kind": peak_kind, "kernel": "bay_stretch_bare",
+                         "peak_kind": peak_kind, "kernel": "bay_stretch_bare (GEMM form)",
                          "launch_us": t_launch * 1e6,
                          "fp32_tflops": flop_launch / t_launch / 1e12},
             "cpu_baseline": cpu,
+            "forms": {"gemm": value, "plain_fp32": plain_value,
+                      "speedup_vs_plain": value / plain_value},
             "clocks": clocks.summary(),
             "result": {"acceptance_rate": res["acceptance_rate"],
                        "tau_max": float(np.max(ac.tau)) if ac is not None else None,
@@ -330,7 +340,8 @@ def main():
         }
         print(json.dumps(line))
     samp.release()
-    sf.release()
+    for x in sfs.values():
+        x.release()
     f.release()
     if dist is not None:
         dist.destroy_process_group()

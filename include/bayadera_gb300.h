@@ -88,8 +88,19 @@ int bay_launch_count(uint64_t* out);
  *                uint32_t dim, const REAL* x);       every term not summed over rows
  * log density = walker(x) + sum over rows of term(row, prep(x)); the sum is spread
  * over a CTA with compensated fp32 partial sums and an FP64 combine; data length is
- * 64-bit. */
-enum bay_form { BAY_FORM_PLAIN = 0, BAY_FORM_TILED = 1 };
+ * 64-bit.
+ *
+ * BAY_FORM_GEMM is the linear-predictor form: with A a rows x gemm_features matrix in
+ * the params (row r at block + gemm_offset + r * gemm_ld, the block being the data or
+ * the hyperparameters) and eta = A x[gemm_coef : gemm_coef + gemm_features],
+ *   REAL  term(REAL eta_r, const REAL* aux_r, uint64_t r, const REAL* x,
+ *              const REAL* prep);                    aux_r = gemm_aux_len values at
+ *                                                     column gemm_aux_col of row r
+ * log density = walker(x) + sum_r term(eta_r, aux_r, r, x, prep(x)).  Walkers are
+ * tiled 64 per CTA with the matrix resident in shared memory (rows * features <=
+ * 40960 floats).  Covers Gaussian targets (A = precision matrix, term = -eta_r x_r/2)
+ * and regression likelihoods (A = design matrix, aux = response). */
+enum bay_form { BAY_FORM_PLAIN = 0, BAY_FORM_TILED = 1, BAY_FORM_GEMM = 2 };
 enum bay_model_flags {
     /* accept if u <= z^(D-1) exp(beta dlogfn) in fp32, the reference's formula
      * (nvidia-gtx-mcmc-stretch.cu:84-88); default compares logs in FP64. */
@@ -110,6 +121,15 @@ typedef struct bay_model_desc {
     uint32_t walkers_per_cta; /* BAY_FORM_TILED: 0 = library choice */
     uint32_t cta_threads;     /* 0 = library choice (multiple of 32, <= 1024) */
     uint32_t flags;           /* bay_model_flags */
+    /* BAY_FORM_GEMM (tile_prep / tile_term / tile_walker name the three functions) */
+    uint32_t gemm_features;   /* columns of A */
+    uint32_t gemm_coef;       /* first walker coordinate multiplied by A */
+    uint32_t gemm_block;      /* 0: A in the data, 1: A in the hyperparameters */
+    uint32_t gemm_ld;         /* floats between rows of A */
+    uint64_t gemm_offset;     /* floats from the block start to row 0 */
+    uint64_t gemm_rows;       /* rows of A; 0 = (block length - offset) / ld */
+    uint32_t gemm_aux_col;    /* column of the row's auxiliary values */
+    uint32_t gemm_aux_len;    /* auxiliary values per row (0..8) */
 } bay_model_desc;
 
 int bay_model_compile(bay_ctx* ctx, const bay_model_desc* desc, bay_model** out);

@@ -161,6 +161,108 @@ def test_step_consistency_gaussian_posterior(factory, M, oracle):
                       lambda s: s.init_position(4, [2.0, 4.0, 1.0, 3.0]), max_mismatch=8)
 
 
+# ------------------------------------------------------------------ GEMM form
+def _regression_data(rng, n, F, kind):
+    X = rng.normal(size=(n, F)).astype(np.float32)
+    beta = rng.normal(scale=1.0 / np.sqrt(F), size=F)
+    eta = X.astype(np.float64) @ beta
+    if kind == "logistic":
+        y = (rng.random(n) < 1.0 / (1.0 + np.exp(-eta))).astype(np.float32)
+        hyper = np.array([5.0], np.float32)
+    else:
+        y = (eta + 0.5 * rng.standard_t(4, n)).astype(np.float32)
+        hyper = np.array([4.0, 10.0, 1.0], np.float32)
+    rows = np.concatenate([X, y[:, None]], axis=1).astype(np.float32)
+    return np.concatenate([rows.reshape(-1), hyper]), rows.size
+
+
+@pytest.mark.parametrize("case", ["mvn50", "logistic", "robust_t"])
+def test_gemm_logfn_matches_fp64(factory, M, oracle, case):
+    """GEMM-form log densities of 1000 walkers vs the oracle's FP64 density: relative
+    error below 2e-5 (fp32 dot products over F features, Kahan row sums)."""
+    rng = np.random.default_rng(3)
+    if case == "mvn50":
+        D = 50
+        A = rng.normal(size=(D, D))
+        P = (A @ A.T / D + np.eye(D)).astype(np.float32)
+        model, oname, params, dl = M.mvn_precision_model(D), "mvn_precision", P.reshape(-1), 0
+        init = lambda s: s.init_position_normal(4, 0.0, 1.0)
+    elif case == "logistic":
+        D = 16
+        params, dl = _regression_data(rng, 512, D, "logistic")
+        model, oname = M.logistic_model(D), "logistic"
+        init = lambda s: s.init_position_normal(4, 0.0, 0.3)
+    else:
+        D = 17
+        params, dl = _regression_data(rng, 512, D - 1, "robust_t")
+        model, oname = M.robust_t_model(D - 1), "robust_t"
+        init = lambda s: s.init_position_normal(4, 0.0, 0.3)
+    sf = factory.mcmc_factory(model, form="gemm")
+    s = sf.create_sampler(3, 1000, params)
+    init(s)
+    pos = s.positions().T.astype(np.float64)
+    lf = s.logfn().astype(np.float64)
+    want = np.array([oracle.logfn64(oname, params, dl, D, p) for p in pos])
+    err = np.abs(lf - want) / np.maximum(np.abs(want), 1.0)
+    assert err.max() < 2e-5, err.max()
+    s.burn_in(3, 2.0)                      # moves run, densities stay consistent
+    pos = s.positions().T.astype(np.float64)
+    lf = s.logfn().astype(np.float64)
+    want = np.array([oracle.logfn64(oname, params, dl, D, p) for p in pos])
+    assert (np.abs(lf - want) / np.maximum(np.abs(want), 1.0)).max() < 2e-5
+    s.release()
+    sf.release()
+
+
+def test_gemm_step_consistency_mvn50(factory, M, oracle):
+    """GEMM-form moves agree with the oracle's reference-order moves except where the
+    accept decision is marginal (the two sum the quadratic form in different orders)."""
+    D, W = 50, 2048
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(D, D))
+    P = (A @ A.T / D + np.eye(D)).astype(np.float32)
+    sf = factory.mcmc_factory(M.mvn_precision_model(D), form="gemm")
+    s = sf.create_sampler(11, W, P.reshape(-1))
+    s.init_position_normal(3, 0.0, 1.0)
+    for t in range(4):
+        pos, lf, rng_state = s.export_state()
+        r = oracle.Stretch("mvn_precision", D, W, P.reshape(-1), seed=int(rng_state[0]),
+                           flags=oracle.ACCEPT_LOG64)
+        r.xs[:] = pos.reshape(-1)
+        r.logfn[:] = lf
+        r.bare_counter = int(rng_state[2])
+        r.move_bare(a=2.0, beta=1.0)
+        s.burn_in(1, 2.0)
+        got = s.positions().T.reshape(W, D)
+        rows = np.any(got != r.xs.reshape(W, D), axis=1)
+        assert rows.sum() <= 8, "step %d: %d walkers differ" % (t, rows.sum())
+    s.release()
+    sf.release()
+
+
+def test_gemm_run_sampler_matches_plain_statistics(factory, M):
+    """Same target, GEMM and plain forms: acceptance rates within 3 binomial s.e. and
+    ensemble means within 4 MC s.e. of each other."""
+    D, W = 10, 4096
+    P = np.diag(np.linspace(0.5, 2.0, D)).astype(np.float32)
+    out = {}
+    for form in ("plain", "gemm"):
+        sf = factory.mcmc_factory(M.mvn_precision_model(D), form=form)
+        s = sf.create_sampler(17, W, P.reshape(-1))
+        s.init_position_normal(18)
+        s.burn_in(300, 2.0)
+        r = s.run_sampler(1000, 2.0, return_means=True)
+        out[form] = (r["acceptance_rate"], r["autocorrelation"])
+        # the last per-step ensemble mean is the mean of the current walkers
+        np.testing.assert_allclose(r["means"][:, -1], s.mean(), rtol=1e-5, atol=1e-6)
+        s.release()
+        sf.release()
+    (ra, aa), (rb, ab) = out["plain"], out["gemm"]
+    se = np.sqrt(ra * (1 - ra) / (W * 1000))
+    assert abs(ra - rb) < 3 * se * np.sqrt(50)          # moves are autocorrelated
+    assert np.all(np.abs(aa.mean - ab.mean) <= 4 * np.hypot(aa.sigma, ab.sigma))
+
+
 # ------------------------------------------------------------------ log densities
 def test_tiled_logfn_matches_fp64(factory, M, oracle):
     rng = np.random.default_rng(1)
@@ -389,23 +491,31 @@ def test_memory_limit(M, N):
 
 # ------------------------------------------------------------------ posterior moments
 def test_mvn_posterior_within_3_mcse(factory, M):
-    """Correlated 10-D Gaussian: ensemble-pooled means within 3.5 MC s.e. (acor sigma;
-    3.5 rather than 3 so that ten dims pass together with 99.5% probability) of the
-    analytic mean 0, and variances within 10% of Sigma's diagonal."""
+    """Correlated 10-D Gaussian (AR(1), rho 0.5): ensemble-pooled means within 3.5 MC
+    s.e. of the analytic mean 0 (3.5 rather than 3 so that ten dims pass together with
+    99.5% probability), the s.e. from 40 batch means of the per-step mean series; acor's
+    sigma within a factor of 2 of it in at least 8 of 10 dims (acor's blocking estimate
+    is itself noisy at n / tau ~ 100); variances within 10% of Sigma's diagonal."""
     D = 10
     rng = np.random.default_rng(2)
     s_ = np.exp(rng.uniform(np.log(0.5), np.log(2.0), D))
     idx = np.arange(D)
-    Sigma = np.outer(s_, s_) * 0.9 ** np.abs(idx[:, None] - idx[None, :])
+    Sigma = np.outer(s_, s_) * 0.5 ** np.abs(idx[:, None] - idx[None, :])
     P = np.linalg.inv(Sigma).astype(np.float32)
     sf = factory.mcmc_factory(M.mvn_precision_model(D))
     s = sf.create_sampler(21, 8192, P.reshape(-1))
     s.init_position_normal(22)
     s.burn_in(2000, 2.0)
-    res = s.run_sampler(4000, 2.0, return_means=True)
+    n = 20000
+    res = s.run_sampler(n, 2.0, return_means=True)
     ac = res["autocorrelation"]
-    pooled = res["means"].astype(np.float64).mean(axis=1)
-    assert np.all(np.abs(pooled) <= 3.5 * ac.sigma + 1e-12), (pooled, ac.sigma)
+    series = res["means"].astype(np.float64)
+    pooled = series.mean(axis=1)
+    batches = series.reshape(D, 40, n // 40).mean(axis=2)
+    se = batches.std(axis=1, ddof=1) / np.sqrt(40)
+    assert np.all(np.abs(pooled) <= 3.5 * se), (pooled, se)
+    ratio = ac.sigma / se
+    assert np.sum((ratio > 0.5) & (ratio < 2.0)) >= 8, ratio
     var = s.variance()
     assert np.all(np.abs(var / np.diag(Sigma) - 1) < 0.1)
     s.release()
