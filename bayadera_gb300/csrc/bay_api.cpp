@@ -169,7 +169,12 @@ struct bay_model {
     uint32_t dim = 0, params_size = 0, form = 0, cta = 256, wpc = 1, flags = 0;
     // GEMM form layout of A (see bay_model_desc)
     uint32_t gemm_features = 0, gemm_block = 0, gemm_ld = 0, gemm_aux_col = 0, gemm_aux_len = 0;
+    uint32_t prep_len = 1;
     uint64_t gemm_offset = 0, gemm_rows = 0;
+    // GEMM form, streaming kernels: propose / accept [bare, accu, logfn], rows [move, logfn]
+    CUkernel k_gp[3] = {nullptr, nullptr, nullptr};
+    CUkernel k_gr[2] = {nullptr, nullptr};
+    CUkernel k_ga[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -306,9 +311,40 @@ struct bay_sampler {
                                      "(device status " + std::to_string(st) + ")");
     }
 
-    uint64_t per_cta() const { return model->form == BAY_FORM_PLAIN ? model->cta : model->wpc; }
+    // GEMM form, streaming mode (matrix read from device memory in row blocks)
+    bool streaming = false;
+    float *s_y = nullptr, *s_b = nullptr, *s_prep = nullptr, *s_w = nullptr, *s_zu = nullptr,
+          *s_part = nullptr;
+    uint32_t s_nsb = 0, s_sbrows = 0;
+    size_t smem_rows = 0;
 
+    uint64_t per_cta() const {
+        if (streaming) return 256;  // the accept kernel: one thread per walker
+        return model->form == BAY_FORM_PLAIN ? model->cta : model->wpc;
+    }
+
+    // CTAs of the launch that writes the accu statistics (and so of the partials)
     unsigned grid() const { return (unsigned)((K + per_cta() - 1) / per_cta()); }
+
+    void launch(CUkernel k, unsigned gx, unsigned gy, size_t sm, bay_stretch_params& p,
+                cudaStream_t st, const char* what) {
+        void* args[] = {&p};
+        cu_check(g_cu.LaunchKernel((CUfunction)k, gx, gy, 1, 256, 1, 1, (unsigned)sm,
+                                   (CUstream)st, args, nullptr),
+                 what);
+    }
+
+    // the three launches of a streaming half-step (mode 0 bare, 1 accu, 2 logfn)
+    void launch_streaming(int mode, uint32_t half, uint32_t step_off, cudaStream_t st) {
+        bay_stretch_params p = make_params(half, step_off);
+        const uint64_t nk = mode == 2 ? W : K;
+        const unsigned g1 = (unsigned)((nk + 255) / 256), gt = (unsigned)((nk + 127) / 128);
+        launch(model->k_gp[mode], g1, 1, 0, p, st, "cuLaunchKernel(gemm propose)");
+        launch(model->k_gr[mode == 2 ? 1 : 0], gt, s_nsb, smem_rows, p, st,
+               "cuLaunchKernel(gemm rows)");
+        launch(model->k_ga[mode], g1, 1, 0, p, st, "cuLaunchKernel(gemm accept)");
+        if (st == ctx->stream) bay::count_launches(3);
+    }
 
     bay_stretch_params make_params(uint32_t half, uint32_t step_off) const {
         bay_stretch_params p;
@@ -331,10 +367,22 @@ struct bay_sampler {
         p.gemm_ld = model->gemm_ld;
         p.gemm_np = gemm_np;
         p.gemm_lay = gemm_lay;
+        p.s_y = s_y;
+        p.s_b = s_b;
+        p.s_prep = s_prep;
+        p.s_w = s_w;
+        p.s_zu = s_zu;
+        p.s_part = s_part;
+        p.s_nsb = s_nsb;
+        p.s_sbrows = s_sbrows;
         return p;
     }
 
     void launch_half(bool accu, uint32_t half, uint32_t step_off, cudaStream_t st) {
+        if (streaming) {
+            launch_streaming(accu ? 1 : 0, half, step_off, st);
+            return;
+        }
         if (st == ctx->stream) bay::count_launches(1);
         bay_stretch_params p = make_params(half, step_off);
         void* args[] = {&p};
@@ -348,6 +396,10 @@ struct bay_sampler {
     }
 
     void launch_logfn_all() {
+        if (streaming) {
+            launch_streaming(2, 0, 0, ctx->stream);
+            return;
+        }
         bay::count_launches(1);
         bay_stretch_params p = make_params(0, 0);
         void* args[] = {&p};
@@ -411,7 +463,8 @@ struct bay_sampler {
             }
             for (; done + kChunk <= n; done += kChunk) {
                 cuda_check(cudaGraphLaunch(ex, ctx->stream), "cudaGraphLaunch");
-                bay::count_launches(2 * kChunk + 1 + ((accu && means_cap) ? 1 : 0));
+                bay::count_launches((streaming ? 6 : 2) * kChunk + 1 +
+                                    ((accu && means_cap) ? 1 : 0));
             }
         }
         while (done < n) {
@@ -661,6 +714,7 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
         m->wpc = g.wpc;
         m->flags = d->flags;
         if (d->form == BAY_FORM_GEMM) {
+            m->prep_len = d->prep_len ? d->prep_len : 1u;
             m->gemm_features = d->gemm_features;
             m->gemm_block = d->gemm_block;
             m->gemm_ld = d->gemm_ld;
@@ -677,8 +731,18 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
             cu_check(g_cu.LibraryGetKernel(&m->k_accu, m->lib, "bay_stretch_accu"), "GetKernel(accu)");
             cu_check(g_cu.LibraryGetKernel(&m->k_logfn, m->lib, "bay_logfn_all"), "GetKernel(logfn)");
             if (d->form == BAY_FORM_GEMM) {
+                const char* gp[3] = {"bay_gemm_propose_bare", "bay_gemm_propose_accu",
+                                     "bay_gemm_propose_logfn"};
+                const char* ga[3] = {"bay_gemm_accept_bare", "bay_gemm_accept_accu",
+                                     "bay_gemm_accept_logfn"};
+                for (int i = 0; i < 3; ++i) {
+                    cu_check(g_cu.LibraryGetKernel(&m->k_gp[i], m->lib, gp[i]), "GetKernel(propose)");
+                    cu_check(g_cu.LibraryGetKernel(&m->k_ga[i], m->lib, ga[i]), "GetKernel(accept)");
+                }
+                cu_check(g_cu.LibraryGetKernel(&m->k_gr[0], m->lib, "bay_gemm_rows_move"), "GetKernel(rows)");
+                cu_check(g_cu.LibraryGetKernel(&m->k_gr[1], m->lib, "bay_gemm_rows_logfn"), "GetKernel(rows)");
                 CUdevice dev = (CUdevice)c->device;
-                for (CUkernel k : {m->k_bare, m->k_accu, m->k_logfn})
+                for (CUkernel k : {m->k_bare, m->k_accu, m->k_logfn, m->k_gr[0], m->k_gr[1]})
                     cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                      (int)kGemmMaxSmem, k, dev),
                              "cuKernelSetAttribute(smem)");
@@ -742,12 +806,24 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                 fail(BAY_ERR_ARG, "the GEMM matrix does not fit its params block");
             }
             s->smem = gemm_smem_bytes(m, s->gemm_rows);
-            if (s->smem > kGemmMaxSmem) {
-                delete s;
-                fail(BAY_ERR_ARG, "GEMM matrix of " + std::to_string(s->gemm_rows) + " x " +
-                                      std::to_string(m->gemm_features) +
-                                      " does not fit in shared memory (the resident GEMM form holds "
-                                      "up to about 40960 values)");
+            s->streaming = (m->flags & BAY_MODEL_GEMM_STREAMING) || s->smem > kGemmMaxSmem;
+            if (s->streaming) {
+                // rows kernel: the coefficient tile (F x 128) + one 32-feature matrix chunk
+                s->smem = 0;
+                s->smem_rows = sizeof(float) * ((size_t)m->gemm_features * 128 + 32 * 129);
+                if (s->smem_rows > kGemmMaxSmem || s->gemm_rows > 0xffffffffull) {
+                    delete s;
+                    fail(BAY_ERR_ARG, "GEMM form: at most 384 features and 2^32 - 1 rows");
+                }
+                // row super-blocks: about 8 CTAs per SM over (walker tiles x super-blocks)
+                const uint64_t n_sub = (s->gemm_rows + 127) / 128;
+                const uint64_t n_wt = (s->K + 127) / 128;
+                const uint64_t target = 8ull * (uint64_t)c->sm_count;
+                uint64_t nsb = (target + n_wt - 1) / n_wt;
+                nsb = std::max<uint64_t>(1, std::min<uint64_t>(nsb, n_sub));
+                const uint64_t per = (n_sub + nsb - 1) / nsb;
+                s->s_sbrows = (uint32_t)(per * 128);
+                s->s_nsb = (uint32_t)((s->gemm_rows + s->s_sbrows - 1) / s->s_sbrows);
             }
         }
         try {
@@ -772,7 +848,15 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                 s->params = p;
                 s->own_params = true;
             }
-            if (m->form == BAY_FORM_GEMM) {
+            if (s->streaming) {
+                const size_t Wn = walkers;
+                s->s_y = (float*)c->alloc(sizeof(float) * Wn * s->D);
+                s->s_b = (float*)c->alloc(sizeof(float) * Wn * m->gemm_features);
+                s->s_prep = (float*)c->alloc(sizeof(float) * Wn * m->prep_len);
+                s->s_w = (float*)c->alloc(sizeof(float) * Wn);
+                s->s_zu = (float*)c->alloc(sizeof(float) * Wn * 2);
+                s->s_part = (float*)c->alloc(sizeof(float) * Wn * 2 * s->s_nsb);
+            } else if (m->form == BAY_FORM_GEMM) {
                 s->gemm_np = (uint32_t)((s->gemm_rows + 63) & ~63ull);
                 const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
                 s->gemm_lay = (float*)c->alloc(
@@ -804,6 +888,7 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
             c->release(s->stats);
             c->release(s->means);
             c->release(s->gemm_lay);
+            for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
             if (s->own_params) c->release((void*)s->params);
             delete s;
             throw;
@@ -840,6 +925,7 @@ int bay_sampler_release(bay_sampler* s) {
         c->release(s->hist);
         c->release(s->counts);
         c->release(s->gemm_lay);
+        for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
         if (s->own_params) c->release((void*)s->params);
         delete s;
     });

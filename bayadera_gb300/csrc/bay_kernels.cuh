@@ -38,6 +38,14 @@ struct bay_stretch_params {
     unsigned int gemm_ld;
     unsigned int gemm_np;
     const float* gemm_lay;
+    float* s_y;
+    float* s_b;
+    float* s_prep;
+    float* s_w;
+    float* s_zu;
+    float* s_part;
+    unsigned int s_nsb;
+    unsigned int s_sbrows;
 };
 
 enum {

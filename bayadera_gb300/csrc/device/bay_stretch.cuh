@@ -75,6 +75,16 @@ struct bay_stretch_params {
     unsigned int gemm_ld;
     unsigned int gemm_np;
     const float* gemm_lay;
+    // GEMM form, streaming (too many rows for shared memory): one half-step's per-walker
+    // scratch and the per-row-block partial sums
+    float* s_y;                     // [nk][DIM] proposals (current positions for logfn)
+    float* s_b;                     // [nk][F] coefficient block
+    float* s_prep;                  // [nk][BAY_PREP_LEN]
+    float* s_w;                     // [nk] terms outside the row sum
+    float* s_zu;                    // [nk][2] stretch factor and accept uniform
+    float* s_part;                  // [nsb][nk] compensated (hi, lo) partial row sums
+    unsigned int s_nsb;             // row super-blocks
+    unsigned int s_sbrows;          // rows per super-block (a multiple of 128)
 };
 
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
@@ -446,6 +456,242 @@ extern "C" __global__ void __launch_bounds__(256) bay_stretch_accu(bay_stretch_p
 }
 extern "C" __global__ void __launch_bounds__(256) bay_logfn_all(bay_stretch_params P) {
     bay_stretch_gemm<false, true>(P);
+}
+
+// ---------------------------------------------------------------- GEMM form, streaming
+// For matrices too large for shared memory.  A half-step is three launches:
+//   propose: one thread per walker -- Philox, stretch, partner, proposal row, prep and the
+//            terms outside the row sum into per-walker scratch;
+//   rows:    CTA (128-walker tile, row super-block): the tile's coefficient block stays in
+//            shared memory (feature-major); for each 128-row sub-block the matrix is
+//            streamed in 32-feature chunks; each thread owns 8 walkers x 8 rows (rows
+//            rg + 16 j) of eta, applies the row term with Kahan sums, and the 16 row-group
+//            lanes of a walker combine as compensated fp32 pairs -> s_part[sb][walker];
+//            blockIdx.x runs over walker tiles so that the tiles sharing a row block run
+//            together and the block is read from HBM once;
+//   accept:  one thread per walker -- partials summed in super-block order, accept,
+//            write-back, statistics.
+#define BAY_SW 128
+#define BAY_SR 128
+#define BAY_SF 32
+#define BAY_XS (BAY_SR + 1)   // odd row stride of the staged matrix chunk (no bank conflicts)
+
+template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions
+__device__ __forceinline__ void bay_gemm_propose_impl(const bay_stretch_params& P) {
+    const unsigned int kind = MODE == 1 ? 1u : 0u;
+    const unsigned int nk = MODE == 2 ? P.W : P.K;
+    const unsigned int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    float* y = P.s_y + (size_t)k * DIM;
+    if (MODE == 2) {
+        const float* x = P.xs + (size_t)k * DIM;
+        for (int d = 0; d < DIM; ++d) y[d] = x[d];
+    } else {
+        const float* X = P.xs + (size_t)P.half * P.K * DIM + (size_t)k * DIM;
+        const unsigned int stream = MODE == 1 ? (P.half ? 2222u : 1111u) : (P.half ? 4444u : 3333u);
+        bay_u4 c;
+        c.x = k;
+        c.y = P.ctl->step[kind] + P.step_off;
+        c.z = stream;
+        c.w = 0xbeeff00du;
+        const bay_u4 r = bay_philox4x32_10(c, P.ctl->seed[kind] + P.half, 0xdecafbadu);
+        const float z = bay_stretch_z(P.ctl->a, bay_u01(r.y));
+        const unsigned int j = bay_partner(bay_u01(r.x), P.K);
+        const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM + (size_t)j * DIM;
+        for (int d = 0; d < DIM; ++d) {
+            const float s = S[d];
+            y[d] = __fmaf_rn(z, __fsub_rn(X[d], s), s);
+        }
+        P.s_zu[2 * (size_t)k] = z;
+        P.s_zu[2 * (size_t)k + 1] = bay_u01(r.z);
+    }
+    for (int f = 0; f < BAY_GEMM_F; ++f) P.s_b[(size_t)k * BAY_GEMM_F + f] = y[BAY_GEMM_COEF + f];
+    const float* hyper = P.params + P.data_len;
+    float pr[BAY_PREP_LEN];
+#pragma unroll
+    for (int i = 0; i < BAY_PREP_LEN; ++i) pr[i] = 0.0f;
+    BAY_GEMM_PREP(hyper, P.params_len, DIM, y, pr);
+#pragma unroll
+    for (int i = 0; i < BAY_PREP_LEN; ++i) P.s_prep[(size_t)k * BAY_PREP_LEN + i] = pr[i];
+    P.s_w[k] = BAY_GEMM_WALKER(P.gemm_rows, hyper, P.params_len, DIM, y);
+}
+
+template <int MODE>
+__device__ __forceinline__ void bay_gemm_rows_impl(const bay_stretch_params& P) {
+    extern __shared__ __align__(128) float bay_smem[];
+    float* Bs = bay_smem;                              // [F][BAY_SW]
+    float* Xs = Bs + (size_t)BAY_GEMM_F * BAY_SW;      // [BAY_SF][BAY_XS]
+    __shared__ float sPrep[BAY_SW][BAY_PREP_LEN];
+    const unsigned int nk = MODE == 2 ? P.W : P.K;
+    const unsigned int tid = threadIdx.x;
+    const unsigned int k0 = blockIdx.x * BAY_SW;
+    const unsigned int sb = blockIdx.y;
+    const unsigned int rows = (unsigned int)P.gemm_rows;
+    const float* A = P.params + P.gemm_base;
+    // the tile's coefficient block, feature-major (walkers past nk are zero)
+    for (unsigned int e = tid; e < BAY_GEMM_F * BAY_SW; e += blockDim.x) {
+        const unsigned int f = e / BAY_SW, w = e - f * BAY_SW;
+        Bs[e] = (k0 + w < nk) ? P.s_b[(size_t)(k0 + w) * BAY_GEMM_F + f] : 0.0f;
+    }
+    for (unsigned int e = tid; e < BAY_SW * BAY_PREP_LEN; e += blockDim.x) {
+        const unsigned int w = e / BAY_PREP_LEN, i = e - w * BAY_PREP_LEN;
+        sPrep[w][i] = (k0 + w < nk) ? P.s_prep[(size_t)(k0 + w) * BAY_PREP_LEN + i] : 0.0f;
+    }
+    const unsigned int wg = tid >> 4, rg = tid & 15u;
+    const unsigned int w0 = wg * 8;
+    float sum[8], cmp[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        sum[i] = 0.0f;
+        cmp[i] = 0.0f;
+    }
+    const unsigned int rb = sb * P.s_sbrows;
+    const unsigned int re = rb + P.s_sbrows < rows ? rb + P.s_sbrows : rows;
+    for (unsigned int r0 = rb; r0 < re; r0 += BAY_SR) {
+        float acc[8][8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+        for (unsigned int f0 = 0; f0 < BAY_GEMM_F; f0 += BAY_SF) {
+            __syncthreads();
+            // chunk of rows r0..r0+127, features f0..f0+31: reads run along each row
+            for (unsigned int e = tid; e < BAY_SR * BAY_SF; e += blockDim.x) {
+                const unsigned int r = e / BAY_SF, fl = e - r * BAY_SF;
+                const unsigned int f = f0 + fl;
+                Xs[fl * BAY_XS + r] = (r0 + r < re && f < BAY_GEMM_F)
+                    ? __ldg(A + (size_t)(r0 + r) * P.gemm_ld + f) : 0.0f;
+            }
+            __syncthreads();
+            const unsigned int fe = BAY_GEMM_F - f0 < BAY_SF ? BAY_GEMM_F - f0 : BAY_SF;
+#pragma unroll 4
+            for (unsigned int fl = 0; fl < fe; ++fl) {
+                const float4 b0 = *reinterpret_cast<const float4*>(&Bs[(f0 + fl) * BAY_SW + w0]);
+                const float4 b1 = *reinterpret_cast<const float4*>(&Bs[(f0 + fl) * BAY_SW + w0 + 4]);
+                const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+                float xv[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) xv[j] = Xs[fl * BAY_XS + rg + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[i][j] = __fmaf_rn(bv[i], xv[j], acc[i][j]);
+            }
+        }
+        // row terms of this sub-block
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const unsigned int r = r0 + rg + 16 * j;
+            if (r < re) {
+                float aux[BAY_AUXS];
+#pragma unroll
+                for (int c = 0; c < BAY_AUXS; ++c)
+                    aux[c] = BAY_GEMM_AUX > 0 ? __ldg(A + (size_t)r * P.gemm_ld + BAY_GEMM_AUXCOL + c) : 0.0f;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const unsigned int kw = k0 + w0 + i < nk ? k0 + w0 + i : nk - 1;
+                    const float t = BAY_GEMM_TERM(acc[i][j], aux, (uint64_t)r,
+                                                  P.s_y + (size_t)kw * DIM, sPrep[w0 + i]);
+                    const float yk = __fsub_rn(t, cmp[i]);
+                    const float s2 = __fadd_rn(sum[i], yk);
+                    cmp[i] = __fsub_rn(__fsub_rn(s2, sum[i]), yk);
+                    sum[i] = s2;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        bay_cf v;
+        v.hi = sum[i];
+        v.lo = -cmp[i];
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) v = bay_cadd(v, bay_cf_shfl_xor(v, o));
+        const unsigned int kw = k0 + w0 + i;
+        if (rg == 0 && kw < nk) {
+            P.s_part[2 * ((size_t)sb * nk + kw)] = v.hi;
+            P.s_part[2 * ((size_t)sb * nk + kw) + 1] = v.lo;
+        }
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ void bay_gemm_accept_impl(const bay_stretch_params& P) {
+    const unsigned int nk = MODE == 2 ? P.W : P.K;
+    const unsigned int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = k < nk;
+    bool accepted = false;
+    if (valid) {
+        bay_cf s;
+        s.hi = 0.0f;
+        s.lo = 0.0f;
+        for (unsigned int sb = 0; sb < P.s_nsb; ++sb) {
+            bay_cf p;
+            p.hi = P.s_part[2 * ((size_t)sb * nk + k)];
+            p.lo = P.s_part[2 * ((size_t)sb * nk + k) + 1];
+            s = bay_cadd(s, p);
+        }
+        const float ly = bay_cf_total(P.s_w[k], s);
+        if (MODE == 2) {
+            P.logfn[k] = ly;
+        } else {
+            const float lx = P.logfn[(size_t)P.half * P.K + k];
+            accepted = bay_accept(P.s_zu[2 * (size_t)k + 1], P.s_zu[2 * (size_t)k], ly, lx,
+                                  MODE == 1 ? 1.0f : P.ctl->beta);
+            if (accepted) {
+                float* X = P.xs + (size_t)P.half * P.K * DIM + (size_t)k * DIM;
+                const float* y = P.s_y + (size_t)k * DIM;
+                for (int d = 0; d < DIM; ++d) X[d] = y[d];
+                P.logfn[(size_t)P.half * P.K + k] = ly;
+            }
+        }
+    }
+    if (MODE != 1) return;
+    // accu: acceptance count and the per-dim sums of this CTA's walkers (new positions)
+    const int n_acc = __syncthreads_count(accepted);
+    if (threadIdx.x == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
+    if (P.means_cap == 0) return;
+    const unsigned int k0 = blockIdx.x * blockDim.x;
+    const unsigned int nv = nk - k0 < blockDim.x ? nk - k0 : blockDim.x;
+    const float* Xc = P.xs + (size_t)P.half * P.K * DIM + (size_t)k0 * DIM;
+    float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x + blockIdx.x;
+    for (unsigned int d = threadIdx.x; d < DIM; d += blockDim.x) {
+        bay_cf s;
+        s.hi = 0.0f;
+        s.lo = 0.0f;
+        for (unsigned int w = 0; w < nv; ++w) {
+            bay_cf y;
+            y.hi = Xc[(size_t)w * DIM + d];
+            y.lo = 0.0f;
+            s = bay_cadd(s, y);
+        }
+        out[(size_t)d * gridDim.x] = __fadd_rn(s.hi, s.lo);
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_propose_bare(bay_stretch_params P) {
+    bay_gemm_propose_impl<0>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_propose_accu(bay_stretch_params P) {
+    bay_gemm_propose_impl<1>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_propose_logfn(bay_stretch_params P) {
+    bay_gemm_propose_impl<2>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_rows_move(bay_stretch_params P) {
+    bay_gemm_rows_impl<0>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_rows_logfn(bay_stretch_params P) {
+    bay_gemm_rows_impl<2>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_accept_bare(bay_stretch_params P) {
+    bay_gemm_accept_impl<0>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_accept_accu(bay_stretch_params P) {
+    bay_gemm_accept_impl<1>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_gemm_accept_logfn(bay_stretch_params P) {
+    bay_gemm_accept_impl<2>(P);
 }
 
 #elif !BAY_TILED

@@ -92,15 +92,17 @@ class GB300BayaderaFactory:
         return v.value
 
     def mcmc_factory(self, model, form=None, accept_ref=False, walkers_per_cta=0,
-                     cta_threads=0):
+                     cta_threads=0, streaming=False):
         """EngineFactory/mcmc-factory: compile the model's fused stretch kernels."""
-        return GB300StretchFactory(self, model, form, accept_ref, walkers_per_cta, cta_threads)
+        return GB300StretchFactory(self, model, form, accept_ref, walkers_per_cta, cta_threads,
+                                   streaming)
 
     def acor(self, data_matrix):
         return self.acor_engine.acor(data_matrix)
 
 
-def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0):
+def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0,
+               streaming=False):
     """bay_model_desc of a DeviceDistributionModel; form 'plain' | 'tiled' | None (tiled
     when the model has a tiled form)."""
     if form is None:
@@ -117,7 +119,7 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
     d.logfn = b(model.mcmc_logpdf)
     d.dim = model.dimension
     d.params_size = model.params_size
-    d.flags = N.MODEL_ACCEPT_REF if accept_ref else 0
+    d.flags = (N.MODEL_ACCEPT_REF if accept_ref else 0) | (N.MODEL_GEMM_STREAMING if streaming else 0)
     d.cta_threads = cta_threads
     if form == "tiled":
         t = model.tiled
@@ -160,10 +162,10 @@ def check_model(model, form=None, wgs=1024, accept_ref=False):
 
 class GB300StretchFactory:
     def __init__(self, factory, model, form=None, accept_ref=False, walkers_per_cta=0,
-                 cta_threads=0):
+                 cta_threads=0, streaming=False):
         self.factory = factory
         self.model = model
-        d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads)
+        d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, streaming)
         h = C.c_void_p()
         N.call("bay_model_compile", factory.ctx, C.byref(d), C.byref(h))
         self.handle = h

@@ -96,15 +96,21 @@ int bay_launch_count(uint64_t* out);
  *   REAL  term(REAL eta_r, const REAL* aux_r, uint64_t r, const REAL* x,
  *              const REAL* prep);                    aux_r = gemm_aux_len values at
  *                                                     column gemm_aux_col of row r
- * log density = walker(x) + sum_r term(eta_r, aux_r, r, x, prep(x)).  Walkers are
- * tiled 64 per CTA with the matrix resident in shared memory (rows * features <=
- * 40960 floats).  Covers Gaussian targets (A = precision matrix, term = -eta_r x_r/2)
- * and regression likelihoods (A = design matrix, aux = response). */
+ * log density = walker(x) + sum_r term(eta_r, aux_r, r, x, prep(x)).  With the matrix
+ * resident in shared memory (rows * features up to about 40960 floats) walkers are
+ * tiled 64 per CTA in one launch per half-step; larger matrices are streamed (128-walker
+ * x 128-row register tiles, per-row-block partial sums, 64-bit row counts; features
+ * <= 384).  Covers Gaussian targets (A = precision matrix, term = -eta_r x_r/2) and
+ * regression likelihoods (A = design matrix, aux = response). */
 enum bay_form { BAY_FORM_PLAIN = 0, BAY_FORM_TILED = 1, BAY_FORM_GEMM = 2 };
 enum bay_model_flags {
     /* accept if u <= z^(D-1) exp(beta dlogfn) in fp32, the reference's formula
      * (nvidia-gtx-mcmc-stretch.cu:84-88); default compares logs in FP64. */
-    BAY_MODEL_ACCEPT_REF = 1u << 0
+    BAY_MODEL_ACCEPT_REF = 1u << 0,
+    /* BAY_FORM_GEMM: always stream the matrix from device memory (three launches per
+     * half-step), even when it would fit in shared memory; matrices that do not fit are
+     * streamed regardless. */
+    BAY_MODEL_GEMM_STREAMING = 1u << 1
 };
 
 typedef struct bay_model_desc {

@@ -176,10 +176,12 @@ def _regression_data(rng, n, F, kind):
     return np.concatenate([rows.reshape(-1), hyper]), rows.size
 
 
+@pytest.mark.parametrize("streaming", [False, True])
 @pytest.mark.parametrize("case", ["mvn50", "logistic", "robust_t"])
-def test_gemm_logfn_matches_fp64(factory, M, oracle, case):
+def test_gemm_logfn_matches_fp64(factory, M, oracle, case, streaming):
     """GEMM-form log densities of 1000 walkers vs the oracle's FP64 density: relative
-    error below 2e-5 (fp32 dot products over F features, Kahan row sums)."""
+    error below 2e-5 (fp32 dot products over F features, Kahan row sums), with the
+    matrix resident in shared memory and streamed from device memory."""
     rng = np.random.default_rng(3)
     if case == "mvn50":
         D = 50
@@ -197,7 +199,7 @@ def test_gemm_logfn_matches_fp64(factory, M, oracle, case):
         params, dl = _regression_data(rng, 512, D - 1, "robust_t")
         model, oname = M.robust_t_model(D - 1), "robust_t"
         init = lambda s: s.init_position_normal(4, 0.0, 0.3)
-    sf = factory.mcmc_factory(model, form="gemm")
+    sf = factory.mcmc_factory(model, form="gemm", streaming=streaming)
     s = sf.create_sampler(3, 1000, params)
     init(s)
     pos = s.positions().T.astype(np.float64)
@@ -236,6 +238,53 @@ def test_gemm_step_consistency_mvn50(factory, M, oracle):
         got = s.positions().T.reshape(W, D)
         rows = np.any(got != r.xs.reshape(W, D), axis=1)
         assert rows.sum() <= 8, "step %d: %d walkers differ" % (t, rows.sum())
+    s.release()
+    sf.release()
+
+
+@pytest.mark.parametrize("rows", [200, 3000])
+def test_gemm_streaming_matches_resident_trajectory(factory, M, rows):
+    """Logistic regression: the streamed GEMM form and the resident form propose the same
+    moves (same Philox draws); densities differ only in summation order, so trajectories
+    agree except for marginal accept decisions.  3000 rows also spans several row
+    super-blocks."""
+    rng = np.random.default_rng(9)
+    F = 12
+    params, dl = _regression_data(rng, rows, F, "logistic")
+    out = []
+    for streaming in (False, True):
+        if not streaming and rows * F > 30000:
+            continue
+        sf = factory.mcmc_factory(M.logistic_model(F), form="gemm", streaming=streaming)
+        s = sf.create_sampler(5, 2048, params)
+        s.init_position_normal(6, 0.0, 0.2)
+        s.burn_in(3, 2.0)
+        out.append((s.positions().copy(), s.logfn().copy()))
+        s.release()
+        sf.release()
+    if len(out) == 2:
+        rows_differ = np.any(out[0][0] != out[1][0], axis=0).sum()
+        assert rows_differ <= 20, rows_differ
+        np.testing.assert_allclose(out[0][1], out[1][1], rtol=2e-5, atol=1e-3)
+
+
+def test_gemm_streaming_run_sampler(factory, M, oracle):
+    """Streamed form, accu path: acceptance count, per-step means (last = mean of the
+    walkers) and the densities of the final walkers against the FP64 oracle."""
+    rng = np.random.default_rng(4)
+    F = 8
+    params, dl = _regression_data(rng, 5000, F - 1, "robust_t")
+    sf = factory.mcmc_factory(M.robust_t_model(F - 1), form="gemm", streaming=True)
+    s = sf.create_sampler(8, 1024, params)
+    s.init_position_normal(9, 0.0, 0.2)
+    s.burn_in(50, 2.0)
+    r = s.run_sampler(64, 2.0, return_means=True)
+    assert 0.0 < r["acceptance_rate"] < 1.0
+    np.testing.assert_allclose(r["means"][:, -1], s.mean(), rtol=1e-5, atol=1e-6)
+    pos = s.positions().T.astype(np.float64)
+    lf = s.logfn().astype(np.float64)
+    want = np.array([oracle.logfn64("robust_t", params, dl, F, p) for p in pos[:64]])
+    assert (np.abs(lf[:64] - want) / np.abs(want)).max() < 2e-5
     s.release()
     sf.release()
 
