@@ -21,6 +21,7 @@ FORM_TILED = 1
 FORM_GEMM = 2
 MODEL_ACCEPT_REF = 1
 MODEL_GEMM_STREAMING = 2
+MODEL_GEMM_TENSOR = 4
 HIST_COMPAT_START1 = 1
 HIST_COMPAT_ZERO_LIMITS = 2
 

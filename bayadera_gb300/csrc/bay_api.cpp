@@ -53,6 +53,7 @@ struct DriverApi {
     PFN_cuLibraryGetKernel_v12000 LibraryGetKernel = nullptr;
     PFN_cuLaunchKernel_v4000 LaunchKernel = nullptr;
     PFN_cuKernelSetAttribute_v12000 KernelSetAttribute = nullptr;
+    PFN_cuTensorMapEncodeTiled_v12000 TensorMapEncodeTiled = nullptr;
     bool loaded = false;
 };
 DriverApi g_cu;
@@ -87,6 +88,7 @@ void load_driver_api() {
     resolve("cuLibraryGetKernel", g_cu.LibraryGetKernel, 12000);
     resolve("cuLaunchKernel", g_cu.LaunchKernel, 4000);
     resolve("cuKernelSetAttribute", g_cu.KernelSetAttribute, 12000);
+    resolve("cuTensorMapEncodeTiled", g_cu.TensorMapEncodeTiled, 12000);
     g_cu.loaded = true;
 }
 
@@ -175,6 +177,11 @@ struct bay_model {
     CUkernel k_gp[3] = {nullptr, nullptr, nullptr};
     CUkernel k_gr[2] = {nullptr, nullptr};
     CUkernel k_ga[3] = {nullptr, nullptr, nullptr};
+    // GEMM form on the tensor cores: rows kernels [move, logfn], walker sub-tiles per CTA,
+    // shared-memory stages, dynamic shared memory
+    CUkernel k_gt[2] = {nullptr, nullptr};
+    uint32_t tc_g = 0, tc_stages = 0;
+    size_t tc_smem = 0;
 };
 
 namespace {
@@ -189,6 +196,45 @@ size_t gemm_smem_bytes(const bay_model* m, uint64_t rows) {
     const uint64_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1;
     return sizeof(float) * (m->gemm_features * np + m->gemm_features * kGemmWalkers +
                             kGemmWalkers * dpad + np * auxs);
+}
+
+// Tensor-core rows kernel (bay_gemm_rows_tc_impl): G sub-tiles of 128 walkers per CTA
+// with their bf16 hi + lo coefficient operand resident (G x ceil(F/64) x 32 KB), a ring
+// of S stages of one 128-row x 64-feature hi + lo chunk (32 KB each), two aux buffers,
+// the barriers and flags, and 1 KB to align the operands to the 128-byte swizzle's
+// 1024-byte period.  Largest G (fewer re-reads of the matrix), then up to 6 stages.
+constexpr size_t kTcSmemMax = 232448;  // opt-in dynamic shared memory per CTA, sm_100 family
+bool tc_plan(uint32_t features, uint32_t aux_len, uint32_t* G, uint32_t* S, size_t* smem) {
+    const size_t kc = (features + 63) / 64, auxs = aux_len ? aux_len : 1;
+    for (uint32_t g = 2; g >= 1; --g) {
+        const size_t fixed = (size_t)g * kc * 32768 + 2 * 128 * auxs * sizeof(float) + 1024 + 256;
+        if (fixed + 2 * 32768 > kTcSmemMax) continue;
+        const size_t st = std::min<size_t>(6, (kTcSmemMax - fixed) / 32768);
+        *G = g;
+        *S = (uint32_t)st;
+        *smem = fixed + st * 32768;
+        return true;
+    }
+    return false;
+}
+
+// Host image of the kernel's bay_tmaps parameter.
+struct TcMaps {
+    CUtensorMap xh, xl, bh, bl;
+};
+
+// 2-D bf16 tensor map over a row-major [rows][cols] array, 64 x 128 boxes, 128B swizzle.
+void encode_bf16_map(CUtensorMap* m, void* base, uint64_t cols, uint64_t rows) {
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(cols * 2)};
+    const cuuint32_t box[2] = {64, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    cu_check(g_cu.TensorMapEncodeTiled(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides,
+                                       box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                       CU_TENSOR_MAP_SWIZZLE_128B,
+                                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE),
+             "cuTensorMapEncodeTiled");
 }
 }  // namespace
 
@@ -307,8 +353,9 @@ struct bay_sampler {
                                    ctx->stream),
                    "cudaMemcpy(status)");
         cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
-        if (st) fail(BAY_ERR_DEVICE, "a kernel gave up waiting for its shared-memory copy "
-                                     "(device status " + std::to_string(st) + ")");
+        if (st) fail(BAY_ERR_DEVICE, std::string("a kernel gave up waiting for ") +
+                                         ((st & 2u) ? "its tensor-core pipeline" : "its shared-memory copy") +
+                                         " (device status " + std::to_string(st) + ")");
     }
 
     // GEMM form, streaming mode (matrix read from device memory in row blocks)
@@ -317,6 +364,13 @@ struct bay_sampler {
           *s_part = nullptr;
     uint32_t s_nsb = 0, s_sbrows = 0;
     size_t smem_rows = 0;
+    // streaming on the tensor cores: bf16 hi + lo matrix [rows_pad][tc_fp], coefficient
+    // operand [tc_wpad][tc_fp] (hi, lo), the aux values in gemm_lay [rows_pad][aux]
+    bool tc = false;
+    uint32_t tc_fp = 0;
+    uint64_t tc_rows_pad = 0, tc_wpad = 0;
+    unsigned short *tc_xh = nullptr, *tc_xl = nullptr, *s_bh = nullptr, *s_bl = nullptr;
+    TcMaps tc_maps;
 
     uint64_t per_cta() const {
         if (streaming) return 256;  // the accept kernel: one thread per walker
@@ -340,8 +394,18 @@ struct bay_sampler {
         const uint64_t nk = mode == 2 ? W : K;
         const unsigned g1 = (unsigned)((nk + 255) / 256), gt = (unsigned)((nk + 127) / 128);
         launch(model->k_gp[mode], g1, 1, 0, p, st, "cuLaunchKernel(gemm propose)");
-        launch(model->k_gr[mode == 2 ? 1 : 0], gt, s_nsb, smem_rows, p, st,
-               "cuLaunchKernel(gemm rows)");
+        if (tc) {
+            const uint64_t per = 128ull * model->tc_g;
+            void* args[] = {&p, &tc_maps};
+            cu_check(g_cu.LaunchKernel((CUfunction)model->k_gt[mode == 2 ? 1 : 0],
+                                       (unsigned)((nk + per - 1) / per), s_nsb, 1,
+                                       64 + 128 * model->tc_g, 1, 1, (unsigned)model->tc_smem,
+                                       (CUstream)st, args, nullptr),
+                     "cuLaunchKernel(gemm rows, tensor cores)");
+        } else {
+            launch(model->k_gr[mode == 2 ? 1 : 0], gt, s_nsb, smem_rows, p, st,
+                   "cuLaunchKernel(gemm rows)");
+        }
         launch(model->k_ga[mode], g1, 1, 0, p, st, "cuLaunchKernel(gemm accept)");
         if (st == ctx->stream) bay::count_launches(3);
     }
@@ -375,6 +439,10 @@ struct bay_sampler {
         p.s_part = s_part;
         p.s_nsb = s_nsb;
         p.s_sbrows = s_sbrows;
+        p.s_bh = s_bh;
+        p.s_bl = s_bl;
+        p.tc_fp = tc_fp;
+        p.tc_pad = 0;
         return p;
     }
 
@@ -611,6 +679,8 @@ struct Codegen {
     std::string src;
     std::vector<std::string> opts;
     uint32_t cta = 256, wpc = 1;
+    uint32_t tc_g = 0, tc_stages = 0;
+    size_t tc_smem = 0;
 };
 
 // Source and NVRTC options of a model's fused kernels (the reference's stretch-options,
@@ -671,6 +741,13 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
         opts.push_back(std::string("-DBAY_GEMM_PREP=") + d->tile_prep);
         opts.push_back(std::string("-DBAY_GEMM_TERM=") + d->tile_term);
         opts.push_back(std::string("-DBAY_GEMM_WALKER=") + d->tile_walker);
+        if (d->flags & BAY_MODEL_GEMM_TENSOR) {
+            if (!tc_plan(d->gemm_features, d->gemm_aux_len, &g.tc_g, &g.tc_stages, &g.tc_smem))
+                fail(BAY_ERR_ARG, "tensor-core GEMM form: at most 320 features");
+            opts.push_back("-DBAY_GEMM_TC=1");
+            opts.push_back("-DBAY_TC_G=" + std::to_string(g.tc_g));
+            opts.push_back("-DBAY_TC_STAGES=" + std::to_string(g.tc_stages));
+        }
         wpc = 64;
     } else {
         fail(BAY_ERR_ARG, "unknown model form");
@@ -722,6 +799,9 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
             m->gemm_aux_len = d->gemm_aux_len;
             m->gemm_offset = d->gemm_offset;
             m->gemm_rows = d->gemm_rows;
+            m->tc_g = g.tc_g;
+            m->tc_stages = g.tc_stages;
+            m->tc_smem = g.tc_smem;
         }
         try {
             cu_check(g_cu.LibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr,
@@ -746,6 +826,16 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                     cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                      (int)kGemmMaxSmem, k, dev),
                              "cuKernelSetAttribute(smem)");
+                if (m->tc_g) {
+                    cu_check(g_cu.LibraryGetKernel(&m->k_gt[0], m->lib, "bay_gemm_rows_tc_move"),
+                             "GetKernel(rows tc)");
+                    cu_check(g_cu.LibraryGetKernel(&m->k_gt[1], m->lib, "bay_gemm_rows_tc_logfn"),
+                             "GetKernel(rows tc)");
+                    for (CUkernel k : {m->k_gt[0], m->k_gt[1]})
+                        cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                         (int)m->tc_smem, k, dev),
+                                 "cuKernelSetAttribute(smem)");
+                }
             }
         } catch (...) {
             if (m->lib) g_cu.LibraryUnload(m->lib);
@@ -806,8 +896,28 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                 fail(BAY_ERR_ARG, "the GEMM matrix does not fit its params block");
             }
             s->smem = gemm_smem_bytes(m, s->gemm_rows);
-            s->streaming = (m->flags & BAY_MODEL_GEMM_STREAMING) || s->smem > kGemmMaxSmem;
-            if (s->streaming) {
+            s->tc = m->tc_g != 0;
+            s->streaming = s->tc || (m->flags & BAY_MODEL_GEMM_STREAMING) || s->smem > kGemmMaxSmem;
+            if (s->tc) {
+                // rows kernel on the tensor cores: one CTA per SM over (walker groups x
+                // row super-blocks), one wave; super-blocks are whole 128-row tiles
+                s->smem = 0;
+                if (s->gemm_rows > 0x7fffff00ull) {
+                    delete s;
+                    fail(BAY_ERR_ARG, "tensor-core GEMM form: at most 2^31 - 256 rows");
+                }
+                const uint64_t n_tiles = (s->gemm_rows + 127) / 128;
+                const uint64_t per = 128ull * m->tc_g;
+                const uint64_t n_wg = (s->K + per - 1) / per;
+                uint64_t nsb = std::max<uint64_t>(1, (uint64_t)c->sm_count / n_wg);
+                nsb = std::min<uint64_t>(nsb, n_tiles);
+                const uint64_t tiles = (n_tiles + nsb - 1) / nsb;
+                s->s_sbrows = (uint32_t)(tiles * 128);
+                s->s_nsb = (uint32_t)((s->gemm_rows + s->s_sbrows - 1) / s->s_sbrows);
+                s->tc_fp = (m->gemm_features + 63) & ~63u;
+                s->tc_rows_pad = n_tiles * 128;
+                s->tc_wpad = (walkers + per - 1) / per * per;
+            } else if (s->streaming) {
                 // rows kernel: the coefficient tile (F x 128) + one 32-feature matrix chunk
                 s->smem = 0;
                 s->smem_rows = sizeof(float) * ((size_t)m->gemm_features * 128 + 32 * 129);
@@ -856,6 +966,28 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                 s->s_w = (float*)c->alloc(sizeof(float) * Wn);
                 s->s_zu = (float*)c->alloc(sizeof(float) * Wn * 2);
                 s->s_part = (float*)c->alloc(sizeof(float) * Wn * 2 * s->s_nsb);
+                if (s->tc) {
+                    const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
+                    const size_t nx = (size_t)s->tc_rows_pad * s->tc_fp;
+                    const size_t nb = (size_t)s->tc_wpad * s->tc_fp;
+                    s->tc_xh = (unsigned short*)c->alloc(2 * nx);
+                    s->tc_xl = (unsigned short*)c->alloc(2 * nx);
+                    s->gemm_lay = (float*)c->alloc(sizeof(float) * (size_t)s->tc_rows_pad * auxs);
+                    s->s_bh = (unsigned short*)c->alloc(2 * nb);
+                    s->s_bl = (unsigned short*)c->alloc(2 * nb);
+                    cuda_check(cudaMemsetAsync(s->s_bh, 0, 2 * nb, c->stream), "memset");
+                    cuda_check(cudaMemsetAsync(s->s_bl, 0, 2 * nb, c->stream), "memset");
+                    cuda_check(bay::launch_gemm_split(s->params + s->gemm_base, m->gemm_ld,
+                                                      (uint32_t)s->gemm_rows, m->gemm_features,
+                                                      s->tc_fp, s->tc_rows_pad, m->gemm_aux_col,
+                                                      m->gemm_aux_len, auxs, s->tc_xh, s->tc_xl,
+                                                      s->gemm_lay, c->stream),
+                               "gemm_split");
+                    encode_bf16_map(&s->tc_maps.xh, s->tc_xh, s->tc_fp, s->tc_rows_pad);
+                    encode_bf16_map(&s->tc_maps.xl, s->tc_xl, s->tc_fp, s->tc_rows_pad);
+                    encode_bf16_map(&s->tc_maps.bh, s->s_bh, s->tc_fp, s->tc_wpad);
+                    encode_bf16_map(&s->tc_maps.bl, s->s_bl, s->tc_fp, s->tc_wpad);
+                }
             } else if (m->form == BAY_FORM_GEMM) {
                 s->gemm_np = (uint32_t)((s->gemm_rows + 63) & ~63ull);
                 const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
@@ -889,6 +1021,7 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
             c->release(s->means);
             c->release(s->gemm_lay);
             for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
+            for (unsigned short* q : {s->tc_xh, s->tc_xl, s->s_bh, s->s_bl}) c->release(q);
             if (s->own_params) c->release((void*)s->params);
             delete s;
             throw;
@@ -926,6 +1059,7 @@ int bay_sampler_release(bay_sampler* s) {
         c->release(s->counts);
         c->release(s->gemm_lay);
         for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
+        for (unsigned short* q : {s->tc_xh, s->tc_xl, s->s_bh, s->s_bl}) c->release(q);
         if (s->own_params) c->release((void*)s->params);
         delete s;
     });

@@ -271,6 +271,35 @@ __global__ void gemm_layout(const float* A, uint64_t ld, uint32_t rows, uint32_t
     }
 }
 
+// bf16 of a float rounded to nearest even, as its 16 bits (NaN stays a quiet NaN)
+__device__ __forceinline__ unsigned short bf16_rn(float x) {
+    unsigned int u = __float_as_uint(x);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (unsigned short)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (unsigned short)(u >> 16);
+}
+
+// Tensor-core GEMM form: the matrix as bf16 hi + lo, row-major [rows_pad][Fp] (features
+// past F and rows past `rows` zero), and the rows' aux values [rows_pad][auxs].
+__global__ void gemm_split(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t Fp,
+                           uint64_t rows_pad, uint32_t aux_col, uint32_t aux_len, uint32_t auxs,
+                           unsigned short* hi, unsigned short* lo, float* aux) {
+    const uint64_t nA = rows_pad * Fp, n = nA + rows_pad * auxs;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < nA) {
+            const uint64_t r = i / Fp, f = i % Fp;
+            const float v = (r < rows && f < F) ? A[r * ld + f] : 0.0f;
+            const unsigned short h = bf16_rn(v);
+            hi[i] = h;
+            lo[i] = bf16_rn(__fsub_rn(v, __uint_as_float((unsigned int)h << 16)));
+        } else {
+            const uint64_t e = i - nA, r = e / auxs, c = e % auxs;
+            aux[e] = (r < rows && c < aux_len) ? A[r * ld + aux_col + c] : 0.0f;
+        }
+    }
+}
+
 __global__ void fill_u32(uint32_t* p, uint32_t v, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -457,6 +486,16 @@ cudaError_t launch_gemm_layout(const float* A, uint64_t ld, uint32_t rows, uint3
                                cudaStream_t s) {
     const uint64_t n = (uint64_t)F * NP + (uint64_t)NP * auxs;
     gemm_layout<<<grid_for(n, 256), 256, 0, s>>>(A, ld, rows, F, NP, aux_col, aux_len, auxs, lay);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_split(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t Fp,
+                              uint64_t rows_pad, uint32_t aux_col, uint32_t aux_len, uint32_t auxs,
+                              unsigned short* hi, unsigned short* lo, float* aux, cudaStream_t s) {
+    const uint64_t n = rows_pad * Fp + rows_pad * auxs;
+    gemm_split<<<grid_for(n, 256), 256, 0, s>>>(A, ld, rows, F, Fp, rows_pad, aux_col, aux_len, auxs,
+                                                 hi, lo, aux);
     g_launches++;
     return cudaGetLastError();
 }

@@ -46,6 +46,10 @@ struct bay_stretch_params {
     float* s_part;
     unsigned int s_nsb;
     unsigned int s_sbrows;
+    unsigned short* s_bh;
+    unsigned short* s_bl;
+    unsigned int tc_fp;
+    unsigned int tc_pad;
 };
 
 enum {
@@ -99,6 +103,11 @@ cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, uint64_t n, cudaStream_t s)
 cudaError_t launch_gemm_layout(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t NP,
                                uint32_t aux_col, uint32_t aux_len, uint32_t auxs, float* lay,
                                cudaStream_t s);
+// Tensor-core GEMM form: bf16 hi + lo copies of the matrix, [rows_pad][Fp] row-major with
+// zero padding, and the rows' aux values [rows_pad][auxs].
+cudaError_t launch_gemm_split(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t Fp,
+                              uint64_t rows_pad, uint32_t aux_col, uint32_t aux_len, uint32_t auxs,
+                              unsigned short* hi, unsigned short* lo, float* aux, cudaStream_t s);
 // Per-step ensemble means of `nsteps` accu steps from the stretch kernels' per-CTA sums
 // part[((t*2 + half)*D + d)*G + cta]: means[(ctl->step[1] + t)*D + d] = sum / W, summed
 // in FP64 in (half, cta) order; steps at or past means_cap are dropped.

@@ -85,6 +85,12 @@ struct bay_stretch_params {
     float* s_part;                  // [nsb][nk] compensated (hi, lo) partial row sums
     unsigned int s_nsb;             // row super-blocks
     unsigned int s_sbrows;          // rows per super-block (a multiple of 128)
+    // GEMM form on the tensor cores: the coefficient block split into bf16 hi + lo,
+    // [walker][tc_fp] each (tc_fp = F rounded up to 64; padding columns stay zero)
+    unsigned short* s_bh;
+    unsigned short* s_bl;
+    unsigned int tc_fp;
+    unsigned int tc_pad;
 };
 
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
@@ -476,6 +482,17 @@ extern "C" __global__ void __launch_bounds__(256) bay_logfn_all(bay_stretch_para
 #define BAY_SF 32
 #define BAY_XS (BAY_SR + 1)   // odd row stride of the staged matrix chunk (no bank conflicts)
 
+// bf16 of a float rounded to nearest even, as its 16 bits (NaN stays a quiet NaN)
+__device__ __forceinline__ unsigned short bay_bf16_rn(float x) {
+    unsigned int u = __float_as_uint(x);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (unsigned short)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (unsigned short)(u >> 16);
+}
+__device__ __forceinline__ float bay_bf16_float(unsigned short h) {
+    return __uint_as_float((unsigned int)h << 16);
+}
+
 template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions
 __device__ __forceinline__ void bay_gemm_propose_impl(const bay_stretch_params& P) {
     const unsigned int kind = MODE == 1 ? 1u : 0u;
@@ -505,7 +522,17 @@ __device__ __forceinline__ void bay_gemm_propose_impl(const bay_stretch_params& 
         P.s_zu[2 * (size_t)k] = z;
         P.s_zu[2 * (size_t)k + 1] = bay_u01(r.z);
     }
-    for (int f = 0; f < BAY_GEMM_F; ++f) P.s_b[(size_t)k * BAY_GEMM_F + f] = y[BAY_GEMM_COEF + f];
+    if (!P.s_bh) {
+        for (int f = 0; f < BAY_GEMM_F; ++f) P.s_b[(size_t)k * BAY_GEMM_F + f] = y[BAY_GEMM_COEF + f];
+    } else {
+        // the tensor-core form's operand: coefficient = hi + lo, both bf16
+        for (int f = 0; f < BAY_GEMM_F; ++f) {
+            const float v = y[BAY_GEMM_COEF + f];
+            const unsigned short h = bay_bf16_rn(v);
+            P.s_bh[(size_t)k * P.tc_fp + f] = h;
+            P.s_bl[(size_t)k * P.tc_fp + f] = bay_bf16_rn(__fsub_rn(v, bay_bf16_float(h)));
+        }
+    }
     const float* hyper = P.params + P.data_len;
     float pr[BAY_PREP_LEN];
 #pragma unroll
@@ -693,6 +720,366 @@ extern "C" __global__ void __launch_bounds__(256) bay_gemm_accept_accu(bay_stret
 extern "C" __global__ void __launch_bounds__(256) bay_gemm_accept_logfn(bay_stretch_params P) {
     bay_gemm_accept_impl<2>(P);
 }
+
+#if BAY_GEMM_TC
+// ---------------------------------------------------------------- GEMM form, tensor cores
+// The rows launch of the streaming form with eta on the 5th-generation tensor cores:
+// eta[walker][row] = sum_f B[walker][f] A[row][f], A and B each split into bf16 hi + lo
+// and three products (hi.hi + hi.lo + lo.hi) accumulated in fp32 in tensor memory; the
+// dropped lo.lo product is below 2^-16 of each term.  tcgen05.mma kind::f16 with
+// M = 128 walkers (TMEM lanes), N = 128 rows (TMEM columns), K = 16 per instruction,
+// both operands K-major in shared memory with the 128-byte swizzle TMA writes.
+// CTA roles: warp 0 -- TMA producer (the CTA's walker operand once, then each 128-row
+// tile in 64-feature chunks through a ring of BAY_TC_STAGES stages); warp 1 -- TMEM
+// allocation and the MMA issue (one thread); warps 2 .. 2 + 4 BAY_TC_G - 1 -- epilogue,
+// one thread per walker: tcgen05.ld of its TMEM lane, the model's row term, a Kahan
+// sum over the super-block's rows.  Two accumulator buffers in TMEM let the MMAs of
+// tile t + 1 run under the epilogue of tile t.  Every wait is bounded in time; a wait
+// that gives up sets the sampler's status word and the CTA's abort flag, and the CTA
+// drains its own copies and MMAs, frees its TMEM and exits.
+#ifndef BAY_TC_G
+#define BAY_TC_G 1
+#endif
+#ifndef BAY_TC_STAGES
+#define BAY_TC_STAGES 2
+#endif
+#define BAY_TC_FP ((BAY_GEMM_F + 63) / 64 * 64)
+#define BAY_TC_KC (BAY_TC_FP / 64)
+#define BAY_TC_TILE 16384u                      // one 128 x 64 bf16 operand chunk
+#define BAY_TC_WBYTES ((unsigned int)BAY_TC_G * BAY_TC_KC * 2u * BAY_TC_TILE)
+#define BAY_TC_SBYTES (2u * BAY_TC_TILE)        // a stage: rows hi + lo chunk
+#define BAY_TC_AUXF (128u * BAY_AUXS)
+#define BAY_TC_NEPI (128u * BAY_TC_G)           // epilogue threads
+#define BAY_TC_THREADS (64 + 128 * BAY_TC_G)
+#define BAY_TC_COLS (BAY_TC_G == 2 ? 512u : 256u)
+#define BAY_TC_WAIT_NS 2000000000ull
+// instruction descriptor: fp32 accumulator, bf16 A and B, both K-major, N = 128, M = 128
+#define BAY_TC_IDESC ((1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24))
+
+// the four TMA tensor maps (CUtensorMap, 128 bytes each), a __grid_constant__ parameter
+struct __align__(64) bay_tmaps {
+    unsigned long long xh[16];   // matrix rows, bf16 hi: dims {tc_fp, rows_pad}, box {64, 128}
+    unsigned long long xl[16];   // matrix rows, bf16 lo
+    unsigned long long bh[16];   // coefficient block, bf16 hi: dims {tc_fp, walkers_pad}
+    unsigned long long bl[16];   // coefficient block, bf16 lo
+};
+
+__device__ __forceinline__ unsigned long long bay_globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for the completion of the phase of parity `par` of the mbarrier at shared address
+// `bar`.  Gives up after BAY_TC_WAIT_NS, or as soon as another role has given up (abort
+// flag set; pass abort = nullptr for a wait that must not be cut short).  Giving up on
+// time sets the abort flag and the sampler's status word.
+__device__ __forceinline__ bool bay_tc_wait(unsigned int bar, unsigned int par,
+                                            volatile unsigned int* abort, unsigned int* status) {
+    unsigned long long t0 = 0;
+    for (unsigned int it = 0;; ++it) {
+        unsigned int ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok) : "r"(bar), "r"(par) : "memory");
+        if (ok) return true;
+        if ((it & 15u) == 0u) {
+            if (abort && *abort) return false;
+            const unsigned long long t = bay_globaltimer();
+            if (it == 0u) {
+                t0 = t;
+            } else if (t - t0 > BAY_TC_WAIT_NS) {
+                if (abort) *abort = 1u;
+                atomicOr(status, 2u);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void bay_mbar_init(unsigned int bar, unsigned int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bay_expect_tx(unsigned int bar, unsigned int bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bay_tma2d(unsigned int dst, const void* map, int c0, int c1,
+                                          unsigned int bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"((unsigned long long)map), "r"(c0), "r"(c1), "r"(bar) : "memory");
+}
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ unsigned long long bay_sdesc(unsigned int saddr) {
+    return (unsigned long long)((saddr & 0x3FFFFu) >> 4)
+         | (1ull << 16)                                    // leading offset (unused here)
+         | ((unsigned long long)(1024u >> 4) << 32)        // stride offset
+         | (1ull << 46)                                    // tcgen05 descriptor version
+         | (2ull << 61);                                   // 128-byte swizzle
+}
+__device__ __forceinline__ void bay_mma(unsigned int d, unsigned long long a, unsigned long long b,
+                                        unsigned int acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(d), "l"(a), "l"(b), "r"(BAY_TC_IDESC), "r"(acc) : "memory");
+}
+__device__ __forceinline__ void bay_mma_commit(unsigned int bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void bay_tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void bay_tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// 32 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void bay_tmem_ld32(unsigned int ta, float (&v)[32]) {
+    unsigned int r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+        "%28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(ta));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int MODE>  // 0: move (K walkers of the moving half), 2: log density of all W
+__device__ __forceinline__ void bay_gemm_rows_tc_impl(const bay_stretch_params& P,
+                                                      const bay_tmaps& T) {
+    extern __shared__ __align__(1024) unsigned char bay_smem_tc[];
+    const unsigned int raw = (unsigned int)__cvta_generic_to_shared(bay_smem_tc);
+    const unsigned int pad = ((raw + 1023u) & ~1023u) - raw;
+    unsigned char* sm = bay_smem_tc + pad;
+    const unsigned int s_wop = raw + pad;                    // walker operand [G][KC][hi,lo]
+    const unsigned int s_stg = s_wop + BAY_TC_WBYTES;        // row stages [S][hi,lo]
+    float* saux = (float*)(sm + BAY_TC_WBYTES + BAY_TC_STAGES * BAY_TC_SBYTES);  // [2][AUXF]
+    unsigned long long* bars = (unsigned long long*)(saux + 2 * BAY_TC_AUXF);
+    volatile unsigned int* flags = (volatile unsigned int*)(bars + 2 * BAY_TC_STAGES + 6);
+    const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(bars);
+    // barriers: full[S], empty[S], tmem full[2], tmem empty[2], walker operand, drain
+    const unsigned int b_full = bar0, b_empty = bar0 + 8u * BAY_TC_STAGES;
+    const unsigned int b_tfull = bar0 + 16u * BAY_TC_STAGES, b_tempty = b_tfull + 16u;
+    const unsigned int b_wop = b_tempty + 16u, b_drain = b_wop + 8u;
+    // flags: [0] TMEM base, [1] abort, [2], [3] epilogue go flags of the two buffers
+    volatile unsigned int* abort = flags + 1;
+    unsigned int* status = &P.ctl->status;
+
+    const unsigned int warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const unsigned int nk = MODE == 2 ? P.W : P.K;
+    const unsigned int k0 = blockIdx.x * (128u * BAY_TC_G);
+    const unsigned int rows = (unsigned int)P.gemm_rows;
+    const unsigned int rb = blockIdx.y * P.s_sbrows;
+    const unsigned long long re64 = (unsigned long long)rb + P.s_sbrows;
+    const unsigned int re = re64 < rows ? (unsigned int)re64 : rows;
+    const unsigned int ntile = (re - rb + 127u) / 128u;
+
+    if (threadIdx.x == 0) {
+        for (unsigned int s = 0; s < BAY_TC_STAGES; ++s) {
+            bay_mbar_init(b_full + 8u * s, 1u);
+            bay_mbar_init(b_empty + 8u * s, 1u);
+        }
+        for (unsigned int b = 0; b < 2; ++b) {
+            bay_mbar_init(b_tfull + 8u * b, 1u);
+            bay_mbar_init(b_tempty + 8u * b, 4u * BAY_TC_G);
+        }
+        bay_mbar_init(b_wop, 1u);
+        bay_mbar_init(b_drain, 1u);
+        flags[1] = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        const unsigned int dst = (unsigned int)__cvta_generic_to_shared((const void*)flags);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(dst), "r"(BAY_TC_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    bay_tc_fence_before();
+    __syncthreads();
+    bay_tc_fence_after();
+    const unsigned int tmem = flags[0];
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer
+            bay_expect_tx(b_wop, BAY_TC_WBYTES);
+            for (unsigned int g = 0; g < BAY_TC_G; ++g)
+                for (unsigned int c = 0; c < BAY_TC_KC; ++c) {
+                    const unsigned int dst = s_wop + ((g * BAY_TC_KC + c) * 2u) * BAY_TC_TILE;
+                    bay_tma2d(dst, T.bh, (int)(c * 64u), (int)(k0 + g * 128u), b_wop);
+                    bay_tma2d(dst + BAY_TC_TILE, T.bl, (int)(c * 64u), (int)(k0 + g * 128u), b_wop);
+                }
+            unsigned int issued = 0;
+            bool ok = true;
+            for (unsigned int t = 0; t < ntile && ok; ++t) {
+                for (unsigned int c = 0; c < BAY_TC_KC; ++c) {
+                    const unsigned int s = issued % BAY_TC_STAGES, u = issued / BAY_TC_STAGES;
+                    if (u > 0u && !bay_tc_wait(b_empty + 8u * s, (u - 1u) & 1u, abort, status)) {
+                        ok = false;
+                        break;
+                    }
+                    const unsigned int dst = s_stg + s * BAY_TC_SBYTES;
+                    bay_expect_tx(b_full + 8u * s, BAY_TC_SBYTES);
+                    bay_tma2d(dst, T.xh, (int)(c * 64u), (int)(rb + t * 128u), b_full + 8u * s);
+                    bay_tma2d(dst + BAY_TC_TILE, T.xl, (int)(c * 64u), (int)(rb + t * 128u),
+                              b_full + 8u * s);
+                    ++issued;
+                }
+            }
+            // drain: every copy issued here has landed before the CTA may exit
+            bay_tc_wait(b_wop, 0u, nullptr, status);
+            for (unsigned int i = issued > BAY_TC_STAGES ? issued - BAY_TC_STAGES : 0u; i < issued; ++i)
+                bay_tc_wait(b_full + 8u * (i % BAY_TC_STAGES), (i / BAY_TC_STAGES) & 1u, nullptr, status);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issue
+            bool ok = bay_tc_wait(b_wop, 0u, abort, status);
+            bay_tc_fence_after();
+            unsigned int i = 0;
+            for (unsigned int t = 0; t < ntile && ok; ++t) {
+                const unsigned int b = t & 1u, ub = t >> 1;
+                if (ub > 0u && !(ok = bay_tc_wait(b_tempty + 8u * b, (ub - 1u) & 1u, abort, status)))
+                    break;
+                bay_tc_fence_after();
+                const unsigned int d0 = tmem + b * (128u * BAY_TC_G);
+                for (unsigned int c = 0; c < BAY_TC_KC; ++c, ++i) {
+                    const unsigned int s = i % BAY_TC_STAGES, u = i / BAY_TC_STAGES;
+                    if (!(ok = bay_tc_wait(b_full + 8u * s, u & 1u, abort, status))) break;
+                    bay_tc_fence_after();
+                    const unsigned int xs = s_stg + s * BAY_TC_SBYTES;
+#pragma unroll
+                    for (unsigned int g = 0; g < BAY_TC_G; ++g) {
+                        const unsigned int wa = s_wop + ((g * BAY_TC_KC + c) * 2u) * BAY_TC_TILE;
+#pragma unroll
+                        for (unsigned int ks = 0; ks < 4u; ++ks) {
+                            const unsigned long long ah = bay_sdesc(wa + 32u * ks);
+                            const unsigned long long al = bay_sdesc(wa + BAY_TC_TILE + 32u * ks);
+                            const unsigned long long xh = bay_sdesc(xs + 32u * ks);
+                            const unsigned long long xl = bay_sdesc(xs + BAY_TC_TILE + 32u * ks);
+                            const unsigned int d = d0 + g * 128u;
+                            bay_mma(d, ah, xh, (c | ks) != 0u ? 1u : 0u);
+                            bay_mma(d, ah, xl, 1u);
+                            bay_mma(d, al, xh, 1u);
+                        }
+                    }
+                    bay_mma_commit(b_empty + 8u * s);  // the stage is free once these finish
+                }
+                if (!ok) break;
+                bay_mma_commit(b_tfull + 8u * b);
+            }
+            // drain: every MMA issued here has finished before TMEM is released
+            bay_mma_commit(b_drain);
+            bay_tc_wait(b_drain, 0u, nullptr, status);
+        }
+    } else {
+        // ---- epilogue: one thread per walker
+        const unsigned int et = threadIdx.x - 64u;
+        const unsigned int g = (warp - 2u) >> 2, q = warp & 3u;
+        const unsigned int kw = k0 + g * 128u + 32u * q + lane;
+        const bool wv = kw < nk;
+        const unsigned int kc = wv ? kw : nk - 1u;
+        float prep[BAY_PREP_LEN];
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) prep[i] = P.s_prep[(size_t)kc * BAY_PREP_LEN + i];
+        const float* xw = P.s_y + (size_t)kc * DIM;
+        const float* auxg = P.gemm_lay + (size_t)rb * BAY_AUXS;   // [rows_pad][AUXS]
+        constexpr unsigned int MA = (BAY_TC_AUXF + BAY_TC_NEPI - 1u) / BAY_TC_NEPI;
+        float apre[MA];
+#pragma unroll
+        for (unsigned int m = 0; m < MA; ++m) {
+            const unsigned int j = et + m * BAY_TC_NEPI;
+            apre[m] = (j < BAY_TC_AUXF && ntile > 0u) ? __ldg(auxg + j) : 0.0f;
+        }
+        float sum = 0.0f, cmp = 0.0f;
+        bool ok = true;
+        for (unsigned int t = 0; t < ntile; ++t) {
+            const unsigned int b = t & 1u;
+            float* sa = saux + b * BAY_TC_AUXF;
+#pragma unroll
+            for (unsigned int m = 0; m < MA; ++m) {
+                const unsigned int j = et + m * BAY_TC_NEPI;
+                if (j < BAY_TC_AUXF) sa[j] = apre[m];
+            }
+            // next tile's aux values, in flight during this tile
+#pragma unroll
+            for (unsigned int m = 0; m < MA; ++m) {
+                const unsigned int j = et + m * BAY_TC_NEPI;
+                apre[m] = (j < BAY_TC_AUXF && t + 1u < ntile)
+                    ? __ldg(auxg + (size_t)(t + 1u) * BAY_TC_AUXF + j) : 0.0f;
+            }
+            // one thread waits for the accumulator; the decision is shared so that every
+            // epilogue thread leaves the loop together (the named barrier is not bounded)
+            if (et == 0u) flags[2 + b] = bay_tc_wait(b_tfull + 8u * b, (t >> 1) & 1u, abort, status) ? 1u : 0u;
+            asm volatile("bar.sync 1, %0;" ::"r"(BAY_TC_NEPI) : "memory");
+            if (!flags[2 + b]) {
+                ok = false;
+                break;
+            }
+            bay_tc_wait(b_tfull + 8u * b, (t >> 1) & 1u, nullptr, status);  // already complete
+            bay_tc_fence_after();
+            const unsigned int r0 = rb + t * 128u;
+            const unsigned int nrow = re - r0 < 128u ? re - r0 : 128u;
+            const unsigned int ta = tmem + ((32u * q) << 16) + b * (128u * BAY_TC_G) + g * 128u;
+#pragma unroll 1
+            for (unsigned int j0 = 0; j0 < 128u; j0 += 32u) {
+                float v[32];
+                bay_tmem_ld32(ta + j0, v);
+#pragma unroll
+                for (unsigned int jj = 0; jj < 32u; ++jj) {
+                    const unsigned int j = j0 + jj;
+                    if (j < nrow) {
+                        const float tr = BAY_GEMM_TERM(v[jj], &sa[j * BAY_AUXS], (uint64_t)(r0 + j),
+                                                       xw, prep);
+                        const float yk = __fsub_rn(tr, cmp);
+                        const float s2 = __fadd_rn(sum, yk);
+                        cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
+                        sum = s2;
+                    }
+                }
+            }
+            bay_tc_fence_before();
+            __syncwarp();
+            if (lane == 0u)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(b_tempty + 8u * b) : "memory");
+        }
+        if (ok && wv) {
+            P.s_part[2 * ((size_t)blockIdx.y * nk + kw)] = sum;
+            P.s_part[2 * ((size_t)blockIdx.y * nk + kw) + 1] = -cmp;
+        }
+    }
+    bay_tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        bay_tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(BAY_TC_COLS) : "memory");
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(BAY_TC_THREADS, 1)
+bay_gemm_rows_tc_move(bay_stretch_params P, const __grid_constant__ bay_tmaps T) {
+    bay_gemm_rows_tc_impl<0>(P, T);
+}
+extern "C" __global__ void __launch_bounds__(BAY_TC_THREADS, 1)
+bay_gemm_rows_tc_logfn(bay_stretch_params P, const __grid_constant__ bay_tmaps T) {
+    bay_gemm_rows_tc_impl<2>(P, T);
+}
+#endif  // BAY_GEMM_TC
 
 #elif !BAY_TILED
 // ---------------------------------------------------------------- plain form

@@ -92,17 +92,19 @@ class GB300BayaderaFactory:
         return v.value
 
     def mcmc_factory(self, model, form=None, accept_ref=False, walkers_per_cta=0,
-                     cta_threads=0, streaming=False):
-        """EngineFactory/mcmc-factory: compile the model's fused stretch kernels."""
+                     cta_threads=0, streaming=False, tensor=False):
+        """EngineFactory/mcmc-factory: compile the model's fused stretch kernels.  GEMM form:
+        streaming=True streams the matrix even when it fits in shared memory; tensor=True
+        streams it through the tensor cores (split bf16, fp32 accumulation)."""
         return GB300StretchFactory(self, model, form, accept_ref, walkers_per_cta, cta_threads,
-                                   streaming)
+                                   streaming, tensor)
 
     def acor(self, data_matrix):
         return self.acor_engine.acor(data_matrix)
 
 
 def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0,
-               streaming=False):
+               streaming=False, tensor=False):
     """bay_model_desc of a DeviceDistributionModel; form 'plain' | 'tiled' | None (tiled
     when the model has a tiled form)."""
     if form is None:
@@ -119,7 +121,9 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
     d.logfn = b(model.mcmc_logpdf)
     d.dim = model.dimension
     d.params_size = model.params_size
-    d.flags = (N.MODEL_ACCEPT_REF if accept_ref else 0) | (N.MODEL_GEMM_STREAMING if streaming else 0)
+    d.flags = ((N.MODEL_ACCEPT_REF if accept_ref else 0) |
+               (N.MODEL_GEMM_STREAMING if streaming else 0) |
+               (N.MODEL_GEMM_TENSOR if tensor else 0))
     d.cta_threads = cta_threads
     if form == "tiled":
         t = model.tiled
@@ -154,18 +158,19 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
     return d, keep
 
 
-def check_model(model, form=None, wgs=1024, accept_ref=False):
+def check_model(model, form=None, wgs=1024, accept_ref=False, tensor=False):
     """Compile-check a model's fused kernels with NVRTC (no device needed)."""
-    d, keep = model_desc(model, form, accept_ref)
+    d, keep = model_desc(model, form, accept_ref, tensor=tensor)
     N.call("bay_model_check", C.byref(d), wgs)
 
 
 class GB300StretchFactory:
     def __init__(self, factory, model, form=None, accept_ref=False, walkers_per_cta=0,
-                 cta_threads=0, streaming=False):
+                 cta_threads=0, streaming=False, tensor=False):
         self.factory = factory
         self.model = model
-        d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, streaming)
+        d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, streaming,
+                             tensor)
         h = C.c_void_p()
         N.call("bay_model_compile", factory.ctx, C.byref(d), C.byref(h))
         self.handle = h

@@ -180,6 +180,174 @@ def config():
             "parallelism": "replicas"}
 
 
+# ------------------------------------------------------------------ other workloads
+# (measured with --config; the default line above is the 50-D Gaussian job)
+def _workload(name):
+    """(model factory args, params builder, walkers, burn, run, bins, init, algorithmic
+    FLOP and bytes per walker-step, description) of the other benchmark workloads."""
+    import torch
+    from bayadera_gb300 import models as M
+    if name == "c1":
+        rng = np.random.default_rng(0)
+        data = rng.normal(3.0, 2.0, 10000).astype(np.float32)
+        params = np.concatenate([data, np.array([0.0, 10.0, 0.0, 20.0], np.float32)])
+        return dict(model=M.gaussian_posterior_model(), fast="tiled", params=params,
+                    walkers=4096, burn=512, run=1024, bins=256,
+                    init=lambda s, seed: s.init_position(seed, [2.0, 4.0, 1.0, 3.0]),
+                    flop=3 * 10000, bytes=0,
+                    desc="2-D Gaussian (mu, sigma) posterior, N=10,000 data, prior "
+                         "N(0,10^2) x U(0,20)")
+    if name == "c3":
+        n, F = 1 << 20, 64
+        rng = np.random.default_rng(0)
+        X = rng.standard_normal((n, F), dtype=np.float32)
+        beta = rng.normal(0.0, 1.0 / 8.0, F)
+        eta = X.astype(np.float64) @ beta
+        y = (rng.random(n) < 1.0 / (1.0 + np.exp(-eta))).astype(np.float32)
+        rows = np.empty((n, F + 1), np.float32)
+        rows[:, :F] = X
+        rows[:, F] = y
+        params = torch.from_numpy(np.concatenate([rows.reshape(-1), [5.0]]).astype(np.float32)).cuda()
+        return dict(model=M.logistic_model(F), fast="tensor", forms=("tensor", "gemm", "plain"),
+                    params=params, walkers=8192,
+                    burn=10, run=20, bins=128, plain_burn=1, plain_run=4, rows=n,
+                    row_len=F + 1, hyper_len=1,
+                    init=lambda s, seed: s.init_position_normal(seed, 0.0, 0.05),
+                    flop=2 * F * n, bytes=4 * (F + 1) * n // (8192 // 2),
+                    desc="Bayesian logistic regression, X 1,048,576 x 64 N(0,1), beta* ~ "
+                         "N(0,1/64), prior N(0,5^2 I)")
+    if name == "c5":
+        n, F = 1 << 24, 256
+        rng = np.random.default_rng(0)
+        scale = np.exp(rng.uniform(np.log(0.01), np.log(100.0), F)).astype(np.float32)
+        beta = (rng.normal(0.0, 1.0, F) / (scale * 16.0)).astype(np.float32)
+        params = torch.empty(n * (F + 1) + 3, dtype=torch.float32, device="cuda")
+        rows = params[: n * (F + 1)].view(n, F + 1)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(0)
+        sc = torch.from_numpy(scale).cuda()
+        bt = torch.from_numpy(beta).cuda()
+        for r0 in range(0, n, 1 << 20):
+            r1 = min(n, r0 + (1 << 20))
+            x = torch.randn(r1 - r0, F, device="cuda", generator=g) * sc
+            z = torch.randn(r1 - r0, 5, device="cuda", generator=g)
+            t4 = z[:, 0] / torch.sqrt((z[:, 1:] ** 2).sum(dim=1) / 4.0)
+            rows[r0:r1, :F] = x
+            rows[r0:r1, F] = x @ bt + 0.5 * t4
+        params[n * (F + 1):] = torch.tensor([4.0, 10.0, 1.0], device="cuda")
+        torch.cuda.synchronize()
+        return dict(model=M.robust_t_model(F), fast="tensor", forms=("tensor", "gemm", "plain"),
+                    params=params, walkers=4096,
+                    burn=2, run=10, bins=128, plain_burn=1, plain_run=10, rows=n,
+                    row_len=F + 1, hyper_len=3, plain_rows=1 << 16,
+                    init=lambda s, seed: s.init_position_normal(seed, 0.0, 0.01),
+                    flop=2 * F * n, bytes=4 * (F + 1) * n // (4096 // 2),
+                    desc="robust regression, Student-t(4) residuals, X 16,777,216 x 256 with "
+                         "column scales log-U[0.01,100], D=257")
+    raise ValueError(name)
+
+
+def run_config(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from bayadera_gb300 import _native
+    from bayadera_gb300.engine import GB300BayaderaFactory
+    torch.cuda.set_device(0)
+    wl = _workload(args.config)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    f = GB300BayaderaFactory(device=0, wgs=1024, stream=stream.cuda_stream)
+    W = wl["walkers"]
+    cur = {}
+
+    def job(s, seed):
+        s.init(seed)
+        wl["init"](s, seed + 1)
+        s.burn_in(cur["B"], 2.0)
+        res = s.run_sampler(cur["R"], 2.0)
+        s.mean()
+        s.variance()
+        s.histogram(1, wl["bins"])
+        return res
+
+    out = {}
+    kinds = {"tensor": dict(form="gemm", tensor=True), "gemm": dict(form="gemm"),
+             "tiled": dict(form="tiled"), "plain": dict(form="plain")}
+    forms = wl.get("forms", (wl["fast"], "plain"))
+    for form in forms:
+        sf = f.mcmc_factory(wl["model"], **kinds[form])
+        params = wl["params"]
+        plain_rows = None
+        if form == "plain" and wl.get("plain_rows"):
+            # One thread per walker loops over every row, so the plain form's cost is
+            # linear in the rows; it is measured on the first plain_rows rows (at full size
+            # a job would take many minutes, and C5's 4.3e9-float data exceeds the uint32
+            # data length of the reference's model ABI) and scaled to the full row count.
+            plain_rows = wl["plain_rows"]
+            F1 = wl["row_len"]
+            nh = wl["hyper_len"]
+            params = torch.cat([params[: plain_rows * F1], params[-nh:]])
+        s = sf.create_sampler(11, W, params)
+        steps = args.steps if form == wl["fast"] else 1
+        B = wl["burn"] if form == wl["fast"] else wl.get("plain_burn", wl["burn"])
+        R = wl["run"] if form == wl["fast"] else wl.get("plain_run", wl["run"])
+        cur["B"], cur["R"] = B, R
+        for w in range(args.warmup if form == wl["fast"] else 1):
+            job(s, 100 + w)
+        torch.cuda.synchronize()
+        times = []
+        l0 = _native.launch_count()
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = job(s, 1000 + 17 * k)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        launches = _native.launch_count() - l0
+        # bare-move probe: average time per ensemble step
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        nprobe = max(1, min(B, 8))
+        e0.record(stream)
+        s.burn_in(nprobe, 2.0)
+        e1.record(stream)
+        e1.synchronize()
+        t_step = e0.elapsed_time(e1) / 1e3 / nprobe
+        scale = (plain_rows / wl["rows"]) if plain_rows else 1.0
+        out[form] = {"value": W * (B + R) * steps / sum(times) * scale,
+                     "ms_per_job": 1e3 * sum(times) / steps,
+                     "launches": launches, "ms_per_ensemble_step": 1e3 * t_step,
+                     "fp32_tflops_per_step": W * wl["flop"] * scale / t_step / 1e12,
+                     "acceptance_rate": res["acceptance_rate"]}
+        if plain_rows is not None:
+            out[form]["rows_measured"] = plain_rows
+            out[form]["value_measured"] = out[form]["value"] / scale
+        s.release()
+        sf.release()
+        del params
+    fast = out[wl["fast"]]
+    B, R = wl["burn"], wl["run"]
+    line = {"metric": "walker-steps/s", "value": fast["value"], "unit": "walker-steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": fast["ms_per_job"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": wl["desc"], "walkers": W, "burn_in": B, "run": R,
+                       "form": wl["fast"], "l2": "flushed between timed jobs"},
+            "forms": dict({k: v for k, v in out.items() if k != "plain"},
+                          plain_fp32=out["plain"],
+                          speedup_vs_plain=fast["value"] / out["plain"]["value"]),
+            "algorithmic": {"flop_per_walker_step": wl["flop"],
+                            "bytes_per_walker_step": wl["bytes"]}}
+    print(json.dumps(line))
+    f.release()
+    return 0
+
+
 # ------------------------------------------------------------------ GPU arm
 def main():
     ap = argparse.ArgumentParser()
@@ -188,9 +356,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"],
+                    help="c2 (default): the 50-D Gaussian job; c1, c3, c5: the other "
+                         "benchmark workloads, measured GEMM/tiled form vs plain form")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config != "c2":
+        return run_config(args)
 
     import torch
     rank = int(os.environ.get("RANK", "0"))

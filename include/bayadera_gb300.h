@@ -99,9 +99,11 @@ int bay_launch_count(uint64_t* out);
  * log density = walker(x) + sum_r term(eta_r, aux_r, r, x, prep(x)).  With the matrix
  * resident in shared memory (rows * features up to about 40960 floats) walkers are
  * tiled 64 per CTA in one launch per half-step; larger matrices are streamed (128-walker
- * x 128-row register tiles, per-row-block partial sums, 64-bit row counts; features
- * <= 384).  Covers Gaussian targets (A = precision matrix, term = -eta_r x_r/2) and
- * regression likelihoods (A = design matrix, aux = response). */
+ * x 128-row register tiles, per-row-block partial sums; row index 32-bit, element
+ * offsets 64-bit; features <= 384).  With BAY_MODEL_GEMM_TENSOR the streamed eta runs
+ * on the tensor cores (split bf16, see the flag).  Covers Gaussian targets (A =
+ * precision matrix, term = -eta_r x_r/2) and regression likelihoods (A = design matrix,
+ * aux = response). */
 enum bay_form { BAY_FORM_PLAIN = 0, BAY_FORM_TILED = 1, BAY_FORM_GEMM = 2 };
 enum bay_model_flags {
     /* accept if u <= z^(D-1) exp(beta dlogfn) in fp32, the reference's formula
@@ -110,7 +112,14 @@ enum bay_model_flags {
     /* BAY_FORM_GEMM: always stream the matrix from device memory (three launches per
      * half-step), even when it would fit in shared memory; matrices that do not fit are
      * streamed regardless. */
-    BAY_MODEL_GEMM_STREAMING = 1u << 1
+    BAY_MODEL_GEMM_STREAMING = 1u << 1,
+    /* BAY_FORM_GEMM, streamed, with eta = A b on the tensor cores (tcgen05, bf16 inputs,
+     * fp32 accumulation): A and b are each split into bf16 hi + lo and the three products
+     * hi.hi + hi.lo + lo.hi are accumulated, which leaves a relative error of about 2^-16
+     * per product term (fp32 SIMT: 2^-24).  The sampler keeps a bf16 hi + lo copy of A
+     * (4 bytes per element).  At most 320 features and 2^31 - 256 rows.  No counterpart
+     * in the reference (which evaluates every density per walker in fp32). */
+    BAY_MODEL_GEMM_TENSOR = 1u << 2
 };
 
 typedef struct bay_model_desc {

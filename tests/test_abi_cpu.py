@@ -84,6 +84,18 @@ def test_model_check_benchmark_models(native):
     _check(M.hierarchical_model(4))
 
 
+def test_model_check_tensor_core_form(native):
+    """The tcgen05 rows kernels compile for sm_103a across the feature-chunk counts (1 to
+    5 chunks of 64, one or two walker sub-tiles per CTA); more than 320 features is an
+    argument error, reported before any device work."""
+    from bayadera_gb300 import models as M
+    for F in (7, 64, 130, 256, 320):
+        _check(M.logistic_model(F), "gemm", tensor=True)
+    _check(M.robust_t_model(256), "gemm", tensor=True)
+    with pytest.raises(native.IllegalArgument, match="320 features"):
+        _check(M.logistic_model(321), "gemm", tensor=True)
+
+
 def test_model_check_reports_nvrtc_log(native):
     from bayadera_gb300 import models as M
     bad = M.device_distribution_model("extern \"C\" { inline REAL broken_logpdf( { } }",

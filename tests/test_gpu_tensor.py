@@ -1,0 +1,243 @@
+"""GEMM form on the tensor cores (tcgen05, split bf16, fp32 accumulation) against exact
+and FP64 references.
+
+Error model of the split form: each factor is stored as bf16 hi + lo (residual below
+2^-17 relative), the products hi.hi + hi.lo + lo.hi are summed in fp32 on the tensor
+cores and lo.lo (below 2^-16 relative) is dropped, so each product term x_f b_f carries a
+relative error below 2^-15, plus fp32 accumulation over the F terms.  The tests bound
+|logfn_tc - logfn_exact| by
+
+    sum_r |d term_r / d eta_r| (2^-15 + 4 F 2^-24) sum_f |x_rf b_f|  +  fp32 term rounding,
+
+and, on inputs that bf16 hi + lo represents exactly, check the kernel against the exact
+split-product sum with only the accumulation term left (a dropped hi.lo or lo.hi
+product, a swizzle or layout slip would be off by 2^-9 or more)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LINEAR_SRC = r"""
+#include <stdint.h>
+extern "C" {
+inline REAL tclin_logpdf(const uint32_t data_len, const uint32_t hyper_len,
+                         const REAL* params, const uint32_t dim, const REAL* x) {
+    const uint32_t row = dim + 1, n = data_len / row;
+    REAL res = 0.0f;
+    for (uint32_t i = 0; i < n; ++i) {
+        const REAL* r = params + (uint64_t)i * row;
+        REAL eta = 0.0f;
+        for (uint32_t f = 0; f < dim; ++f) eta = fmaf(r[f], x[f], eta);
+        res += eta * r[dim];
+    }
+    return res;
+}
+inline void tclin_prep(const REAL* h, const uint32_t hl, const uint32_t dim, const REAL* x,
+                       REAL* prep) {}
+inline REAL tclin_term(const REAL eta, const REAL* aux, const uint64_t row, const REAL* x,
+                       const REAL* prep) {
+    return eta * aux[0];
+}
+inline REAL tclin_walker(const uint64_t rows, const REAL* h, const uint32_t hl,
+                         const uint32_t dim, const REAL* x) {
+    return 0.0f;
+}
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def factory():
+    import __graft_entry__
+    __graft_entry__.build()
+    from bayadera_gb300.engine import GB300BayaderaFactory
+    f = GB300BayaderaFactory(device=0, wgs=256)
+    yield f
+    f.release()
+
+
+@pytest.fixture(scope="module")
+def M():
+    from bayadera_gb300 import models
+    return models
+
+
+def linear_model(M, F):
+    g = {"prep": "tclin_prep", "term": "tclin_term", "walker": "tclin_walker",
+         "features": F, "coef": 0, "block": "data", "ld": F + 1, "offset": 0,
+         "aux_col": F, "aux_len": 1}
+    return M.device_distribution_model(LINEAR_SRC, name="tclin", logpdf="tclin_logpdf",
+                                       dimension=F, params_size=1, gemm=g)
+
+
+def bf16_rn(v):
+    """bf16 round-to-nearest-even of float32 values, returned as float64."""
+    u = np.ascontiguousarray(v, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def split(v):
+    v = np.asarray(v, np.float32)
+    hi = bf16_rn(v)
+    lo = bf16_rn((v.astype(np.float64) - hi).astype(np.float32))
+    return hi, lo
+
+
+def sixteen_bit(rng, shape, scale):
+    """float32 values with 16 significant bits (exact as bf16 hi + lo), mixed signs and
+    exponents."""
+    v = (rng.normal(size=shape) * scale * np.exp2(rng.integers(-3, 4, size=shape))).astype(np.float32)
+    return (v.view(np.uint32) & np.uint32(0xFFFFFF00)).view(np.float32)
+
+
+@pytest.mark.parametrize("rows,F,W", [(1000, 64, 512), (300, 7, 200), (777, 130, 260),
+                                      (128, 256, 256), (200, 320, 130), (5000, 64, 1024)])
+def test_tc_eta_exact_split_products(factory, M, rows, F, W):
+    """Linear row term (term = eta_r w_r): with every factor exact in bf16 hi + lo the
+    kernel must equal sum_r w_r sum_f (xh bh + xh bl + xl bh) up to fp32 accumulation.
+    Covers rows and walkers not multiples of the 128 tiles, features padded to 64,
+    one and two walker sub-tiles per CTA and 1..5 feature chunks."""
+    rng = np.random.default_rng(rows + F)
+    X = sixteen_bit(rng, (rows, F), 1.0)
+    w = sixteen_bit(rng, rows, 1.0)
+    pos = sixteen_bit(rng, (W, F), 0.5)
+    params = np.concatenate([np.concatenate([X, w[:, None]], axis=1).reshape(-1),
+                             np.zeros(1, np.float32)]).astype(np.float32)
+    sf = factory.mcmc_factory(linear_model(M, F), form="gemm", tensor=True)
+    s = sf.create_sampler(3, W, params)
+    s.init_position(pos)
+    got = s.logfn().astype(np.float64)
+    xh, xl = split(X)
+    bh, bl = split(pos)
+    eta = bh @ xh.T + bl @ xh.T + bh @ xl.T                      # (W, rows), exact in fp64
+    want = eta @ w.astype(np.float64)
+    mag = (np.abs(pos).astype(np.float64) @ np.abs(X).T.astype(np.float64)) @ np.abs(w).astype(np.float64)
+    tol = 4 * F * 2.0 ** -24 * mag + 2.0 ** -22 * (np.abs(eta) @ np.abs(w).astype(np.float64)) + 1e-30
+    err = np.abs(got - want)
+    assert np.all(err <= tol), (err / tol).max()
+    # and the split-product sum is itself within the 2^-15 model of the exact sum
+    exact = (pos.astype(np.float64) @ X.T.astype(np.float64)) @ w.astype(np.float64)
+    assert np.all(np.abs(want - exact) <= 2.0 ** -15 * mag)
+    s.release()
+    sf.release()
+
+
+def _regression(rng, n, F, kind):
+    X = rng.normal(size=(n, F)).astype(np.float32)
+    beta = rng.normal(scale=1.0 / np.sqrt(F), size=F)
+    eta = X.astype(np.float64) @ beta
+    if kind == "logistic":
+        y = (rng.random(n) < 1.0 / (1.0 + np.exp(-eta))).astype(np.float32)
+        hyper = np.array([5.0], np.float32)
+    else:
+        y = (eta + 0.5 * rng.standard_t(4, n)).astype(np.float32)
+        hyper = np.array([4.0, 10.0, 1.0], np.float32)
+    rows = np.concatenate([X, y[:, None]], axis=1).astype(np.float32)
+    return np.concatenate([rows.reshape(-1), hyper]), rows.size, X, hyper
+
+
+def _bound(kind, X, hyper, pos, F, lf64):
+    """Per-walker bound on |logfn_tc - logfn_fp64| (module docstring)."""
+    b = pos[:, :F].astype(np.float64)
+    mag_rows = np.abs(b) @ np.abs(X.astype(np.float64)).T       # (W, rows)
+    if kind == "logistic":
+        sens = np.ones(len(pos))
+    else:
+        nu = float(hyper[0])
+        sens = (nu + 1.0) / (2.0 * np.sqrt(nu)) * np.exp(-pos[:, F].astype(np.float64))
+    eta_err = (2.0 ** -15 + 4 * F * 2.0 ** -24) * mag_rows.sum(axis=1)
+    rows = X.shape[0]
+    return sens * eta_err + 1e-6 * rows + 1e-5 * np.abs(lf64)
+
+
+@pytest.mark.parametrize("kind,rows,F,W", [("logistic", 3000, 64, 512),
+                                           ("logistic", 1000, 7, 1000),
+                                           ("robust_t", 700, 255, 300),
+                                           ("robust_t", 2000, 64, 258)])
+def test_tc_logfn_within_bound_of_fp64(factory, M, oracle, kind, rows, F, W):
+    """Model log densities (logistic softplus terms, Student-t terms) of the initial and of
+    moved walkers against the oracle's FP64 density, within the split-bf16 bound."""
+    rng = np.random.default_rng(11)
+    params, dl, X, hyper = _regression(rng, rows, F, kind)
+    model = M.logistic_model(F) if kind == "logistic" else M.robust_t_model(F)
+    D = model.dimension
+    sf = factory.mcmc_factory(model, form="gemm", tensor=True)
+    s = sf.create_sampler(5, W, params)
+    s.init_position_normal(6, 0.0, 0.3)
+    for phase in range(2):
+        pos = s.positions().T.astype(np.float64)
+        lf = s.logfn().astype(np.float64)
+        idx = np.arange(0, W, max(1, W // 64))
+        want = np.array([oracle.logfn64(kind, params, dl, D, pos[i]) for i in idx])
+        tol = _bound(kind, X, hyper, pos[idx].astype(np.float32), F, want)
+        err = np.abs(lf[idx] - want)
+        assert np.all(err <= tol), (phase, (err / tol).max())
+        s.burn_in(2, 2.0)
+    s.release()
+    sf.release()
+
+
+def test_tc_matches_simt_streaming(factory, M):
+    """Same seeds, tensor-core and fp32 SIMT streamed forms: log densities at the same
+    positions agree within the split-bf16 bound, and the first moves make the same
+    accept decisions except for marginal ones."""
+    rng = np.random.default_rng(21)
+    F, rows, W = 64, 20000, 2048
+    params, dl, X, hyper = _regression(rng, rows, F, "logistic")
+    out = []
+    for tensor in (False, True):
+        sf = factory.mcmc_factory(M.logistic_model(F), form="gemm", streaming=True,
+                                  tensor=tensor)
+        s = sf.create_sampler(7, W, params)
+        s.init_position_normal(8, 0.0, 0.05)
+        lf0 = s.logfn().copy()
+        s.burn_in(3, 2.0)
+        out.append((lf0, s.positions().copy()))
+        s.release()
+        sf.release()
+    d = np.abs(out[0][0].astype(np.float64) - out[1][0])
+    assert np.median(d) < 0.05, np.median(d)
+    walkers_differ = np.any(out[0][1] != out[1][1], axis=0).sum()
+    assert walkers_differ <= W // 50, walkers_differ
+
+
+def test_tc_run_sampler_statistics(factory, M):
+    """Accu path on the tensor cores: acceptance count, per-step means (last = mean of the
+    walkers), and posterior means within 4 MC standard errors of the fp32 SIMT form (same
+    seeds, so the two chains share their Philox draws until a marginal accept decision
+    differs)."""
+    rng = np.random.default_rng(4)
+    F = 8
+    params, dl, X, hyper = _regression(rng, 5000, F, "robust_t")
+    res = {}
+    for tensor in (False, True):
+        sf = factory.mcmc_factory(M.robust_t_model(F), form="gemm", streaming=True,
+                                  tensor=tensor)
+        s = sf.create_sampler(8, 2048, params)
+        s.init_position_normal(9, 0.0, 0.2)
+        s.burn_in(1000, 2.0)
+        r = s.run_sampler(512, 2.0, return_means=True)
+        assert 0.1 < r["acceptance_rate"] < 0.9
+        np.testing.assert_allclose(r["means"][:, -1], s.mean(), rtol=1e-5, atol=1e-6)
+        m = r["means"].mean(axis=1)
+        ac = r["autocorrelation"]
+        # MC s.e. of the run mean, sqrt(var tau / (W n)); acor's tau where it is a usable
+        # estimate, else a conservative 100 (a short run can give acor a negative D)
+        tau = np.asarray(ac.tau, np.float64) if ac is not None else np.full(F + 1, np.nan)
+        tau = np.where(np.isfinite(tau) & (tau > 1.0), tau, 100.0)
+        se = np.sqrt(s.variance() * tau / (2048 * 512))
+        res[tensor] = (m, se, r["acceptance_rate"])
+        s.release()
+        sf.release()
+    (m0, se0, a0), (m1, se1, a1) = res[False], res[True]
+    se = np.sqrt(se0 ** 2 + se1 ** 2)
+    assert np.all(np.abs(m0 - m1) <= 4 * se + 1e-6), np.abs(m0 - m1) / se
+    n = 2048 * 512
+    assert abs(a0 - a1) <= 3 * np.sqrt(2 * a0 * (1 - a0) / n) + 0.01
+
+
+def test_tc_rejects_too_many_features(factory, M):
+    from bayadera_gb300._native import BayaderaError
+    with pytest.raises(BayaderaError, match="320 features"):
+        factory.mcmc_factory(M.logistic_model(384), form="gemm", tensor=True)
