@@ -399,7 +399,7 @@ struct bay_sampler {
             void* args[] = {&p, &tc_maps};
             cu_check(g_cu.LaunchKernel((CUfunction)model->k_gt[mode == 2 ? 1 : 0],
                                        (unsigned)((nk + per - 1) / per), s_nsb, 1,
-                                       64 + 128 * model->tc_g, 1, 1, (unsigned)model->tc_smem,
+                                       576, 1, 1, (unsigned)model->tc_smem,
                                        (CUstream)st, args, nullptr),
                      "cuLaunchKernel(gemm rows, tensor cores)");
         } else {

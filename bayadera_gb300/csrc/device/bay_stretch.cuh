@@ -731,9 +731,9 @@ extern "C" __global__ void __launch_bounds__(256) bay_gemm_accept_logfn(bay_stre
 // both operands K-major in shared memory with the 128-byte swizzle TMA writes.
 // CTA roles: warp 0 -- TMA producer (the CTA's walker operand once, then each 128-row
 // tile in 64-feature chunks through a ring of BAY_TC_STAGES stages); warp 1 -- TMEM
-// allocation and the MMA issue (one thread); warps 2 .. 2 + 4 BAY_TC_G - 1 -- epilogue,
-// one thread per walker: tcgen05.ld of its TMEM lane, the model's row term, a Kahan
-// sum over the super-block's rows.  Two accumulator buffers in TMEM let the MMAs of
+// allocation and the MMA issue (one thread); warps 2 .. 17 -- epilogue, a thread per
+// walker and share of a tile's rows: tcgen05.ld of its TMEM lane, the model's row terms,
+// a compensated sum over the super-block's rows.  Two accumulator buffers in TMEM let the MMAs of
 // tile t + 1 run under the epilogue of tile t.  Every wait is bounded in time; a wait
 // that gives up sets the sampler's status word and the CTA's abort flag, and the CTA
 // drains its own copies and MMAs, frees its TMEM and exits.
@@ -749,8 +749,8 @@ extern "C" __global__ void __launch_bounds__(256) bay_gemm_accept_logfn(bay_stre
 #define BAY_TC_WBYTES ((unsigned int)BAY_TC_G * BAY_TC_KC * 2u * BAY_TC_TILE)
 #define BAY_TC_SBYTES (2u * BAY_TC_TILE)        // a stage: rows hi + lo chunk
 #define BAY_TC_AUXF (128u * BAY_AUXS)
-#define BAY_TC_NEPI (128u * BAY_TC_G)           // epilogue threads
-#define BAY_TC_THREADS (64 + 128 * BAY_TC_G)
+#define BAY_TC_NEPI 512u                        // epilogue threads (16 warps)
+#define BAY_TC_THREADS 576
 #define BAY_TC_COLS (BAY_TC_G == 2 ? 512u : 256u)
 #define BAY_TC_WAIT_NS 2000000000ull
 // instruction descriptor: fp32 accumulator, bf16 A and B, both K-major, N = 128, M = 128
@@ -837,23 +837,19 @@ __device__ __forceinline__ void bay_tc_fence_before() {
 __device__ __forceinline__ void bay_tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// 32 consecutive TMEM columns of this thread's lane
-__device__ __forceinline__ void bay_tmem_ld32(unsigned int ta, float (&v)[32]) {
-    unsigned int r[32];
+// 16 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void bay_tmem_ld16(unsigned int ta, float (&v)[16]) {
+    unsigned int r[16];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-        "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
-        "%28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-          "=r"(r[31])
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(ta));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 template <int MODE>  // 0: move (K walkers of the moving half), 2: log density of all W
@@ -893,7 +889,7 @@ __device__ __forceinline__ void bay_gemm_rows_tc_impl(const bay_stretch_params& 
         }
         for (unsigned int b = 0; b < 2; ++b) {
             bay_mbar_init(b_tfull + 8u * b, 1u);
-            bay_mbar_init(b_tempty + 8u * b, 4u * BAY_TC_G);
+            bay_mbar_init(b_tempty + 8u * b, BAY_TC_NEPI / 32u);
         }
         bay_mbar_init(b_wop, 1u);
         bay_mbar_init(b_drain, 1u);
@@ -986,10 +982,20 @@ __device__ __forceinline__ void bay_gemm_rows_tc_impl(const bay_stretch_params& 
             bay_tc_wait(b_drain, 0u, nullptr, status);
         }
     } else {
-        // ---- epilogue: one thread per walker
+        // ---- epilogue, 16 warps in 4 groups of 4 (a group covers the 128 TMEM lanes).
+        //      G = 2: group e takes walker sub-tile e / 2, rows 64 (e % 2) .. + 63 of a tile;
+        //      G = 1: group e takes sub-tile 0, rows 32 e .. 32 e + 31.  A thread owns one
+        //      walker (its TMEM lane): per 16-row batch it evaluates the row terms, sums them
+        //      pairwise and adds the batch sum to a Kahan-compensated running sum; the
+        //      groups' partial sums of a walker are combined at the end in group order.
+        constexpr unsigned int GPS = 4u / BAY_TC_G;        // groups per walker sub-tile
+        constexpr unsigned int NCOL = 128u / GPS;          // rows of a tile per group
         const unsigned int et = threadIdx.x - 64u;
-        const unsigned int g = (warp - 2u) >> 2, q = warp & 3u;
-        const unsigned int kw = k0 + g * 128u + 32u * q + lane;
+        const unsigned int grp = (warp - 2u) >> 2, q = warp & 3u;
+        const unsigned int g = grp / GPS;
+        const unsigned int c0 = NCOL * (grp % GPS);
+        const unsigned int wl = 32u * q + lane;
+        const unsigned int kw = k0 + g * 128u + wl;
         const bool wv = kw < nk;
         const unsigned int kc = wv ? kw : nk - 1u;
         float prep[BAY_PREP_LEN];
@@ -1033,32 +1039,69 @@ __device__ __forceinline__ void bay_gemm_rows_tc_impl(const bay_stretch_params& 
             bay_tc_fence_after();
             const unsigned int r0 = rb + t * 128u;
             const unsigned int nrow = re - r0 < 128u ? re - r0 : 128u;
-            const unsigned int ta = tmem + ((32u * q) << 16) + b * (128u * BAY_TC_G) + g * 128u;
+            const unsigned int ta = tmem + ((32u * q) << 16) + b * (128u * BAY_TC_G) + g * 128u + c0;
 #pragma unroll 1
-            for (unsigned int j0 = 0; j0 < 128u; j0 += 32u) {
-                float v[32];
-                bay_tmem_ld32(ta + j0, v);
+            for (unsigned int j0 = 0; j0 < NCOL; j0 += 16u) {
+                float v[16];
+                bay_tmem_ld16(ta + j0, v);
+                const unsigned int jb = c0 + j0;   // the batch's first row within the tile
+                // the batch's aux values: 16 * AUXS consecutive floats, 16-byte aligned
+                float av[16 * BAY_AUXS];
 #pragma unroll
-                for (unsigned int jj = 0; jj < 32u; ++jj) {
-                    const unsigned int j = j0 + jj;
-                    if (j < nrow) {
-                        const float tr = BAY_GEMM_TERM(v[jj], &sa[j * BAY_AUXS], (uint64_t)(r0 + j),
-                                                       xw, prep);
-                        const float yk = __fsub_rn(tr, cmp);
-                        const float s2 = __fadd_rn(sum, yk);
-                        cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
-                        sum = s2;
-                    }
+                for (unsigned int i = 0; i < 4u * BAY_AUXS; ++i) {
+                    const float4 a4 = reinterpret_cast<const float4*>(sa + jb * BAY_AUXS)[i];
+                    av[4 * i] = a4.x;
+                    av[4 * i + 1] = a4.y;
+                    av[4 * i + 2] = a4.z;
+                    av[4 * i + 3] = a4.w;
                 }
+                if (jb + 16u <= nrow) {
+#pragma unroll
+                    for (unsigned int jj = 0; jj < 16u; ++jj)
+                        v[jj] = BAY_GEMM_TERM(v[jj], &av[jj * BAY_AUXS], (uint64_t)(r0 + jb + jj),
+                                              xw, prep);
+                } else {
+#pragma unroll
+                    for (unsigned int jj = 0; jj < 16u; ++jj)
+                        v[jj] = jb + jj < nrow
+                            ? BAY_GEMM_TERM(v[jj], &av[jj * BAY_AUXS], (uint64_t)(r0 + jb + jj), xw, prep)
+                            : 0.0f;
+                }
+#pragma unroll
+                for (unsigned int w = 8u; w >= 1u; w >>= 1)
+#pragma unroll
+                    for (unsigned int i = 0; i < w; ++i) v[i] = __fadd_rn(v[i], v[i + w]);
+                const float yk = __fsub_rn(v[0], cmp);
+                const float s2 = __fadd_rn(sum, yk);
+                cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
+                sum = s2;
             }
             bay_tc_fence_before();
             __syncwarp();
             if (lane == 0u)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(b_tempty + 8u * b) : "memory");
         }
-        if (ok && wv) {
-            P.s_part[2 * ((size_t)blockIdx.y * nk + kw)] = sum;
-            P.s_part[2 * ((size_t)blockIdx.y * nk + kw) + 1] = -cmp;
+        // the groups' partial sums of each walker, combined as compensated pairs in group
+        // order; stage 0 is free once the last tile's MMAs (hence its copies) are complete
+        float* xchg = (float*)(sm + BAY_TC_WBYTES);        // [4 groups][128 lanes][hi, lo]
+        if (ok) {
+            xchg[2 * (grp * 128u + wl)] = sum;
+            xchg[2 * (grp * 128u + wl) + 1] = -cmp;
+        }
+        asm volatile("bar.sync 1, %0;" ::"r"(BAY_TC_NEPI) : "memory");
+        if (ok && grp % GPS == 0u && wv) {
+            bay_cf a;
+            a.hi = sum;
+            a.lo = -cmp;
+#pragma unroll
+            for (unsigned int o = 1; o < GPS; ++o) {
+                bay_cf p;
+                p.hi = xchg[2 * ((grp + o) * 128u + wl)];
+                p.lo = xchg[2 * ((grp + o) * 128u + wl) + 1];
+                a = bay_cadd(a, p);
+            }
+            P.s_part[2 * ((size_t)blockIdx.y * nk + kw)] = a.hi;
+            P.s_part[2 * ((size_t)blockIdx.y * nk + kw) + 1] = a.lo;
         }
     }
     bay_tc_fence_before();

@@ -15,22 +15,24 @@ inline REAL robust_t_logpdf(const uint32_t data_len, const uint32_t hyper_len,
         REAL eta = 0.0f;
         for (uint32_t f = 0; f < F; ++f) eta = fmaf(r[f], x[f], eta);
         const REAL z = (r[F] - eta) * inv_s;
-        res += -0.5f * (nu + 1.0f) * log1pf(z * z / nu);
+        res += -0.5f * (nu + 1.0f) * logf(1.0f + z * z / nu);
     }
     REAL pb = 0.0f;
     for (uint32_t f = 0; f < F; ++f) pb = fmaf(x[f], x[f], pb);
     return res - (REAL)n * ls - pb / (2.0f * h[1] * h[1]) - ls * ls / (2.0f * h[2] * h[2]);
 }
-// GEMM form: A = the data rows' features, aux = y; prep = (1/sigma, nu).
+// GEMM form: A = the data rows' features, aux = y; prep = (1/sigma, 1/(nu sigma^2),
+// -(nu+1)/2), so that a row term is two multiply-adds and one log.
 inline void robust_t_prep(const REAL* h, const uint32_t hyper_len, const uint32_t dim,
                           const REAL* x, REAL* prep) {
     prep[0] = expf(-x[dim - 1]);
-    prep[1] = h[0];
+    prep[1] = prep[0] * prep[0] / h[0];
+    prep[2] = -0.5f * (h[0] + 1.0f);
 }
 inline REAL robust_t_term(const REAL eta, const REAL* aux, const uint64_t row, const REAL* x,
                           const REAL* prep) {
-    const REAL z = (aux[0] - eta) * prep[0];
-    return -0.5f * (prep[1] + 1.0f) * log1pf(z * z / prep[1]);
+    const REAL r = aux[0] - eta;
+    return prep[2] * logf(fmaf(r * r, prep[1], 1.0f));
 }
 inline REAL robust_t_walker(const uint64_t rows, const REAL* h, const uint32_t hyper_len,
                             const uint32_t dim, const REAL* x) {

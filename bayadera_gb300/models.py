@@ -225,7 +225,7 @@ def logistic_model(features):
 def robust_t_model(features):
     """Student-t regression on data rows (x_1..x_F, y), x = (beta, log sigma)."""
     g = {"prep": "robust_t_prep", "term": "robust_t_term", "walker": "robust_t_walker",
-         "prep_len": 2, "features": features, "coef": 0, "block": "data", "ld": features + 1,
+         "prep_len": 3, "features": features, "coef": 0, "block": "data", "ld": features + 1,
          "offset": 0, "aux_col": features, "aux_len": 1}
     return device_distribution_model(get_source("robust_t"), name="robust_t",
                                      dimension=features + 1, params_size=3,

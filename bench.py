@@ -275,6 +275,8 @@ def run_config(args):
     kinds = {"tensor": dict(form="gemm", tensor=True), "gemm": dict(form="gemm"),
              "tiled": dict(form="tiled"), "plain": dict(form="plain")}
     forms = wl.get("forms", (wl["fast"], "plain"))
+    if args.forms:
+        forms = tuple(args.forms.split(","))
     for form in forms:
         sf = f.mcmc_factory(wl["model"], **kinds[form])
         params = wl["params"]
@@ -330,6 +332,10 @@ def run_config(args):
         s.release()
         sf.release()
         del params
+    if wl["fast"] not in out or "plain" not in out:
+        print(json.dumps({"config": wl["desc"], "forms": out}))
+        f.release()
+        return 0
     fast = out[wl["fast"]]
     B, R = wl["burn"], wl["run"]
     line = {"metric": "walker-steps/s", "value": fast["value"], "unit": "walker-steps/s",
@@ -359,6 +365,9 @@ def main():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"],
                     help="c2 (default): the 50-D Gaussian job; c1, c3, c5: the other "
                          "benchmark workloads, measured GEMM/tiled form vs plain form")
+    ap.add_argument("--forms", default="",
+                    help="with --config: comma-separated subset of the forms to run "
+                         "(tensor, gemm, tiled, plain), e.g. for a profile of one form")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -298,7 +298,7 @@ static double m_mvn64(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, co
 
 /* Bayesian logistic regression.  data: N rows of (x_1..x_F, y), F = dim;
  * hyper: {prior_sd}.  loglik = sum y*eta - softplus(eta); prior N(0, sd^2 I). */
-static float softplus32(float e) { return fmaxf(e, 0.0f) + log1pf(expf(-fabsf(e))); }
+static float softplus32(float e) { return fmaxf(e, 0.0f) + logf(1.0f + expf(-fabsf(e))); }
 static float m_logistic32(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, const float* x) {
     (void)pl;
     const uint32_t row = dim + 1, N = dl / row;
@@ -344,7 +344,7 @@ static float m_robust32(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, 
         float eta = 0.0f;
         for (uint32_t f = 0; f < F; f++) eta = fmaf(r[f], x[f], eta);
         const float z = (r[F] - eta) * inv_s;
-        res += -0.5f * (nu + 1.0f) * log1pf(z * z / nu);
+        res += -0.5f * (nu + 1.0f) * logf(1.0f + z * z / nu);
     }
     float pb = 0.0f;
     for (uint32_t f = 0; f < F; f++) pb = fmaf(x[f], x[f], pb);
