@@ -19,6 +19,7 @@ BAY_ERR_DEVICE = 6
 FORM_PLAIN = 0
 FORM_TILED = 1
 FORM_GEMM = 2
+FORM_BATCH = 3
 MODEL_ACCEPT_REF = 1
 MODEL_GEMM_STREAMING = 2
 MODEL_GEMM_TENSOR = 4
@@ -62,6 +63,11 @@ class ModelDesc(C.Structure):
 class SamplerInfo(C.Structure):
     _fields_ = [("walkers", C.c_uint64), ("dim", C.c_uint32), ("wgs", C.c_uint32),
                 ("iteration_counter", C.c_uint64), ("data_len", C.c_uint64)]
+
+
+class BatchMember(C.Structure):
+    _fields_ = [("dim", C.c_uint32), ("seed", C.c_uint32), ("walkers", C.c_uint64),
+                ("params", C.c_void_p), ("n_params", C.c_uint64), ("rows", C.c_uint64)]
 
 
 class RunResult(C.Structure):
@@ -110,6 +116,16 @@ _SIGNATURES = {
     "bay_state_import": (C.c_int, [P, P, P, P]),
     "bay_logfn_values": (C.c_int, [P, P]),
     "bay_sampler_set_graphs": (C.c_int, [P, C.c_int]),
+    "bay_batch_create": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32, C.POINTER(P)]),
+    "bay_batch_release": (C.c_int, [P]),
+    "bay_batch_init_position_normal": (C.c_int, [P, P, C.c_float, C.c_float]),
+    "bay_batch_init_position_host": (C.c_int, [P, P]),
+    "bay_batch_burn_in": (C.c_int, [P, C.c_uint64, C.c_float]),
+    "bay_batch_run_sampler": (C.c_int, [P, C.c_uint64, C.c_float, P, P]),
+    "bay_batch_state_export": (C.c_int, [P, P, P]),
+    "bay_batch_info": (C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                 C.POINTER(C.c_uint64)]),
+    "bay_batch_set_graphs": (C.c_int, [P, C.c_int]),
 }
 
 _lib = None

@@ -19,9 +19,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 
 EMBED = [("bay_embedded_rng", "device/bay_rng.cuh"),
-         ("bay_embedded_stretch", "device/bay_stretch.cuh")]
+         ("bay_embedded_stretch", "device/bay_stretch.cuh"),
+         ("bay_embedded_batch", "device/bay_batch.cuh")]
 SOURCES = ["bay_api.cpp", "bay_kernels.cu"]
-HEADERS = ["bay_kernels.cuh", os.path.join("..", "..", "include", "bayadera_gb300.h")]
+HEADERS = ["bay_kernels.cuh", "bay_batch_api.inc",
+           os.path.join("..", "..", "include", "bayadera_gb300.h")]
 
 
 def cuda_home():

@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -182,6 +183,9 @@ struct bay_model {
     CUkernel k_gt[2] = {nullptr, nullptr};
     uint32_t tc_g = 0, tc_stages = 0;
     size_t tc_smem = 0;
+    // batch form: propose / accept in k_gp / k_ga, rows in k_gr, per-step means here
+    CUkernel k_bmeans = nullptr;
+    uint32_t row_len = 0;
 };
 
 namespace {
@@ -749,6 +753,18 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
             opts.push_back("-DBAY_TC_STAGES=" + std::to_string(g.tc_stages));
         }
         wpc = 64;
+    } else if (d->form == BAY_FORM_BATCH) {
+        if (!valid_ident(d->tile_prep) || !valid_ident(d->tile_term) ||
+            !valid_ident(d->tile_walker))
+            fail(BAY_ERR_ARG, "batch form needs tile_prep, tile_term and tile_walker names");
+        if (d->row_len == 0 || d->row_len > 64) fail(BAY_ERR_ARG, "row_len must be in [1, 64]");
+        const uint32_t pl = d->prep_len ? d->prep_len : 1u;
+        if (pl > 64) fail(BAY_ERR_ARG, "prep_len must be <= 64");
+        opts.push_back("-DBAY_ROW_LEN=" + std::to_string(d->row_len));
+        opts.push_back("-DBAY_PREP_LEN=" + std::to_string(pl));
+        opts.push_back(std::string("-DBAY_TILE_PREP=") + d->tile_prep);
+        opts.push_back(std::string("-DBAY_TILE_TERM=") + d->tile_term);
+        opts.push_back(std::string("-DBAY_TILE_WALKER=") + d->tile_walker);
     } else {
         fail(BAY_ERR_ARG, "unknown model form");
     }
@@ -757,8 +773,13 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
     src += bay_embedded_rng;
     src += "\n#line 1 \"model\"\n";
     src += d->source;
-    src += "\n#line 1 \"bay_stretch.cuh\"\n";
-    src += bay_embedded_stretch;
+    if (d->form == BAY_FORM_BATCH) {
+        src += "\n#line 1 \"bay_batch.cuh\"\n";
+        src += bay_embedded_batch;
+    } else {
+        src += "\n#line 1 \"bay_stretch.cuh\"\n";
+        src += bay_embedded_stretch;
+    }
     g.cta = cta;
     g.wpc = wpc;
     return g;
@@ -807,9 +828,25 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
             cu_check(g_cu.LibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr,
                                        nullptr, 0),
                      "cuLibraryLoadData");
-            cu_check(g_cu.LibraryGetKernel(&m->k_bare, m->lib, "bay_stretch_bare"), "GetKernel(bare)");
-            cu_check(g_cu.LibraryGetKernel(&m->k_accu, m->lib, "bay_stretch_accu"), "GetKernel(accu)");
-            cu_check(g_cu.LibraryGetKernel(&m->k_logfn, m->lib, "bay_logfn_all"), "GetKernel(logfn)");
+            if (d->form == BAY_FORM_BATCH) {
+                const char* bp[3] = {"bay_batch_propose_bare", "bay_batch_propose_accu",
+                                     "bay_batch_propose_logfn"};
+                const char* ba[3] = {"bay_batch_accept_bare", "bay_batch_accept_accu",
+                                     "bay_batch_accept_logfn"};
+                for (int i = 0; i < 3; ++i) {
+                    cu_check(g_cu.LibraryGetKernel(&m->k_gp[i], m->lib, bp[i]), "GetKernel(propose)");
+                    cu_check(g_cu.LibraryGetKernel(&m->k_ga[i], m->lib, ba[i]), "GetKernel(accept)");
+                }
+                cu_check(g_cu.LibraryGetKernel(&m->k_gr[0], m->lib, "bay_batch_rows_move"), "GetKernel(rows)");
+                cu_check(g_cu.LibraryGetKernel(&m->k_gr[1], m->lib, "bay_batch_rows_logfn"), "GetKernel(rows)");
+                cu_check(g_cu.LibraryGetKernel(&m->k_bmeans, m->lib, "bay_batch_means"), "GetKernel(means)");
+                m->row_len = d->row_len;
+                m->prep_len = d->prep_len ? d->prep_len : 1u;
+            } else {
+                cu_check(g_cu.LibraryGetKernel(&m->k_bare, m->lib, "bay_stretch_bare"), "GetKernel(bare)");
+                cu_check(g_cu.LibraryGetKernel(&m->k_accu, m->lib, "bay_stretch_accu"), "GetKernel(accu)");
+                cu_check(g_cu.LibraryGetKernel(&m->k_logfn, m->lib, "bay_logfn_all"), "GetKernel(logfn)");
+            }
             if (d->form == BAY_FORM_GEMM) {
                 const char* gp[3] = {"bay_gemm_propose_bare", "bay_gemm_propose_accu",
                                      "bay_gemm_propose_logfn"};
@@ -1571,3 +1608,5 @@ int bay_logfn_values(bay_sampler* s, float* out) {
 }
 
 }  // extern "C"
+
+#include "bay_batch_api.inc"

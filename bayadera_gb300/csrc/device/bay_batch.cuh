@@ -1,0 +1,328 @@
+// bay_batch.cuh -- batched stretch moves: many independent models of one model family
+// (one NVRTC compile), each member with its own dimension, walkers, data, hyperparameters
+// and seed, advanced together.  Compiled by NVRTC per model family with bay_rng.cuh and
+// the model source in front.
+//
+// A half-step of every member is three launches over work lists the host builds once:
+//   propose: CTA = (member, 256-walker tile): Philox draw with the member's seed and the
+//            single-sampler counter {k, step, stream, 0xbeeff00d}, stretch factor, partner
+//            from the member's other half, the proposal y -> scratch (coalesced over the
+//            tile's contiguous block), per-walker prep and the terms outside the row sum;
+//   rows:    CTA = (member, tile of wpc walkers, chunk of rows): the model's row terms of
+//            the chunk, 256 / wpc threads per walker, Kahan sums combined in lane order ->
+//            a compensated partial per (walker, chunk).  wpc and the chunk size are chosen
+//            per member so that every item carries about the same work, which balances
+//            members whose data differ by orders of magnitude;
+//   accept:  CTA = (member, 256-walker tile): partials summed in chunk order, FP64 log
+//            accept, write-back; accu: accepted count per member, per-CTA per-dim sums.
+// Counter and key words per member are those of a single sampler with the member's seed,
+// so a member's trajectory is the trajectory that sampler would take (up to the order of
+// the log-density sums).
+//
+// Model ABI (row form, runtime dimension):
+//   void BAY_TILE_PREP(const REAL* hyper, uint32_t hyper_len, uint32_t dim, const REAL* x,
+//                      REAL* prep)                          BAY_PREP_LEN values per walker
+//   REAL BAY_TILE_TERM(const REAL* row, const REAL* x, const REAL* prep)    one data row
+//   REAL BAY_TILE_WALKER(uint64_t n_rows, const REAL* hyper, uint32_t hyper_len,
+//                        uint32_t dim, const REAL* x)       every term not summed over rows
+// log density = walker(x) + sum over the member's rows of term(row, x, prep(x)); a member's
+// params are rows (BAY_ROW_LEN floats each) followed by hyper_len hyperparameters.
+
+#ifndef BAY_PREP_LEN
+#define BAY_PREP_LEN 1
+#endif
+
+struct bay_ctl {
+    unsigned int step[2];
+    unsigned int seed[2];
+    float a;
+    float beta;
+    unsigned int ticket[2];
+    unsigned long long accepted;
+    unsigned int status;
+    unsigned int pad;
+};
+
+// per member (host-built, read-only on the device)
+struct bay_bmember {
+    unsigned long long xs;        // float offset of the member's positions, W x dim
+    unsigned long long params;    // float offset of its rows || hyperparameters
+    unsigned long long rows;      // data rows
+    unsigned long long part;      // float offset of its partials, W x chunks x 2
+    unsigned long long dsum;      // float offset of its per-CTA dim sums, tiles x dim
+    unsigned long long means;     // float offset of its per-step means, cap x dim
+    unsigned int dim, W, K, hyper_len;
+    unsigned int walker0;         // first walker of the member in the per-walker arrays
+    unsigned int chunks, chunk_rows;
+    unsigned int tile0;           // first move tile (accept CTA) of the member
+    unsigned int ntiles;          // move tiles of the member
+    unsigned int pad[3];
+};
+struct bay_bitem { unsigned int m, k0, c, wpc; };   // rows work item
+struct bay_btile { unsigned int m, k0; };           // propose / accept CTA
+
+struct bay_batch_params {
+    const bay_bmember* mem;
+    const bay_bitem* items;
+    const bay_btile* tiles;
+    const unsigned int* seeds;    // [member][2]: bare, accu
+    const float* params;
+    float* xs;
+    float* y;                     // proposals, laid out like xs
+    float* logfn;                 // [walker0 + w]
+    float* prep;                  // [walker0 + k][BAY_PREP_LEN]
+    float* wterm;                 // [walker0 + k]
+    float* zu;                    // [walker0 + k][2]
+    float* part;
+    unsigned long long* accepted; // [member]
+    float* dsum;                  // [step_off * 2 + half][dsum_stride]
+    float* means;
+    bay_ctl* ctl;
+    unsigned long long dsum_stride;
+    unsigned int half, step_off, means_cap, n_members;
+};
+
+// log u <= (dim - 1) log z + beta (ly - lx) in FP64; a non-finite proposal is rejected
+__device__ __forceinline__ bool bay_batch_accept(float u2, float z, float ly, float lx,
+                                                 float beta, unsigned int dim) {
+    if (!isfinite(ly)) return false;
+    const double lq = (double)(dim - 1) * (double)__logf(z)
+        + (double)beta * ((double)ly - (double)lx);
+    return (double)__logf(u2) <= lq;
+}
+
+struct bay_bcf {
+    float hi, lo;
+};
+__device__ __forceinline__ bay_bcf bay_bcadd(bay_bcf a, bay_bcf b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+    const float hi = __fadd_rn(s, lo);
+    bay_bcf r;
+    r.hi = hi;
+    r.lo = __fsub_rn(lo, __fsub_rn(hi, s));
+    return r;
+}
+
+__device__ __forceinline__ float bay_stretch_z(float a, float u1) {
+    const float inv_a = __fdiv_rn(1.0f, a);
+    const float c1 = __fadd_rn(__fsub_rn(a, 2.0f), inv_a);
+    const float c2 = __fmul_rn(2.0f, __fsub_rn(1.0f, inv_a));
+    return __fadd_rn(__fmaf_rn(__fmul_rn(c1, u1), u1, __fmul_rn(c2, u1)), inv_a);
+}
+__device__ __forceinline__ unsigned int bay_partner(float u0, unsigned int K) {
+    unsigned int j = __float2uint_rz(__fmul_rn(u0, (float)K));
+    return j < K ? j : K - 1;
+}
+
+template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions (all W)
+__device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P) {
+    __shared__ float sZ[256];
+    __shared__ unsigned int sJ[256];
+    const bay_btile T = P.tiles[blockIdx.x];
+    const bay_bmember& M = P.mem[T.m];
+    const unsigned int nk = MODE == 2 ? M.W : M.K;
+    const unsigned int dim = M.dim;
+    const unsigned int tid = threadIdx.x;
+    const unsigned int k = T.k0 + tid;
+    const unsigned int nt = nk - T.k0 < 256u ? nk - T.k0 : 256u;   // walkers of the tile
+    const unsigned int kind = MODE == 1 ? 1u : 0u;
+    if (MODE != 2 && tid < nt) {
+        const unsigned int stream = MODE == 1 ? (P.half ? 2222u : 1111u) : (P.half ? 4444u : 3333u);
+        bay_u4 c;
+        c.x = k;
+        c.y = P.ctl->step[kind] + P.step_off;
+        c.z = stream;
+        c.w = 0xbeeff00du;
+        const bay_u4 r = bay_philox4x32_10(c, P.seeds[2 * T.m + kind] + P.half, 0xdecafbadu);
+        const float z = bay_stretch_z(P.ctl->a, bay_u01(r.y));
+        sZ[tid] = z;
+        sJ[tid] = bay_partner(bay_u01(r.x), M.K);
+        P.zu[2 * ((size_t)M.walker0 + k)] = z;
+        P.zu[2 * ((size_t)M.walker0 + k) + 1] = bay_u01(r.z);
+    }
+    __syncthreads();
+    // the tile's proposals: one contiguous block of nt * dim floats, element-wise
+    float* Y = P.y + M.xs + (size_t)T.k0 * dim;
+    const float* X = P.xs + M.xs + (MODE == 2 ? 0 : (size_t)P.half * M.K * dim) + (size_t)T.k0 * dim;
+    const float* S = P.xs + M.xs + (size_t)(1u - P.half) * M.K * dim;
+    const unsigned int ne = nt * dim;
+    for (unsigned int e = tid; e < ne; e += blockDim.x) {
+        if (MODE == 2) {
+            Y[e] = X[e];
+        } else {
+            const unsigned int w = e / dim, d = e - w * dim;
+            const float s = S[(size_t)sJ[w] * dim + d];
+            Y[e] = __fmaf_rn(sZ[w], __fsub_rn(X[e], s), s);
+        }
+    }
+    __syncthreads();
+    if (tid < nt) {
+        const float* y = Y + (size_t)tid * dim;
+        const float* hyper = P.params + M.params + M.rows * BAY_ROW_LEN;
+        float pr[BAY_PREP_LEN];
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) pr[i] = 0.0f;
+        BAY_TILE_PREP(hyper, M.hyper_len, dim, y, pr);
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) P.prep[((size_t)M.walker0 + k) * BAY_PREP_LEN + i] = pr[i];
+        P.wterm[(size_t)M.walker0 + k] = BAY_TILE_WALKER(M.rows, hyper, M.hyper_len, dim, y);
+    }
+}
+
+template <int MODE>  // 0: move (K walkers), 2: log density of all W
+__device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
+    extern __shared__ __align__(16) float bay_bsm[];
+    const bay_bitem I = P.items[blockIdx.x];
+    const bay_bmember& M = P.mem[I.m];
+    const unsigned int nk = MODE == 2 ? M.W : M.K;
+    const unsigned int dim = M.dim, wpc = I.wpc, tid = threadIdx.x;
+    float* Ys = bay_bsm;                                   // [wpc][dim]
+    float* Pr = Ys + ((wpc * dim + 3u) & ~3u);              // [wpc][BAY_PREP_LEN]
+    float* red = Pr + ((wpc * BAY_PREP_LEN + 3u) & ~3u);    // [256][2]
+    const unsigned int nv = nk - I.k0 < wpc ? nk - I.k0 : wpc;   // walkers of the item
+    const float* Yg = P.y + M.xs + (size_t)I.k0 * dim;
+    for (unsigned int e = tid; e < wpc * dim; e += blockDim.x) Ys[e] = e < nv * dim ? Yg[e] : 0.0f;
+    for (unsigned int e = tid; e < wpc * BAY_PREP_LEN; e += blockDim.x)
+        Pr[e] = e < nv * BAY_PREP_LEN ? P.prep[((size_t)M.walker0 + I.k0) * BAY_PREP_LEN + e] : 0.0f;
+    __syncthreads();
+    const unsigned int L = blockDim.x / wpc, w = tid % wpc, l = tid / wpc;
+    const unsigned long long r0 = (unsigned long long)I.c * M.chunk_rows;
+    const unsigned long long r1 = r0 + M.chunk_rows < M.rows ? r0 + M.chunk_rows : M.rows;
+    const float* data = P.params + M.params;
+    float sum = 0.0f, cmp = 0.0f;
+    if (w < nv) {
+        const float* xw = Ys + w * dim;
+        const float* pw = Pr + w * BAY_PREP_LEN;
+        for (unsigned long long r = r0 + l; r < r1; r += L) {
+            const float t = BAY_TILE_TERM(data + r * BAY_ROW_LEN, xw, pw);
+            const float yk = __fsub_rn(t, cmp);
+            const float s2 = __fadd_rn(sum, yk);
+            cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
+            sum = s2;
+        }
+    }
+    red[2 * tid] = sum;
+    red[2 * tid + 1] = -cmp;
+    __syncthreads();
+    if (tid < nv) {
+        bay_bcf a;
+        a.hi = 0.0f;
+        a.lo = 0.0f;
+        for (unsigned int j = 0; j < L; ++j) {
+            bay_bcf b;
+            b.hi = red[2 * (j * wpc + tid)];
+            b.lo = red[2 * (j * wpc + tid) + 1];
+            a = bay_bcadd(a, b);
+        }
+        float* out = P.part + M.part + 2 * ((size_t)(I.k0 + tid) * M.chunks + I.c);
+        out[0] = a.hi;
+        out[1] = a.lo;
+    }
+}
+
+template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions
+__device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P) {
+    const bay_btile T = P.tiles[blockIdx.x];
+    const bay_bmember& M = P.mem[T.m];
+    const unsigned int nk = MODE == 2 ? M.W : M.K;
+    const unsigned int dim = M.dim, tid = threadIdx.x;
+    const unsigned int k = T.k0 + tid;
+    const bool valid = k < nk;
+    bool accepted = false;
+    if (valid) {
+        const size_t wk = (size_t)M.walker0 + k;
+        bay_bcf s;
+        s.hi = P.wterm[wk];
+        s.lo = 0.0f;
+        const float* pp = P.part + M.part + 2 * (size_t)k * M.chunks;
+        for (unsigned int c = 0; c < M.chunks; ++c) {
+            bay_bcf p;
+            p.hi = pp[2 * c];
+            p.lo = pp[2 * c + 1];
+            s = bay_bcadd(s, p);
+        }
+        const float ly = __fadd_rn(s.hi, s.lo);
+        if (MODE == 2) {
+            P.logfn[wk] = ly;
+        } else {
+            const size_t lk = (size_t)M.walker0 + (size_t)P.half * M.K + k;
+            accepted = bay_batch_accept(P.zu[2 * wk + 1], P.zu[2 * wk], ly, P.logfn[lk],
+                                        MODE == 1 ? 1.0f : P.ctl->beta, dim);
+            if (accepted) {
+                float* X = P.xs + M.xs + ((size_t)P.half * M.K + k) * dim;
+                const float* y = P.y + M.xs + (size_t)k * dim;
+                for (unsigned int d = 0; d < dim; ++d) X[d] = y[d];
+                P.logfn[lk] = ly;
+            }
+        }
+    }
+    if (MODE != 1) return;
+    // accu: the member's accepted count and this CTA's per-dim sums of the moved walkers
+    const int n_acc = __syncthreads_count(accepted);
+    if (tid == 0 && n_acc) atomicAdd(&P.accepted[T.m], (unsigned long long)n_acc);
+    if (P.means_cap == 0) return;
+    const unsigned int nt = nk - T.k0 < blockDim.x ? nk - T.k0 : blockDim.x;
+    const float* Xc = P.xs + M.xs + ((size_t)P.half * M.K + T.k0) * dim;
+    float* out = P.dsum + ((size_t)P.step_off * 2 + P.half) * P.dsum_stride + M.dsum
+        + (size_t)(blockIdx.x - M.tile0) * dim;
+    for (unsigned int d = tid; d < dim; d += blockDim.x) {
+        bay_bcf s;
+        s.hi = 0.0f;
+        s.lo = 0.0f;
+        for (unsigned int w = 0; w < nt; ++w) {
+            bay_bcf y;
+            y.hi = Xc[(size_t)w * dim + d];
+            y.lo = 0.0f;
+            s = bay_bcadd(s, y);
+        }
+        out[d] = __fadd_rn(s.hi, s.lo);
+    }
+}
+
+// Per-step ensemble means of each member from the accu launches' per-CTA sums:
+// grid (members, steps); means[M.means + (step[1] + t) * dim + d] = sum / W in FP64.
+__device__ __forceinline__ void bay_batch_means_impl(const bay_batch_params& P) {
+    const unsigned int m = blockIdx.x, t = blockIdx.y;
+    const bay_bmember& M = P.mem[m];
+    const unsigned int step = P.ctl->step[1] + t;
+    if (step >= P.means_cap) return;
+    for (unsigned int d = threadIdx.x; d < M.dim; d += blockDim.x) {
+        double s = 0.0;
+        for (unsigned int h = 0; h < 2; ++h) {
+            const float* src = P.dsum + ((size_t)t * 2 + h) * P.dsum_stride + M.dsum + d;
+            for (unsigned int c = 0; c < M.ntiles; ++c) s += (double)src[(size_t)c * M.dim];
+        }
+        P.means[M.means + (size_t)step * M.dim + d] = (float)(s / (double)M.W);
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) bay_batch_propose_bare(bay_batch_params P) {
+    bay_batch_propose_impl<0>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_propose_accu(bay_batch_params P) {
+    bay_batch_propose_impl<1>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_propose_logfn(bay_batch_params P) {
+    bay_batch_propose_impl<2>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_move(bay_batch_params P) {
+    bay_batch_rows_impl<0>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_logfn(bay_batch_params P) {
+    bay_batch_rows_impl<2>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_accept_bare(bay_batch_params P) {
+    bay_batch_accept_impl<0>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_accept_accu(bay_batch_params P) {
+    bay_batch_accept_impl<1>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_accept_logfn(bay_batch_params P) {
+    bay_batch_accept_impl<2>(P);
+}
+extern "C" __global__ void __launch_bounds__(128) bay_batch_means(bay_batch_params P) {
+    bay_batch_means_impl(P);
+}

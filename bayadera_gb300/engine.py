@@ -136,6 +136,16 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
         d.row_len = t["row_len"]
         d.prep_len = t["prep_len"]
         d.walkers_per_cta = walkers_per_cta
+    elif form == "batch":
+        bt = model.batch
+        if not bt:
+            raise ValueError("model %s has no batch form" % model.name)
+        d.form = N.FORM_BATCH
+        d.tile_prep = b(bt["prep"])
+        d.tile_term = b(bt["term"])
+        d.tile_walker = b(bt["walker"])
+        d.row_len = bt["row_len"]
+        d.prep_len = bt.get("prep_len", 1)
     elif form == "gemm":
         gm = model.gemm
         if not gm:
@@ -184,6 +194,109 @@ class GB300StretchFactory:
         """SamplerFactory/create-sampler: params = data || hyperparameters (numpy, or a
         CUDA tensor that stays resident and must outlive the sampler)."""
         return GB300Stretch(self, seed, walkers, params)
+
+    def create_batch(self, members):
+        """A batch of independent models of this (batch-form) family; members is a list of
+        dicts {dim, seed, walkers, params (numpy float32: rows || hyperparameters), rows}."""
+        return GB300Batch(self, members)
+
+
+class GB300Batch:
+    """Many independent models of one family advanced together (bay_batch_*): member m
+    behaves as GB300Stretch(seed_m, walkers_m, params_m) of dimension dim_m."""
+
+    def __init__(self, sfactory, members):
+        self.sfactory = sfactory
+        self.members = [dict(m) for m in members]
+        arr = (N.BatchMember * len(members))()
+        self._keep = []
+        for i, m in enumerate(self.members):
+            p = np.ascontiguousarray(m["params"], np.float32)
+            self._keep.append(p)
+            arr[i].dim = int(m["dim"])
+            arr[i].seed = int(m["seed"]) & 0xffffffff
+            arr[i].walkers = int(m["walkers"])
+            arr[i].params = p.ctypes.data
+            arr[i].n_params = p.size
+            arr[i].rows = int(m["rows"])
+        h = C.c_void_p()
+        N.call("bay_batch_create", sfactory.handle, arr, len(members), C.byref(h))
+        self.handle = h
+        self._keep = None
+        self.dims = np.array([m["dim"] for m in self.members], np.int64)
+        self.walkers = np.array([m["walkers"] for m in self.members], np.int64)
+
+    def release(self):
+        if self.handle:
+            N.call("bay_batch_release", self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.release()
+
+    def info(self):
+        w, f, it = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        N.call("bay_batch_info", self.handle, C.byref(w), C.byref(f), C.byref(it))
+        return {"walkers": w.value, "floats": f.value, "items": it.value}
+
+    def set_graphs(self, enabled):
+        N.call("bay_batch_set_graphs", self.handle, 1 if enabled else 0)
+
+    def init_position_normal(self, seeds, mean=0.0, sd=1.0):
+        sd_ = np.ascontiguousarray(seeds, np.uint32)
+        if sd_.size != len(self.members):
+            raise ValueError("one seed per member")
+        N.call("bay_batch_init_position_normal", self.handle, _ptr(sd_), mean, sd)
+        return self
+
+    def init_position(self, positions):
+        """positions: a list of (walkers_m, dim_m) arrays."""
+        flat = np.concatenate([np.ascontiguousarray(p, np.float32).reshape(-1)
+                               for p in positions])
+        if flat.size != int(np.sum(self.dims * self.walkers)):
+            raise ValueError("positions must hold walkers_m x dim_m values per member")
+        N.call("bay_batch_init_position_host", self.handle, _ptr(flat))
+        return self
+
+    def burn_in(self, n, a):
+        N.call("bay_batch_burn_in", self.handle, int(n), float(a))
+        return self
+
+    def run_sampler(self, n, a, return_means=False):
+        rates = np.zeros(len(self.members))
+        flat = np.zeros(int(np.sum(self.dims)) * int(n), np.float32) if return_means else None
+        N.call("bay_batch_run_sampler", self.handle, int(n), float(a), _ptr(rates),
+               _ptr(flat) if flat is not None else None)
+        out = {"acceptance_rates": rates}
+        if flat is not None:
+            means, o = [], 0
+            for d in self.dims:
+                means.append(flat[o:o + n * d].reshape(n, d).T)
+                o += n * d
+            out["means"] = means
+        return out
+
+    def _split(self, flat, per):
+        out, o = [], 0
+        for p in per:
+            out.append(flat[o:o + p])
+            o += p
+        return out
+
+    def positions(self):
+        """list of (walkers_m, dim_m) arrays"""
+        flat = np.zeros(int(np.sum(self.dims * self.walkers)), np.float32)
+        N.call("bay_batch_state_export", self.handle, _ptr(flat), None)
+        return [f.reshape(w, d) for f, w, d in
+                zip(self._split(flat, self.dims * self.walkers), self.walkers, self.dims)]
+
+    def logfn(self):
+        flat = np.zeros(int(np.sum(self.walkers)), np.float32)
+        N.call("bay_batch_state_export", self.handle, None, _ptr(flat))
+        return self._split(flat, self.walkers)
 
 
 class GB300Stretch:

@@ -73,7 +73,7 @@ class DeviceDistributionModel:
     """
 
     def __init__(self, name, logpdf, mcmc_logpdf, dimension, params_size, limits, source,
-                 dialect="c99", tiled=None, gemm=None):
+                 dialect="c99", tiled=None, gemm=None, batch=None):
         self.name = name
         self.logpdf = logpdf
         self.mcmc_logpdf = mcmc_logpdf
@@ -84,6 +84,7 @@ class DeviceDistributionModel:
         self.dialect = dialect
         self.tiled = tiled
         self.gemm = gemm
+        self.batch = batch
 
     def source(self):
         return self.sources
@@ -101,12 +102,13 @@ class DeviceDistributionModel:
 
 
 def device_distribution_model(source, name=None, logpdf=None, mcmc_logpdf=None, dimension=1,
-                              params_size=1, limits=None, dialect="c99", tiled=None, gemm=None):
+                              params_size=1, limits=None, dialect="c99", tiled=None, gemm=None,
+                              batch=None):
     """device-distribution-model (models.clj:84-89) with the same defaults."""
     name = name or _gensym("distribution")
     logpdf = logpdf or "%s_logpdf" % name
     return DeviceDistributionModel(name, logpdf, mcmc_logpdf or logpdf, dimension, params_size,
-                                   limits, source, dialect, tiled, gemm)
+                                   limits, source, dialect, tiled, gemm, batch)
 
 
 def device_likelihood_model(source, name=None, loglik=None, dialect="c99"):
@@ -236,3 +238,38 @@ def hierarchical_model(groups):
     return device_distribution_model(get_source("hierarchical"), name="hierarchical",
                                      dimension=groups + 2, params_size=2,
                                      logpdf="hierarchical_logpdf")
+
+
+HROWS_BATCH = {"prep": "hrows_prep", "term": "hrows_term", "walker": "hrows_walker",
+               "row_len": 3, "prep_len": 1}
+
+
+def hierarchical_rows_model(groups):
+    """Gaussian hierarchical model on observation rows (y, group, -1/(2 sigma^2)), plain
+    single-model form, D = groups + 2; also the batch family member of that dimension."""
+    return device_distribution_model(get_source("hierarchical_rows"), name="hrows",
+                                     dimension=groups + 2, params_size=2,
+                                     logpdf="hrows_logpdf", batch=HROWS_BATCH)
+
+
+def hierarchical_rows_batch_model(max_groups=128):
+    """The batch family of the row-encoded hierarchical model (runtime dimension up to
+    max_groups + 2): many independent models advanced by one bay_batch."""
+    return device_distribution_model(get_source("hierarchical_rows"), name="hrows",
+                                     dimension=max_groups + 2, params_size=2,
+                                     logpdf="hrows_logpdf", batch=HROWS_BATCH)
+
+
+def hierarchical_rows_params(groups_y, sigmas, h0=10.0, h1=1.0):
+    """params of the row-encoded hierarchical model: one row (y, j, -1/(2 sigma_j^2)) per
+    observation of group j, then (h0, h1).  Returns (params float32, rows)."""
+    rows = []
+    for j, (y, s) in enumerate(zip(groups_y, sigmas)):
+        y = np.asarray(y, np.float32)
+        r = np.empty((y.size, 3), np.float32)
+        r[:, 0] = y
+        r[:, 1] = j
+        r[:, 2] = -0.5 / (float(s) * float(s))
+        rows.append(r)
+    rows = np.concatenate(rows) if rows else np.zeros((0, 3), np.float32)
+    return np.concatenate([rows.reshape(-1), np.array([h0, h1], np.float32)]), rows.shape[0]

@@ -354,6 +354,146 @@ def run_config(args):
     return 0
 
 
+# ------------------------------------------------------------------ batched models
+def c4_members(M, n=512, seed=0):
+    """512 Gaussian hierarchical models: J log-uniform in [2, 128] groups (dimension
+    J + 2), n_j log-uniform in [10, 1000] observations per group, sigma_j log-uniform in
+    [0.5, 2] (known), theta_j ~ N(mu, tau^2) with mu ~ N(0, 3^2), log tau ~ N(0, 0.5^2);
+    walkers per model from {256, 512, 1024, 4096}; seeded."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(n):
+        J = int(round(np.exp(rng.uniform(np.log(2.0), np.log(128.0)))))
+        nj = np.round(np.exp(rng.uniform(np.log(10.0), np.log(1000.0), J))).astype(int)
+        sig = np.exp(rng.uniform(np.log(0.5), np.log(2.0), J))
+        mu, tau = rng.normal(0.0, 3.0), np.exp(rng.normal(0.0, 0.5))
+        theta = rng.normal(mu, tau, J)
+        ys = [rng.normal(theta[j], sig[j], nj[j]) for j in range(J)]
+        params, rows = M.hierarchical_rows_params(ys, sig)
+        W = int(rng.choice([256, 512, 1024, 4096]))
+        out.append({"dim": J + 2, "seed": 1000 + m, "walkers": W, "params": params,
+                    "rows": rows})
+    return out
+
+
+def run_c4(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from bayadera_gb300 import _native
+    from bayadera_gb300 import models as M
+    from bayadera_gb300.engine import GB300BayaderaFactory
+    torch.cuda.set_device(0)
+    BURN4, RUN4 = 1000, 2000
+    mem = c4_members(M)
+    W = np.array([m["walkers"] for m in mem], np.float64)
+    N = np.array([m["rows"] for m in mem], np.float64)
+    J = np.array([m["dim"] - 2 for m in mem], np.float64)
+    flop_step = float(np.sum(W * (3 * N + 3 * J)))
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    f = GB300BayaderaFactory(device=0, wgs=1024, stream=stream.cuda_stream)
+    fam = f.mcmc_factory(M.hierarchical_rows_batch_model(128), form="batch")
+    b = fam.create_batch(mem)
+    seeds = [7 + i for i in range(len(mem))]
+
+    def job(k):
+        b.init_position_normal([s + 31 * k for s in seeds], 0.0, 1.0)
+        b.burn_in(BURN4, 2.0)
+        return b.run_sampler(RUN4, 2.0)
+
+    for w in range(args.warmup):
+        job(100 + w)
+    torch.cuda.synchronize()
+    times = []
+    l0 = _native.launch_count()
+    with ClockSampler(0) as clocks:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = job(k)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    launches = _native.launch_count() - l0
+    # one burn-in step alone: time per ensemble step of the whole batch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.burn_in(64, 2.0)
+    e1.record(stream)
+    e1.synchronize()
+    t_step = e0.elapsed_time(e1) / 1e3 / 64
+    info = b.info()
+    b.release()
+    fam.release()
+    value = float(np.sum(W)) * (BURN4 + RUN4) * args.steps / sum(times)
+
+    # plain single-model form: a uniform random sample of the members, each its own
+    # sampler (one plain kernel per half-step, the reference's structure), run in turn;
+    # the full job's time is estimated as (members / sample) x the sample's time
+    rng = np.random.default_rng(1)
+    sample = sorted(rng.choice(len(mem), size=16, replace=False).tolist())
+    PB, PR = 50, 100
+    compiled, t_plain = {}, 0.0
+    for i in sample:
+        m = mem[i]
+        if m["dim"] not in compiled:
+            compiled[m["dim"]] = f.mcmc_factory(M.hierarchical_rows_model(m["dim"] - 2),
+                                                form="plain")
+        s = compiled[m["dim"]].create_sampler(m["seed"], m["walkers"], m["params"])
+        s.init_position_normal(seeds[i], 0.0, 1.0)
+        s.burn_in(5, 2.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.burn_in(PB, 2.0)
+        s.run_sampler(PR, 2.0)
+        e1.record(stream)
+        e1.synchronize()
+        t_plain += e0.elapsed_time(e1) / 1e3 * (BURN4 + RUN4) / (PB + PR)
+        s.release()
+    for sf in compiled.values():
+        sf.release()
+    f.release()
+    t_plain_full = t_plain * len(mem) / len(sample)
+    plain_value = float(np.sum(W)) * (BURN4 + RUN4) / t_plain_full
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    achieved = flop_step / t_step / 1e12
+    rates = res["acceptance_rates"]
+    line = {"metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "512 Gaussian hierarchical models, J log-U[2,128], n_j "
+                                   "log-U[10,1000], walkers {256,512,1024,4096}",
+                       "models": len(mem), "walkers_total": int(np.sum(W)),
+                       "rows_total": int(np.sum(N)), "burn_in": BURN4, "run": RUN4,
+                       "form": "batch (3 launches per half-step over balanced work lists, "
+                               "CUDA-graph chunks)",
+                       "rows_items_per_half_step": info["items"],
+                       "l2": "flushed between timed jobs"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                         "peak_kind": "nominal (152 SMs x 128 FMA lanes x 2.07 GHz)",
+                         "ms_per_ensemble_step": 1e3 * t_step,
+                         "flop_per_ensemble_step": flop_step},
+            "forms": {"batch": value, "plain_fp32": plain_value,
+                      "speedup_vs_plain": value / plain_value,
+                      "plain_sample": "%d of %d members, %d+%d steps each, time scaled to the "
+                                      "full job" % (len(sample), len(mem), PB, PR)},
+            "clocks": clocks.summary(),
+            "result": {"acceptance_rate_min": float(rates.min()),
+                       "acceptance_rate_max": float(rates.max())}}
+    print(json.dumps(line))
+    return 0
+
+
 # ------------------------------------------------------------------ GPU arm
 def main():
     ap = argparse.ArgumentParser()
@@ -362,7 +502,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"],
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default): the 50-D Gaussian job; c1, c3, c5: the other "
                          "benchmark workloads, measured GEMM/tiled form vs plain form")
     ap.add_argument("--forms", default="",
@@ -371,6 +511,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "c4":
+        return run_c4(args)
     if args.config != "c2":
         return run_config(args)
 

@@ -104,7 +104,15 @@ int bay_launch_count(uint64_t* out);
  * on the tensor cores (split bf16, see the flag).  Covers Gaussian targets (A =
  * precision matrix, term = -eta_r x_r/2) and regression likelihoods (A = design matrix,
  * aux = response). */
-enum bay_form { BAY_FORM_PLAIN = 0, BAY_FORM_TILED = 1, BAY_FORM_GEMM = 2 };
+/* BAY_FORM_BATCH compiles a model family for bay_batch (many independent models advanced
+ * together), row form with the dimension known only at run time:
+ *   void  prep(const REAL* hyper, uint32_t hyper_len, uint32_t dim, const REAL* x,
+ *              REAL* prep);                         per walker, prep_len values
+ *   REAL  term(const REAL* row, const REAL* x, const REAL* prep);  one row of row_len floats
+ *   REAL  walker(uint64_t n_rows, const REAL* hyper, uint32_t hyper_len, uint32_t dim,
+ *                const REAL* x);                     every term not summed over rows
+ * dim in the description is the largest member dimension. */
+enum bay_form { BAY_FORM_PLAIN = 0, BAY_FORM_TILED = 1, BAY_FORM_GEMM = 2, BAY_FORM_BATCH = 3 };
 enum bay_model_flags {
     /* accept if u <= z^(D-1) exp(beta dlogfn) in fp32, the reference's formula
      * (nvidia-gtx-mcmc-stretch.cu:84-88); default compares logs in FP64. */
@@ -264,6 +272,43 @@ int bay_logfn_values(bay_sampler* s, float* out);
 
 /* Execution control: CUDA-graph replay of the step loops (default on). */
 int bay_sampler_set_graphs(bay_sampler* s, int enabled);
+
+/* ---------------------------------------------------------------- batched models
+ * Many independent models of one BAY_FORM_BATCH family -- each with its own dimension,
+ * walkers, data and seed -- advanced together: every half-step of every member is three
+ * launches over balanced work lists (propose, row terms, accept), and the step loops
+ * replay as CUDA graphs.  Member m behaves as a sampler created with its seed (same
+ * Philox counters and keys, same init!/init-move! seed rules), so the per-member
+ * semantics are those of the functions above.  No counterpart in the reference, which
+ * runs one model per sampler. */
+typedef struct bay_batch bay_batch;
+typedef struct bay_batch_member {
+    uint32_t dim;             /* walker dimension, <= the model's dim */
+    uint32_t seed;            /* the member's seed (as bay_sampler_create) */
+    uint64_t walkers;         /* even, >= 4 */
+    const float* params;      /* rows (row_len floats each) || hyperparameters, host memory */
+    uint64_t n_params;        /* floats in params */
+    uint64_t rows;            /* data rows at the start of params */
+} bay_batch_member;
+
+int bay_batch_create(bay_model* model, const bay_batch_member* members, uint32_t n,
+                     bay_batch** out);
+int bay_batch_release(bay_batch* b);
+/* Walkers of member m ~ N(mean, sd^2) i.i.d. with seeds[m] (bay_init_position_normal). */
+int bay_batch_init_position_normal(bay_batch* b, const uint32_t* seeds, float mean, float sd);
+/* Positions of every member from host memory (member-major, walkers x dim each). */
+int bay_batch_init_position_host(bay_batch* b, const float* positions);
+int bay_batch_burn_in(bay_batch* b, uint64_t steps, float a);
+/* init-move! and `steps` accu steps of every member: acc_rates[m] (n doubles) and, when
+ * means is not NULL, the per-step ensemble means of each member (member-major, steps x
+ * dim each, the layout bay_acor reads). */
+int bay_batch_run_sampler(bay_batch* b, uint64_t steps, float a, double* acc_rates,
+                          float* means);
+/* Positions (member-major, walkers x dim each) and log densities (member-major), host. */
+int bay_batch_state_export(bay_batch* b, float* positions, float* logfn);
+/* total walkers, total positions (floats), rows work items of a move half-step */
+int bay_batch_info(bay_batch* b, uint64_t* walkers, uint64_t* floats, uint64_t* items);
+int bay_batch_set_graphs(bay_batch* b, int enabled);
 
 #ifdef __cplusplus
 }

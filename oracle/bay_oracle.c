@@ -419,6 +419,46 @@ static double m_hier64(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, c
     return res - mu * mu / (2.0 * (double)h[0] * h[0]) - lt * lt / (2.0 * (double)h[1] * h[1]);
 }
 
+/* The same hierarchical model on observation rows (y, g, c = -1/(2 sigma_g^2)), data
+ * length 3 N, hyper {mu_sd, logtau_sd}: the batch-form model of the library
+ * (csrc/library/hierarchical_rows.h), rows summed in order. */
+static float m_hrows32(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, const float* x) {
+    (void)pl;
+    const uint32_t n = dl / 3, J = dim - 2;
+    const float* h = p + dl;
+    float res = 0.0f;
+    for (uint32_t i = 0; i < n; i++) {
+        const float* r = p + 3 * (uint64_t)i;
+        const float d = r[0] - x[(uint32_t)r[1]];
+        res += r[2] * d * d;
+    }
+    const float mu = x[J], lt = x[J + 1], c = -0.5f * expf(-2.0f * lt);
+    float s = 0.0f;
+    for (uint32_t j = 0; j < J; j++) {
+        const float d = x[j] - mu;
+        s = fmaf(d * d, c, s);
+    }
+    return res + (s - (float)J * lt - mu * mu / (2.0f * h[0] * h[0]) - lt * lt / (2.0f * h[1] * h[1]));
+}
+static double m_hrows64(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, const double* x) {
+    (void)pl;
+    const uint32_t n = dl / 3, J = dim - 2;
+    const float* h = p + dl;
+    double res = 0.0;
+    for (uint32_t i = 0; i < n; i++) {
+        const float* r = p + 3 * (uint64_t)i;
+        const double d = (double)r[0] - x[(uint32_t)r[1]];
+        res += (double)r[2] * d * d;
+    }
+    const double mu = x[J], lt = x[J + 1], c = -0.5 * exp(-2.0 * lt);
+    for (uint32_t j = 0; j < J; j++) {
+        const double d = x[j] - mu;
+        res += d * d * c;
+    }
+    return res - (double)J * lt - mu * mu / (2.0 * (double)h[0] * h[0])
+        - lt * lt / (2.0 * (double)h[1] * h[1]);
+}
+
 typedef struct {
     const char* name;
     logfn32_t f32;
@@ -434,6 +474,7 @@ static const bo_model bo_models[] = {
     {"logistic", m_logistic32, m_logistic64},
     {"robust_t", m_robust32, m_robust64},
     {"hierarchical", m_hier32, m_hier64},
+    {"hrows", m_hrows32, m_hrows64},
 };
 
 static const bo_model* find_model(const char* name) {

@@ -84,6 +84,16 @@ def test_model_check_benchmark_models(native):
     _check(M.hierarchical_model(4))
 
 
+def test_model_check_batch_form(native):
+    """The batched engine's kernels (runtime dimension) compile for the hierarchical family;
+    a model without a batch form is an argument error."""
+    from bayadera_gb300 import models as M
+    _check(M.hierarchical_rows_batch_model(128), "batch")
+    _check(M.hierarchical_rows_model(7), "plain")
+    with pytest.raises(ValueError, match="batch form"):
+        _check(M.logistic_model(8), "batch")
+
+
 def test_model_check_tensor_core_form(native):
     """The tcgen05 rows kernels compile for sm_103a across the feature-chunk counts (1 to
     5 chunks of 64, one or two walker sub-tiles per CTA); more than 320 features is an

@@ -1,0 +1,169 @@
+"""Batched engine (bay_batch_*): many independent hierarchical models of uneven dimension,
+walkers and data advanced together, against the oracle's FP64 density, the single-model
+sampler with the same seed, and an FP64 quadrature of the posterior."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def factory():
+    import __graft_entry__
+    __graft_entry__.build()
+    from bayadera_gb300.engine import GB300BayaderaFactory
+    f = GB300BayaderaFactory(device=0, wgs=256)
+    yield f
+    f.release()
+
+
+@pytest.fixture(scope="module")
+def M():
+    from bayadera_gb300 import models
+    return models
+
+
+@pytest.fixture(scope="module")
+def family(factory, M):
+    sf = factory.mcmc_factory(M.hierarchical_rows_batch_model(128), form="batch")
+    yield sf
+    sf.release()
+
+
+def _member(M, rng, J, n_lo, n_hi, walkers, seed):
+    sig = np.exp(rng.uniform(np.log(0.5), np.log(2.0), J))
+    mu, tau = rng.normal(0.0, 3.0), np.exp(rng.normal(0.0, 0.5))
+    theta = rng.normal(mu, tau, J)
+    ys = [rng.normal(theta[j], sig[j], int(rng.integers(n_lo, n_hi + 1))) for j in range(J)]
+    params, rows = M.hierarchical_rows_params(ys, sig)
+    return {"dim": J + 2, "seed": seed, "walkers": walkers, "params": params, "rows": rows,
+            "ys": ys, "sig": sig}
+
+
+def _members(M, seed=0):
+    rng = np.random.default_rng(seed)
+    spec = [(2, 10, 30, 4), (5, 10, 100, 256), (17, 50, 400, 258), (40, 200, 600, 512),
+            (3, 3000, 9000, 1024), (128, 10, 40, 256), (9, 0, 0, 64)]
+    out = []
+    for i, (J, lo, hi, W) in enumerate(spec):
+        m = _member(M, rng, J, lo, hi, W, 100 + 7 * i)
+        out.append(m)
+    return out
+
+
+def test_batch_logfn_matches_fp64(family, M, oracle):
+    """After init-position, every member's log densities against the oracle's FP64 density
+    (relative 2e-5: fp32 row terms, Kahan chunk sums, compensated chunk combine).  Members
+    span dimension 4..130, 4..1024 walkers, 0..~40000 rows (several row chunks)."""
+    mem = _members(M)
+    b = family.create_batch(mem)
+    b.init_position_normal([11 + i for i in range(len(mem))], 0.0, 1.0)
+    pos, lf = b.positions(), b.logfn()
+    for m, p, l in zip(mem, pos, lf):
+        idx = np.arange(0, m["walkers"], max(1, m["walkers"] // 24))
+        want = np.array([oracle.logfn64("hrows", m["params"], 3 * m["rows"], m["dim"],
+                                        p[i].astype(np.float64)) for i in idx])
+        err = np.abs(l[idx] - want) / np.maximum(np.abs(want), 1.0)
+        assert err.max() < 2e-5, (m["dim"], m["rows"], err.max())
+    b.release()
+
+
+def test_batch_member_matches_single_sampler(factory, family, M):
+    """Member m uses the single sampler's Philox keys and counters with its seed: the same
+    initial walkers bit-for-bit, and after burn-in steps the same walkers except where an
+    accept decision is marginal (the two sum the density in different orders)."""
+    mem = _members(M, seed=1)[:5]
+    b = family.create_batch(mem)
+    seeds = [21 + i for i in range(len(mem))]
+    b.init_position_normal(seeds, 0.0, 0.5)
+    init = [p.copy() for p in b.positions()]
+    b.burn_in(6, 2.0)
+    got = b.positions()
+    for i, m in enumerate(mem):
+        sf = factory.mcmc_factory(M.hierarchical_rows_model(m["dim"] - 2), form="plain")
+        s = sf.create_sampler(m["seed"], m["walkers"], m["params"])
+        s.init_position_normal(seeds[i], 0.0, 0.5)
+        np.testing.assert_array_equal(s.positions().T, init[i])
+        s.burn_in(6, 2.0)
+        differ = np.any(s.positions().T != got[i], axis=1).sum()
+        assert differ <= max(2, m["walkers"] // 20), (i, differ)
+        s.release()
+        sf.release()
+    b.release()
+
+
+def test_batch_graphs_match_direct_launches(family, M):
+    """Graph replay and direct launches run the same kernels in the same order: identical
+    positions and log densities."""
+    mem = _members(M, seed=2)[:4]
+    out = []
+    for graphs in (True, False):
+        b = family.create_batch(mem)
+        b.set_graphs(graphs)
+        b.init_position_normal([5, 6, 7, 8], 0.0, 1.0)
+        b.burn_in(40, 2.0)
+        out.append((np.concatenate([p.reshape(-1) for p in b.positions()]),
+                    np.concatenate(b.logfn())))
+        b.release()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+def _posterior_grid(ys, sig, h0=10.0, h1=1.0):
+    """E[mu | y] and E[log tau | y] of the hierarchical model by FP64 quadrature over
+    u = log tau: theta integrates out exactly (ybar_j | mu, tau ~ N(mu, s_j^2 + tau^2),
+    s_j^2 = sigma_j^2 / n_j), then mu (Gaussian)."""
+    yb = np.array([np.mean(np.asarray(y, np.float32).astype(np.float64)) for y in ys])
+    s2 = np.array([float(np.float32(s)) ** 2 / len(y) for y, s in zip(ys, sig)])
+    u = np.linspace(-12.0, 6.0, 40001)
+    V = s2[None, :] + np.exp(2.0 * u)[:, None]
+    lam = 1.0 / h0 ** 2 + np.sum(1.0 / V, axis=1)
+    b = np.sum(yb[None, :] / V, axis=1)
+    logp = (-0.5 * np.sum(np.log(V), axis=1) - 0.5 * np.sum(yb[None, :] ** 2 / V, axis=1)
+            + 0.5 * b * b / lam - 0.5 * np.log(lam) - 0.5 * u * u / h1 ** 2)
+    w = np.exp(logp - logp.max())
+    w /= w.sum()
+    return float(np.sum(w * b / lam)), float(np.sum(w * u))
+
+
+def _batch_se(series, nb=16):
+    n = series.size // nb * nb
+    bm = series[:n].reshape(nb, -1).mean(axis=1)
+    return bm.std(ddof=1) / np.sqrt(nb)
+
+
+def test_batch_posterior_matches_quadrature(family, M):
+    """Posterior means of mu and log tau of several members (run means over 2000 steps)
+    within 4.5 batch-means standard errors of the FP64 quadrature, and acceptance counts
+    per member: the per-step means' last column is the mean of the walkers."""
+    rng = np.random.default_rng(7)
+    mem = [_member(M, rng, J, lo, hi, W, 300 + i) for i, (J, lo, hi, W) in
+           enumerate([(3, 20, 60, 512), (8, 10, 50, 1024), (12, 30, 90, 512), (6, 5, 15, 1024)])]
+    b = family.create_batch(mem)
+    b.init_position_normal([31, 32, 33, 34], 0.0, 0.5)
+    b.burn_in(1500, 2.0)
+    r = b.run_sampler(2000, 2.0, return_means=True)
+    pos = b.positions()
+    for i, m in enumerate(mem):
+        a = r["acceptance_rates"][i]
+        assert 0.05 < a < 0.95, a
+        means = r["means"][i]
+        np.testing.assert_allclose(means[:, -1], pos[i].mean(axis=0), rtol=1e-4, atol=1e-5)
+        mu_ref, lt_ref = _posterior_grid(m["ys"], m["sig"])
+        J = m["dim"] - 2
+        for d, ref in ((J, mu_ref), (J + 1, lt_ref)):
+            est = means[d].mean()
+            se = _batch_se(means[d])
+            assert abs(est - ref) <= 4.5 * se + 1e-3, (i, d, est, ref, se)
+    b.release()
+
+
+def test_batch_rejects_bad_members(family, M):
+    from bayadera_gb300._native import BayaderaError
+    rng = np.random.default_rng(3)
+    m = _member(M, rng, 4, 5, 10, 64, 1)
+    bad = dict(m, dim=131)
+    with pytest.raises(BayaderaError, match="dim"):
+        family.create_batch([m, bad])
+    with pytest.raises(BayaderaError, match="walkers"):
+        family.create_batch([dict(m, walkers=7)])
