@@ -8,11 +8,14 @@
 //            single-sampler counter {k, step, stream, 0xbeeff00d}, stretch factor, partner
 //            from the member's other half, the proposal y -> scratch (coalesced over the
 //            tile's contiguous block), per-walker prep and the terms outside the row sum;
-//   rows:    CTA = (member, tile of wpc walkers, chunk of rows): the model's row terms of
-//            the chunk, 256 / wpc threads per walker, Kahan sums combined in lane order ->
-//            a compensated partial per (walker, chunk).  wpc and the chunk size are chosen
-//            per member so that every item carries about the same work, which balances
-//            members whose data differ by orders of magnitude;
+//   rows:    CTA = (member, tile of wpc walkers, chunk of rows): the chunk of rows and the
+//            walkers' proposals are staged in shared memory, then each of 256 / wpc lanes
+//            per walker sums the row terms of its rows (walkers fastest, so a warp reads
+//            one row as a broadcast) in pairwise batches with a Kahan carry; lanes combine
+//            by an xor butterfly and in warp order -> a compensated partial per (walker,
+//            chunk).  wpc and the chunk size are chosen per member so that every item
+//            carries about the same work, which balances members whose data differ by
+//            orders of magnitude;
 //   accept:  CTA = (member, 256-walker tile): partials summed in chunk order, FP64 log
 //            accept, write-back; accu: accepted count per member, per-CTA per-dim sums.
 // Counter and key words per member are those of a single sampler with the member's seed,
@@ -31,6 +34,8 @@
 #ifndef BAY_PREP_LEN
 #define BAY_PREP_LEN 1
 #endif
+// staged rows: BAY_ROW_LEN floats padded to a 16-byte stride, one vector load per row
+#define BAY_ROW_STRIDE ((BAY_ROW_LEN + 3) & ~3)
 
 struct bay_ctl {
     unsigned int step[2];
@@ -179,42 +184,102 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
     const bay_bmember& M = P.mem[I.m];
     const unsigned int nk = MODE == 2 ? M.W : M.K;
     const unsigned int dim = M.dim, wpc = I.wpc, tid = threadIdx.x;
-    float* Ys = bay_bsm;                                   // [wpc][dim]
-    float* Pr = Ys + ((wpc * dim + 3u) & ~3u);              // [wpc][BAY_PREP_LEN]
-    float* red = Pr + ((wpc * BAY_PREP_LEN + 3u) & ~3u);    // [256][2]
+    const unsigned long long r0 = (unsigned long long)I.c * M.chunk_rows;
+    const unsigned int nr = (unsigned int)(r0 + M.chunk_rows < M.rows ? M.chunk_rows : M.rows - r0);
+    const unsigned int dpad = dim | 1u;   // odd walker stride: the lanes' x[j] hit distinct banks
+    float* Ys = bay_bsm;                                              // [wpc][dpad]
+    float* Pr = Ys + ((wpc * dpad + 3u) & ~3u);                        // [wpc][BAY_PREP_LEN]
+    float* Rs = Pr + ((wpc * BAY_PREP_LEN + 3u) & ~3u);                // [nr][BAY_ROW_STRIDE]
+    float* red = Rs + M.chunk_rows * BAY_ROW_STRIDE;                   // [256][2]
     const unsigned int nv = nk - I.k0 < wpc ? nk - I.k0 : wpc;   // walkers of the item
+    // stage the item's walkers, their prep values and its chunk of rows (coalesced,
+    // every load issued before any is used)
     const float* Yg = P.y + M.xs + (size_t)I.k0 * dim;
-    for (unsigned int e = tid; e < wpc * dim; e += blockDim.x) Ys[e] = e < nv * dim ? Yg[e] : 0.0f;
+    for (unsigned int e = tid; e < wpc * dim; e += blockDim.x) {
+        const unsigned int ww = e / dim;
+        Ys[ww * dpad + (e - ww * dim)] = e < nv * dim ? Yg[e] : 0.0f;
+    }
     for (unsigned int e = tid; e < wpc * BAY_PREP_LEN; e += blockDim.x)
         Pr[e] = e < nv * BAY_PREP_LEN ? P.prep[((size_t)M.walker0 + I.k0) * BAY_PREP_LEN + e] : 0.0f;
+    const float* Rg = P.params + M.params + r0 * BAY_ROW_LEN;
+    const unsigned int nf = nr * BAY_ROW_LEN;
+#pragma unroll 4
+    for (unsigned int e = tid; e < nf; e += blockDim.x) {
+        const unsigned int rr = e / BAY_ROW_LEN;
+        Rs[rr * BAY_ROW_STRIDE + (e - rr * BAY_ROW_LEN)] = __ldg(Rg + e);
+    }
     __syncthreads();
+    // walkers fastest: a warp's lanes are up to 32 walkers on the same row (a broadcast)
     const unsigned int L = blockDim.x / wpc, w = tid % wpc, l = tid / wpc;
-    const unsigned long long r0 = (unsigned long long)I.c * M.chunk_rows;
-    const unsigned long long r1 = r0 + M.chunk_rows < M.rows ? r0 + M.chunk_rows : M.rows;
-    const float* data = P.params + M.params;
     float sum = 0.0f, cmp = 0.0f;
     if (w < nv) {
-        const float* xw = Ys + w * dim;
+        const float* xw = Ys + w * dpad;
         const float* pw = Pr + w * BAY_PREP_LEN;
-        for (unsigned long long r = r0 + l; r < r1; r += L) {
-            const float t = BAY_TILE_TERM(data + r * BAY_ROW_LEN, xw, pw);
-            const float yk = __fsub_rn(t, cmp);
+        unsigned int r = l;
+        // batches of 8 rows summed pairwise, each batch added with Kahan compensation;
+        // a row comes to registers as BAY_ROW_STRIDE / 4 vector loads (a warp's lanes load
+        // the same row: a broadcast)
+        for (; r + 7u * L < nr; r += 8u * L) {
+            float t[8];
+#pragma unroll
+            for (unsigned int i = 0; i < 8u; ++i) {
+                float rv[BAY_ROW_STRIDE];
+                const float4* rp = reinterpret_cast<const float4*>(Rs + (r + i * L) * BAY_ROW_STRIDE);
+#pragma unroll
+                for (int q = 0; q < BAY_ROW_STRIDE / 4; ++q) {
+                    const float4 v4 = rp[q];
+                    rv[4 * q] = v4.x;
+                    rv[4 * q + 1] = v4.y;
+                    rv[4 * q + 2] = v4.z;
+                    rv[4 * q + 3] = v4.w;
+                }
+                t[i] = BAY_TILE_TERM(rv, xw, pw);
+            }
+#pragma unroll
+            for (unsigned int h = 4u; h >= 1u; h >>= 1)
+#pragma unroll
+                for (unsigned int i = 0; i < h; ++i) t[i] = __fadd_rn(t[i], t[i + h]);
+            const float yk = __fsub_rn(t[0], cmp);
+            const float s2 = __fadd_rn(sum, yk);
+            cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
+            sum = s2;
+        }
+        for (; r < nr; r += L) {
+            const float yk = __fsub_rn(BAY_TILE_TERM(Rs + r * BAY_ROW_STRIDE, xw, pw), cmp);
             const float s2 = __fadd_rn(sum, yk);
             cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
             sum = s2;
         }
     }
-    red[2 * tid] = sum;
-    red[2 * tid + 1] = -cmp;
+    // combine the lanes of each walker: inside a warp by an xor butterfly over the lane
+    // bits above the walker bits (bay_bcadd is symmetric, so every lane of a walker ends
+    // with the same bits), then across warps in warp order
+    bay_bcf v;
+    v.hi = sum;
+    v.lo = -cmp;
+    for (unsigned int o = 16u; o >= wpc && o >= 1u; o >>= 1) {
+        bay_bcf u;
+        u.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+        u.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        v = bay_bcadd(v, u);
+    }
+    const unsigned int lane = tid & 31u, warp = tid >> 5;
+    const unsigned int wpw = wpc < 32u ? wpc : 32u;   // walkers per warp
+    if (lane < wpw) {
+        red[2 * (warp * 32u + lane)] = v.hi;
+        red[2 * (warp * 32u + lane) + 1] = v.lo;
+    }
     __syncthreads();
     if (tid < nv) {
+        // walker tid's partials: warps holding it, each at lane tid % 32
+        const unsigned int stride = wpc < 32u ? 1u : wpc / 32u;   // warps between its copies
         bay_bcf a;
         a.hi = 0.0f;
         a.lo = 0.0f;
-        for (unsigned int j = 0; j < L; ++j) {
+        for (unsigned int wq = tid / 32u; wq < blockDim.x / 32u; wq += stride) {
             bay_bcf b;
-            b.hi = red[2 * (j * wpc + tid)];
-            b.lo = red[2 * (j * wpc + tid) + 1];
+            b.hi = red[2 * (wq * 32u + (tid & 31u))];
+            b.lo = red[2 * (wq * 32u + (tid & 31u)) + 1];
             a = bay_bcadd(a, b);
         }
         float* out = P.part + M.part + 2 * ((size_t)(I.k0 + tid) * M.chunks + I.c);
