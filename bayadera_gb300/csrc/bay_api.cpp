@@ -181,6 +181,8 @@ struct bay_model {
     // GEMM form on the tensor cores: rows kernels [move, logfn], walker sub-tiles per CTA,
     // shared-memory stages, dynamic shared memory
     CUkernel k_gt[2] = {nullptr, nullptr};
+    // GEMM form on the tensor cores with the matrix resident: [bare, accu, logfn]
+    CUkernel k_tr[3] = {nullptr, nullptr, nullptr};
     uint32_t tc_g = 0, tc_stages = 0;
     size_t tc_smem = 0;
     // batch form: propose / accept in k_gp / k_ga, rows in k_gr, per-step means here
@@ -371,6 +373,7 @@ struct bay_sampler {
     // streaming on the tensor cores: bf16 hi + lo matrix [rows_pad][tc_fp], coefficient
     // operand [tc_wpad][tc_fp] (hi, lo), the aux values in gemm_lay [rows_pad][aux]
     bool tc = false;
+    bool tcr = false;   // tensor cores, matrix resident (one launch per half-step)
     uint32_t tc_fp = 0;
     uint64_t tc_rows_pad = 0, tc_wpad = 0;
     unsigned short *tc_xh = nullptr, *tc_xl = nullptr, *s_bh = nullptr, *s_bl = nullptr;
@@ -378,6 +381,7 @@ struct bay_sampler {
 
     uint64_t per_cta() const {
         if (streaming) return 256;  // the accept kernel: one thread per walker
+        if (tcr) return 64;
         return model->form == BAY_FORM_PLAIN ? model->cta : model->wpc;
     }
 
@@ -458,8 +462,9 @@ struct bay_sampler {
         if (st == ctx->stream) bay::count_launches(1);
         bay_stretch_params p = make_params(half, step_off);
         void* args[] = {&p};
-        cu_check(g_cu.LaunchKernel((CUfunction)(accu ? model->k_accu : model->k_bare), grid(), 1, 1,
-                                   model->cta, 1, 1, (unsigned)smem, (CUstream)st, args, nullptr),
+        CUkernel k = tcr ? model->k_tr[accu ? 1 : 0] : (accu ? model->k_accu : model->k_bare);
+        cu_check(g_cu.LaunchKernel((CUfunction)k, grid(), 1, 1, tcr ? 256 : model->cta, 1, 1,
+                                   (unsigned)smem, (CUstream)st, args, nullptr),
                  "cuLaunchKernel(stretch)");
     }
 
@@ -476,8 +481,9 @@ struct bay_sampler {
         bay_stretch_params p = make_params(0, 0);
         void* args[] = {&p};
         const unsigned g = (unsigned)((W + per_cta() - 1) / per_cta());
-        cu_check(g_cu.LaunchKernel((CUfunction)model->k_logfn, g, 1, 1, model->cta, 1, 1,
-                                   (unsigned)smem, (CUstream)ctx->stream, args, nullptr),
+        cu_check(g_cu.LaunchKernel((CUfunction)(tcr ? model->k_tr[2] : model->k_logfn), g, 1, 1,
+                                   tcr ? 256 : model->cta, 1, 1, (unsigned)smem,
+                                   (CUstream)ctx->stream, args, nullptr),
                  "cuLaunchKernel(logfn)");
     }
 
@@ -872,6 +878,13 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                         cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                          (int)m->tc_smem, k, dev),
                                  "cuKernelSetAttribute(smem)");
+                    const char* tr[3] = {"bay_tcr_bare", "bay_tcr_accu", "bay_tcr_logfn"};
+                    for (int i = 0; i < 3; ++i) {
+                        cu_check(g_cu.LibraryGetKernel(&m->k_tr[i], m->lib, tr[i]), "GetKernel(tcr)");
+                        cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                         (int)kGemmMaxSmem, m->k_tr[i], dev),
+                                 "cuKernelSetAttribute(smem)");
+                    }
                 }
             }
         } catch (...) {
@@ -934,7 +947,27 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
             }
             s->smem = gemm_smem_bytes(m, s->gemm_rows);
             s->tc = m->tc_g != 0;
-            s->streaming = s->tc || (m->flags & BAY_MODEL_GEMM_STREAMING) || s->smem > kGemmMaxSmem;
+            if (s->tc && !(m->flags & BAY_MODEL_GEMM_STREAMING) && s->gemm_rows <= 256 &&
+                m->gemm_features <= 256) {
+                // resident on the tensor cores when the image, the walker operand and the
+                // proposals fit (layout in bay_stretch_tcr)
+                const uint64_t np = (s->gemm_rows + 15) & ~15ull, kc = (m->gemm_features + 63) / 64;
+                const uint64_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1;
+                const uint64_t img = 2 * kc * np * 128 + np * auxs * 4;
+                // image, 2 kc atoms of 64 walker rows (8 KB), then the proposals and the
+                // reduction scratch -- at least 8 KB, which the M = 128 MMA reads past the
+                // last atom (walker rows 64..127, never read back)
+                const uint64_t tail = std::max<uint64_t>(8192, 64ull * (m->dim | 1u) * 4 + 1024);
+                const uint64_t sm = 1024 + ((img + 1023) & ~1023ull) + 2 * kc * 8192 + tail;
+                if (sm <= kGemmMaxSmem) {
+                    s->tc = false;
+                    s->tcr = true;
+                    s->smem = (size_t)sm;
+                    s->gemm_np = (uint32_t)np;
+                }
+            }
+            s->streaming = s->tc || (!s->tcr && ((m->flags & BAY_MODEL_GEMM_STREAMING) ||
+                                                  s->smem > kGemmMaxSmem));
             if (s->tc) {
                 // rows kernel on the tensor cores: one CTA per SM over (walker groups x
                 // row super-blocks), one wave; super-blocks are whole 128-row tiles
@@ -1025,6 +1058,16 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                     encode_bf16_map(&s->tc_maps.bh, s->s_bh, s->tc_fp, s->tc_wpad);
                     encode_bf16_map(&s->tc_maps.bl, s->s_bl, s->tc_fp, s->tc_wpad);
                 }
+            } else if (s->tcr) {
+                const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
+                const uint32_t kc = (m->gemm_features + 63) / 64;
+                const size_t img = 2ull * kc * s->gemm_np * 128 + (size_t)s->gemm_np * auxs * 4;
+                s->gemm_lay = (float*)c->alloc(img);
+                cuda_check(bay::launch_gemm_tc_image(s->params + s->gemm_base, m->gemm_ld,
+                                                     (uint32_t)s->gemm_rows, m->gemm_features, kc,
+                                                     s->gemm_np, m->gemm_aux_col, m->gemm_aux_len,
+                                                     auxs, s->gemm_lay, c->stream),
+                           "gemm_tc_image");
             } else if (m->form == BAY_FORM_GEMM) {
                 s->gemm_np = (uint32_t)((s->gemm_rows + 63) & ~63ull);
                 const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;

@@ -300,6 +300,46 @@ __global__ void gemm_split(const float* A, uint64_t ld, uint32_t rows, uint32_t 
     }
 }
 
+// Resident tensor-core GEMM form: the matrix as the MMA's B operand -- bf16 hi atoms then
+// lo atoms, each atom [NP rows][64 features] in 128-byte rows with 16-byte unit u of row r
+// stored at unit u ^ (r % 8) -- followed by the rows' aux values [NP][auxs]; rows past
+// `rows` and features past F are zero.
+__global__ void gemm_tc_image(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t KC,
+                              uint32_t NP, uint32_t aux_col, uint32_t aux_len, uint32_t auxs,
+                              unsigned char* img) {
+    const uint64_t n_units = (uint64_t)KC * NP * 8;      // 16-byte units per hi (or lo) block
+    const uint64_t n = n_units + (uint64_t)NP * auxs;
+    const uint64_t lo_off = n_units * 16;
+    float* aux = reinterpret_cast<float*>(img + 2 * lo_off);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < n_units) {
+            const uint32_t c = (uint32_t)(i / ((uint64_t)NP * 8));
+            const uint32_t rem = (uint32_t)(i - (uint64_t)c * NP * 8);
+            const uint32_t r = rem >> 3, u = rem & 7u;
+            unsigned int hw[4], lw[4];
+            for (int q = 0; q < 4; ++q) {
+                unsigned int hh[2], ll[2];
+                for (int j = 0; j < 2; ++j) {
+                    const uint32_t f = c * 64u + u * 8u + 2u * q + j;
+                    const float v = (r < rows && f < F) ? A[(uint64_t)r * ld + f] : 0.0f;
+                    const unsigned short h = bf16_rn(v);
+                    hh[j] = h;
+                    ll[j] = bf16_rn(__fsub_rn(v, __uint_as_float((unsigned int)h << 16)));
+                }
+                hw[q] = hh[0] | (hh[1] << 16);
+                lw[q] = ll[0] | (ll[1] << 16);
+            }
+            const uint64_t off = (uint64_t)c * NP * 128 + (uint64_t)r * 128 + ((u ^ (r & 7u)) << 4);
+            *reinterpret_cast<uint4*>(img + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4*>(img + lo_off + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        } else {
+            const uint64_t e = i - n_units, r = e / auxs, cc = e % auxs;
+            aux[e] = (r < rows && cc < aux_len) ? A[r * ld + aux_col + cc] : 0.0f;
+        }
+    }
+}
+
 __global__ void fill_u32(uint32_t* p, uint32_t v, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -496,6 +536,16 @@ cudaError_t launch_gemm_split(const float* A, uint64_t ld, uint32_t rows, uint32
     const uint64_t n = rows_pad * Fp + rows_pad * auxs;
     gemm_split<<<grid_for(n, 256), 256, 0, s>>>(A, ld, rows, F, Fp, rows_pad, aux_col, aux_len, auxs,
                                                  hi, lo, aux);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_tc_image(const float* A, uint64_t ld, uint32_t rows, uint32_t F,
+                                 uint32_t KC, uint32_t NP, uint32_t aux_col, uint32_t aux_len,
+                                 uint32_t auxs, void* img, cudaStream_t s) {
+    const uint64_t n = (uint64_t)KC * NP * 8 + (uint64_t)NP * auxs;
+    gemm_tc_image<<<grid_for(n, 256), 256, 0, s>>>(A, ld, rows, F, KC, NP, aux_col, aux_len, auxs,
+                                                    static_cast<unsigned char*>(img));
     g_launches++;
     return cudaGetLastError();
 }

@@ -108,6 +108,12 @@ cudaError_t launch_gemm_layout(const float* A, uint64_t ld, uint32_t rows, uint3
 cudaError_t launch_gemm_split(const float* A, uint64_t ld, uint32_t rows, uint32_t F, uint32_t Fp,
                               uint64_t rows_pad, uint32_t aux_col, uint32_t aux_len, uint32_t auxs,
                               unsigned short* hi, unsigned short* lo, float* aux, cudaStream_t s);
+// Resident tensor-core GEMM form: the matrix image (bf16 hi then lo 128B-swizzled
+// K-major atoms [KC][NP rows][64 features], then aux [NP][auxs]); 2 KC NP 128 + 4 NP auxs
+// bytes.
+cudaError_t launch_gemm_tc_image(const float* A, uint64_t ld, uint32_t rows, uint32_t F,
+                                 uint32_t KC, uint32_t NP, uint32_t aux_col, uint32_t aux_len,
+                                 uint32_t auxs, void* img, cudaStream_t s);
 // Per-step ensemble means of `nsteps` accu steps from the stretch kernels' per-CTA sums
 // part[((t*2 + half)*D + d)*G + cta]: means[(ctl->step[1] + t)*D + d] = sum / W, summed
 // in FP64 in (half, cta) order; steps at or past means_cap are dropped.

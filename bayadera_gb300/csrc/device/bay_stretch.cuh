@@ -1122,6 +1122,368 @@ extern "C" __global__ void __launch_bounds__(BAY_TC_THREADS, 1)
 bay_gemm_rows_tc_logfn(bay_stretch_params P, const __grid_constant__ bay_tmaps T) {
     bay_gemm_rows_tc_impl<2>(P, T);
 }
+
+// ---------------------------------------------------------------- GEMM form, tensor cores,
+// resident matrix.  For matrices of at most 256 rows that fit in shared memory with the
+// walker operand (e.g. a precision matrix): one launch per half-step, a CTA per 64
+// walkers (M = 128 MMAs of which lanes 0..63 are read back: small CTAs, four per SM).  The sampler keeps an image of the matrix as the MMA's B operand -- bf16 hi
+// and lo, rows padded to gemm_np (a multiple of 16), K-major in 128-byte-swizzled
+// 64-feature atoms -- followed by the rows' aux values; one bulk copy brings it into
+// shared memory while the CTA draws its proposals.  The proposals' coefficient blocks are
+// split into bf16 hi + lo and written in the same swizzled layout as the A operand; one
+// thread issues the 3 x (features / 16) MMAs (N = gemm_np rows, fp32 accumulators in
+// TMEM); then each walker's row terms are read back from its TMEM lane (two warps per
+// lane group, half of the rows each), summed pairwise with a Kahan carry and combined,
+// and the accept step and write-back follow as in the SIMT form.
+#define BAY_TR_W 64u                                    // walkers per CTA
+#define BAY_TR_ATOM 8192u                               // 64 walkers x 64 bf16 (one atom)
+#define BAY_TR_DPAD (DIM | 1)
+
+__device__ __forceinline__ void bay_tmem_ld8(unsigned int ta, float (&v)[8]) {
+    unsigned int r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                   "=r"(r[6]), "=r"(r[7])
+                 : "r"(ta));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void bay_mma_n(unsigned int d, unsigned long long a, unsigned long long b,
+                                          unsigned int idesc, unsigned int acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(d), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
+}
+
+template <bool ACCU, bool LOGFN_ONLY>
+__device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
+    // Shared memory: [matrix image][A: hi atoms, lo atoms (64 walker rows each)][Yw][red].
+    // The MMA runs M = 128: it also reads the 8 KB after each atom's 64 rows (the next atom,
+    // or Yw and the slack after A's last atom) as walker rows 64..127, whose accumulator
+    // lanes are never read; the host reserves at least 8 KB after the last atom.
+    extern __shared__ __align__(1024) unsigned char bay_smem_tr[];
+    const unsigned int NP = P.gemm_np;                       // rows padded to 16
+    const unsigned int rows = (unsigned int)P.gemm_rows;
+    const unsigned int raw = (unsigned int)__cvta_generic_to_shared(bay_smem_tr);
+    const unsigned int pad = ((raw + 1023u) & ~1023u) - raw;
+    unsigned char* sm = bay_smem_tr + pad;
+    const unsigned int img_bytes = 2u * BAY_TC_KC * NP * 128u + NP * BAY_AUXS * 4u;
+    const unsigned int a_off = (img_bytes + 1023u) & ~1023u;
+    const unsigned int s_img = raw + pad, s_a = s_img + a_off;
+    const float* Aux = (const float*)(sm + 2u * BAY_TC_KC * NP * 128u);     // [NP][AUXS]
+    float* Yw = (float*)(sm + a_off + 2u * BAY_TC_KC * BAY_TR_ATOM);         // [64][DPAD]
+    float* red = Yw + BAY_TR_W * BAY_TR_DPAD;                                // [8][32]
+    __shared__ float sZ[BAY_TR_W], sU2[BAY_TR_W], sW[BAY_TR_W], sLx[BAY_TR_W];
+    __shared__ unsigned int sJ[BAY_TR_W];
+    __shared__ float sPrep[BAY_TR_W][BAY_PREP_LEN];
+    __shared__ float sHalf[BAY_TR_W][2];
+    __shared__ unsigned char sAcc[BAY_TR_W];
+    __shared__ __align__(8) unsigned long long sBar[2];
+    __shared__ unsigned int sTmem, sOk;
+
+    const unsigned int kind = ACCU ? 1u : 0u;
+    const unsigned int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const unsigned int k0 = blockIdx.x * BAY_TR_W;
+    const unsigned int nk = LOGFN_ONLY ? P.W : P.K;
+    const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
+    const unsigned int step = P.ctl->step[kind] + P.step_off;
+    const float* hyper = P.params + P.data_len;
+    float* X = P.xs + (LOGFN_ONLY ? 0 : (size_t)P.half * P.K * DIM);
+    const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM;
+    const unsigned int bar_img = (unsigned int)__cvta_generic_to_shared(&sBar[0]);
+    const unsigned int bar_mma = (unsigned int)__cvta_generic_to_shared(&sBar[1]);
+    unsigned int* status = &P.ctl->status;
+    const unsigned int ncols = NP <= 32u ? 32u : (NP <= 64u ? 64u : (NP <= 128u ? 128u : 256u));
+
+    // 1. barriers, TMEM, and the matrix image's bulk copy (overlaps the proposals)
+    if (tid == 0) {
+        bay_mbar_init(bar_img, 1u);
+        bay_mbar_init(bar_mma, 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        const unsigned int dst = (unsigned int)__cvta_generic_to_shared(&sTmem);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(dst), "r"(ncols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    bay_tc_fence_before();
+    __syncthreads();
+    bay_tc_fence_after();
+    const unsigned int tmem = sTmem;
+    if (tid == 0) {
+        bay_expect_tx(bar_img, img_bytes);
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+            ::"r"(s_img), "l"(P.gemm_lay), "r"(img_bytes), "r"(bar_img) : "memory");
+    }
+    // 2. proposals (Philox, z, partner) of the tile
+    if (!LOGFN_ONLY && tid < nt) {
+        const unsigned int k = k0 + tid;
+        const unsigned int stream = ACCU ? (P.half ? 2222u : 1111u) : (P.half ? 4444u : 3333u);
+        bay_u4 c;
+        c.x = k;
+        c.y = step;
+        c.z = stream;
+        c.w = 0xbeeff00du;
+        const bay_u4 r = bay_philox4x32_10(c, P.ctl->seed[kind] + P.half, 0xdecafbadu);
+        sZ[tid] = bay_stretch_z(P.ctl->a, bay_u01(r.y));
+        sJ[tid] = bay_partner(bay_u01(r.x), P.K);
+        sU2[tid] = bay_u01(r.z);
+        sLx[tid] = P.logfn[(size_t)P.half * P.K + k];
+    }
+    __syncthreads();
+    // 3. Y of the tile (walker-major, odd stride), gathered element-wise (coalesced); each
+    //    thread keeps a batch of its loads in flight before it uses any of them
+    constexpr int NE = (int)((BAY_TR_W * DIM + 255) / 256);   // elements per thread
+    constexpr int CH = 16;
+    {
+        const float* Xt = X + (size_t)k0 * DIM;
+        const unsigned int n_own = nt * DIM;
+#pragma unroll
+        for (int c0 = 0; c0 < NE; c0 += CH) {
+            float xv[CH], sv[CH];
+#pragma unroll
+            for (int i = 0; i < CH; ++i) {
+                const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
+                const unsigned int w = e / DIM, d = e - w * DIM;
+                const bool ev = (c0 + i < NE) && e < n_own;
+                xv[i] = ev ? Xt[e] : 0.0f;
+                sv[i] = (!LOGFN_ONLY && ev) ? S[(size_t)sJ[w] * DIM + d] : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < CH; ++i) {
+                const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
+                if ((c0 + i < NE) && e < BAY_TR_W * DIM) {
+                    const unsigned int w = e / DIM, d = e - w * DIM;
+                    const float y = LOGFN_ONLY ? xv[i]
+                        : (e < n_own ? __fmaf_rn(sZ[w], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
+                    Yw[w * BAY_TR_DPAD + d] = y;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // 4. the A operand: each thread writes 16-byte units (8 features) of hi and lo,
+    //    unit u of walker w at unit u ^ (w % 8) of its 128-byte row (the 128B swizzle)
+    for (unsigned int q = tid; q < BAY_TR_W * BAY_TC_KC * 8u; q += blockDim.x) {
+        const unsigned int w = q / (BAY_TC_KC * 8u), cu = q - w * (BAY_TC_KC * 8u);
+        const unsigned int c = cu >> 3, u = cu & 7u;
+        unsigned int hw[4], lw[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            unsigned int hh[2], ll[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const unsigned int f = c * 64u + u * 8u + 2u * i + j;
+                const float v = f < BAY_GEMM_F ? Yw[w * BAY_TR_DPAD + BAY_GEMM_COEF + f] : 0.0f;
+                const unsigned short h = bay_bf16_rn(v);
+                hh[j] = h;
+                ll[j] = bay_bf16_rn(__fsub_rn(v, bay_bf16_float(h)));
+            }
+            hw[i] = hh[0] | (hh[1] << 16);
+            lw[i] = ll[0] | (ll[1] << 16);
+        }
+        const unsigned int off = c * BAY_TR_ATOM + w * 128u + ((u ^ (w & 7u)) << 4);
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(s_a + off), "r"(hw[0]),
+                     "r"(hw[1]), "r"(hw[2]), "r"(hw[3]) : "memory");
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+                     ::"r"(s_a + BAY_TC_KC * BAY_TR_ATOM + off), "r"(lw[0]), "r"(lw[1]), "r"(lw[2]),
+                     "r"(lw[3]) : "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // A visible to the MMAs
+    __syncthreads();
+    // 5. one thread: wait for the image, issue the MMAs, commit; the others precompute
+    if (tid == 0) {
+        unsigned int ok = bay_tc_wait(bar_img, 0u, nullptr, status) ? 1u : 0u;
+        if (ok) {
+            bay_tc_fence_after();
+            const unsigned int idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((NP >> 3) << 17) |
+                                       ((128u >> 4) << 24);
+            for (unsigned int c = 0; c < BAY_TC_KC; ++c) {
+#pragma unroll
+                for (unsigned int ks = 0; ks < 4u; ++ks) {
+                    const unsigned int ao = c * BAY_TR_ATOM + 32u * ks;
+                    const unsigned int bo = c * NP * 128u + 32u * ks;
+                    const unsigned long long ah = bay_sdesc(s_a + ao);
+                    const unsigned long long al = bay_sdesc(s_a + BAY_TC_KC * BAY_TR_ATOM + ao);
+                    const unsigned long long bh = bay_sdesc(s_img + bo);
+                    const unsigned long long bl = bay_sdesc(s_img + BAY_TC_KC * NP * 128u + bo);
+                    bay_mma_n(tmem, ah, bh, idesc, (c | ks) != 0u ? 1u : 0u);
+                    bay_mma_n(tmem, ah, bl, idesc, 1u);
+                    bay_mma_n(tmem, al, bh, idesc, 1u);
+                }
+            }
+        }
+        bay_mma_commit(bar_mma);   // also arrives with nothing issued (a failed wait)
+        sOk = ok;
+    }
+    if (tid < BAY_TR_W) {
+        float pr[BAY_PREP_LEN];
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) pr[i] = 0.0f;
+        float wt = 0.0f;
+        if (tid < nt) {
+            BAY_GEMM_PREP(hyper, P.params_len, DIM, &Yw[tid * BAY_TR_DPAD], pr);
+            wt = BAY_GEMM_WALKER(P.gemm_rows, hyper, P.params_len, DIM, &Yw[tid * BAY_TR_DPAD]);
+        }
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) sPrep[tid][i] = pr[i];
+        sW[tid] = wt;
+    }
+    // every thread waits for the MMAs (bounded; the commit arrives even if none were issued)
+    // and observes the image copy itself before reading the aux values it brought
+    bay_tc_wait(bar_mma, 0u, nullptr, status);
+    bay_tc_wait(bar_img, 0u, nullptr, status);
+    __syncthreads();
+    bay_tc_fence_after();
+    const bool ok = sOk != 0u;
+    // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
+    //    rows [NP/2 * (w / 4), + NP/2) in 8-column loads; the two halves then combine
+    if ((warp & 3u) < 2u) {
+        const unsigned int wl = 32u * (warp & 3u) + lane;
+        const unsigned int h = warp >> 2, half_rows = NP >> 1;
+        const unsigned int c0 = h * half_rows;
+        const unsigned int ta = tmem + ((32u * (warp & 3u)) << 16) + c0;
+        const float* xw = &Yw[wl * BAY_TR_DPAD];
+        float sum = 0.0f, cmp = 0.0f;
+        for (unsigned int j0 = 0; j0 < half_rows; j0 += 8u) {
+            float v[8];
+            bay_tmem_ld8(ta + j0, v);
+#pragma unroll
+            for (unsigned int i = 0; i < 8u; ++i) {
+                const unsigned int r = c0 + j0 + i;
+                v[i] = r < rows ? BAY_GEMM_TERM(v[i], &Aux[r * BAY_AUXS], (uint64_t)r, xw, sPrep[wl]) : 0.0f;
+            }
+#pragma unroll
+            for (unsigned int s2 = 4u; s2 >= 1u; s2 >>= 1)
+#pragma unroll
+                for (unsigned int i = 0; i < s2; ++i) v[i] = __fadd_rn(v[i], v[i + s2]);
+            const float yk = __fsub_rn(v[0], cmp);
+            const float t = __fadd_rn(sum, yk);
+            cmp = __fsub_rn(__fsub_rn(t, sum), yk);
+            sum = t;
+        }
+        if (h) {                                        // second half of the rows
+            sHalf[wl][0] = sum;
+            sHalf[wl][1] = -cmp;
+        } else {                                        // first half: red[wl], red[64 + wl]
+            red[wl] = sum;
+            red[64u + wl] = -cmp;
+        }
+    }
+    bay_tc_fence_before();
+    __syncthreads();
+    // 7. accept (one thread per walker), write-back, statistics
+    bool accepted = false;
+    if (tid < nt && ok) {
+        const unsigned int k = k0 + tid;
+        bay_cf t, a, b;
+        t.hi = sW[tid];
+        t.lo = 0.0f;
+        a.hi = red[tid];
+        a.lo = red[64u + tid];
+        b.hi = sHalf[tid][0];
+        b.lo = sHalf[tid][1];
+        t = bay_cadd(t, bay_cadd(a, b));
+        const float ly = __fadd_rn(t.hi, t.lo);
+        if (LOGFN_ONLY) {
+            P.logfn[k] = ly;
+        } else {
+            accepted = bay_accept(sU2[tid], sZ[tid], ly, sLx[tid], ACCU ? 1.0f : P.ctl->beta);
+            if (accepted) P.logfn[(size_t)P.half * P.K + k] = ly;
+        }
+    }
+    if (!LOGFN_ONLY) {
+        if (tid < BAY_TR_W) sAcc[tid] = accepted ? 1 : 0;
+        const int n_acc = __syncthreads_count(accepted);
+        float* Xt = X + (size_t)k0 * DIM;
+        if (ACCU) {
+            // the statistics need every walker's new position in Yw: the rejected walkers'
+            // current rows are loaded in batches (all in flight), the accepted ones stored
+#pragma unroll
+            for (int c0 = 0; c0 < NE; c0 += CH) {
+                float xv[CH];
+#pragma unroll
+                for (int i = 0; i < CH; ++i) {
+                    const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
+                    const bool ev = (c0 + i < NE) && e < nt * DIM && !sAcc[e / DIM];
+                    xv[i] = ev ? Xt[e] : 0.0f;
+                }
+#pragma unroll
+                for (int i = 0; i < CH; ++i) {
+                    const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
+                    if ((c0 + i < NE) && e < nt * DIM) {
+                        const unsigned int w = e / DIM, d = e - w * DIM;
+                        if (sAcc[w]) Xt[e] = Yw[w * BAY_TR_DPAD + d];
+                        else Yw[w * BAY_TR_DPAD + d] = xv[i];
+                    }
+                }
+            }
+            if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
+            if (P.means_cap != 0) {
+                __syncthreads();
+                // per-dim sums of the tile's new positions: warp q sums walkers 8 q .. 8 q + 7
+                // of 32 dims (one per lane) in fp32, then the 8 warps combine as compensated
+                // pairs in warp order
+                float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x
+                    + blockIdx.x;
+                for (unsigned int d0 = 0; d0 < DIM; d0 += 32u) {
+                    const unsigned int d = d0 + lane;
+                    float v = 0.0f;
+                    if (d < DIM) {
+#pragma unroll
+                        for (unsigned int i = 0; i < 8u; ++i) {
+                            const unsigned int w = 8u * warp + i;
+                            if (w < nt) v = __fadd_rn(v, Yw[w * BAY_TR_DPAD + d]);
+                        }
+                    }
+                    red[warp * 32u + lane] = v;
+                    __syncthreads();
+                    if (tid < 32u && d0 + tid < DIM) {
+                        bay_cf a;
+                        a.hi = 0.0f;
+                        a.lo = 0.0f;
+                        for (unsigned int q = 0; q < blockDim.x / 32u; ++q) {
+                            bay_cf b;
+                            b.hi = red[q * 32u + tid];
+                            b.lo = 0.0f;
+                            a = bay_cadd(a, b);
+                        }
+                        out[(size_t)(d0 + tid) * gridDim.x] = __fadd_rn(a.hi, a.lo);
+                    }
+                    __syncthreads();
+                }
+            }
+        } else {
+            for (unsigned int e = tid; e < nt * DIM; e += blockDim.x) {
+                const unsigned int w = e / DIM;
+                if (sAcc[w]) Xt[e] = Yw[w * BAY_TR_DPAD + (e - w * DIM)];
+            }
+        }
+    }
+    // 8. release TMEM (every MMA completed before the epilogue read it)
+    if (warp == 0) {
+        __syncwarp();
+        bay_tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(ncols) : "memory");
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) bay_tcr_bare(bay_stretch_params P) {
+    bay_stretch_tcr<false, false>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_tcr_accu(bay_stretch_params P) {
+    bay_stretch_tcr<true, false>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_tcr_logfn(bay_stretch_params P) {
+    bay_stretch_tcr<false, true>(P);
+}
 #endif  // BAY_GEMM_TC
 
 #elif !BAY_TILED

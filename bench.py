@@ -114,7 +114,7 @@ def measured_peaks():
 
 def profile_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "stretch_gemm_mvn50.txt")
+    p = os.path.join(ROOT, "profiles", "stretch_tcr_mvn50.txt")
     if not os.path.exists(p):
         return None
     for ln in open(p):
@@ -175,7 +175,8 @@ def run_reference(args):
 def config():
     return {"workload": "mvn50-ar1 (50-D correlated Gaussian, rho 0.9, scales log-U[0.1,10])",
             "dim": DIM, "walkers": WALKERS, "burn_in": BURN, "run": RUN, "bins": BINS,
-            "model_form": "gemm (64-walker tiles, x'Px register-blocked from shared memory)",
+            "model_form": "gemm on the tensor cores (128-walker tiles, x'Px as a tcgen05 "
+                          "split-bf16 product, fp32 accumulation, resident precision matrix)",
             "l2": "flushed between timed steps (256 MiB device write)",
             "parallelism": "replicas"}
 
@@ -538,7 +539,8 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     f = GB300BayaderaFactory(device=local, wgs=1024, stream=stream.cuda_stream)
     model = M.mvn_precision_model(DIM)
-    sfs = {"gemm": f.mcmc_factory(model, form="gemm"),
+    sfs = {"tensor": f.mcmc_factory(model, form="gemm", tensor=True),
+           "gemm": f.mcmc_factory(model, form="gemm"),
            "plain": f.mcmc_factory(model, form="plain")}
     seed_base = 1000 * (rank + 1)
 
@@ -583,12 +585,18 @@ def main():
             t_total = float(t.item())
         return WALKERS * (BURN + RUN) * steps * world / t_total, t_total, results
 
-    # headline: the GEMM form (walker tiles, shared-memory register-blocked x'Px)
-    samp = sfs["gemm"].create_sampler(seed_base, WALKERS, dP)
+    # headline: the GEMM form on the tensor cores (128-walker tiles, x'Px as a split-bf16
+    # tcgen05 product against the resident precision matrix)
+    samp = sfs["tensor"].create_sampler(seed_base, WALKERS, dP)
     launches0 = _native.launch_count()
     with ClockSampler(local) as clocks:
         value, t_total, results = timed_jobs(samp, args.steps, args.warmup)
     launches = _native.launch_count() - launches0
+
+    # the fp32 SIMT GEMM form (64-walker tiles, register-blocked x'Px from shared memory)
+    samp_gemm = sfs["gemm"].create_sampler(seed_base, WALKERS, dP)
+    gemm_value, _, _ = timed_jobs(samp_gemm, max(1, min(args.steps, 2)), 1)
+    samp_gemm.release()
 
     # the plain FP32 form (one thread per walker, the reference's kernel structure)
     samp_plain = sfs["plain"].create_sampler(seed_base, WALKERS, dP)
@@ -619,7 +627,7 @@ def main():
     for k in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s2 = sfs["gemm"].create_sampler(seed_base + 31 * k, WALKERS, P.reshape(-1))
+        s2 = sfs["tensor"].create_sampler(seed_base + 31 * k, WALKERS, P.reshape(-1))
         res, mean, var, hist = job(s2, seed_base + 31 * k)
         s2.release()
         e2e_times.append(time.perf_counter() - t0)
@@ -631,8 +639,11 @@ def main():
     res, mean, var, hist = results
     ac = res["autocorrelation"]
     within = None
+    err_sd = None
     if ac is not None:
         within = int(np.sum(np.abs(ac.mean) <= 3 * ac.sigma))
+        # the run mean's distance from the analytic mean 0, in posterior standard deviations
+        err_sd = float(np.max(np.abs(ac.mean) / np.sqrt(np.diag(sigma))))
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -651,16 +662,18 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                         "peak_kind": peak_kind, "kernel": "bay_stretch_bare (GEMM form)",
+                         "peak_kind": peak_kind,
+                         "kernel": "bay_tcr_bare (GEMM form on the tensor cores, resident matrix)",
                          "launch_us": t_launch * 1e6,
                          "fp32_tflops": flop_launch / t_launch / 1e12},
             "cpu_baseline": cpu,
-            "forms": {"gemm": value, "plain_fp32": plain_value,
+            "forms": {"tensor": value, "gemm_fp32_simt": gemm_value, "plain_fp32": plain_value,
                       "speedup_vs_plain": value / plain_value},
             "clocks": clocks.summary(),
             "result": {"acceptance_rate": res["acceptance_rate"],
                        "tau_max": float(np.max(ac.tau)) if ac is not None else None,
-                       "means_within_3se": within, "dims": DIM},
+                       "means_within_3se": within, "dims": DIM,
+                       "max_abs_mean_over_posterior_sd": err_sd},
         }
         print(json.dumps(line))
     samp.release()

@@ -92,12 +92,16 @@ def sixteen_bit(rng, shape, scale):
 
 
 @pytest.mark.parametrize("rows,F,W", [(1000, 64, 512), (300, 7, 200), (777, 130, 260),
-                                      (128, 256, 256), (200, 320, 130), (5000, 64, 1024)])
+                                      (128, 256, 256), (200, 320, 130), (5000, 64, 1024),
+                                      (50, 50, 512), (100, 7, 258), (256, 64, 130),
+                                      (16, 130, 200)])
 def test_tc_eta_exact_split_products(factory, M, rows, F, W):
     """Linear row term (term = eta_r w_r): with every factor exact in bf16 hi + lo the
     kernel must equal sum_r w_r sum_f (xh bh + xh bl + xl bh) up to fp32 accumulation.
-    Covers rows and walkers not multiples of the 128 tiles, features padded to 64,
-    one and two walker sub-tiles per CTA and 1..5 feature chunks."""
+    Streamed form (rows > 256 or a large operand): rows and walkers not multiples of the
+    128 tiles, features padded to 64, one and two walker sub-tiles per CTA, 1..5 feature
+    chunks.  Resident form (the last four: rows <= 256, one launch per half-step): N =
+    rows padded to 16, 1..3 feature atoms, partial walker tiles."""
     rng = np.random.default_rng(rows + F)
     X = sixteen_bit(rng, (rows, F), 1.0)
     w = sixteen_bit(rng, rows, 1.0)
@@ -242,3 +246,57 @@ def test_tc_rejects_too_many_features(factory, M):
     from bayadera_gb300._native import BayaderaError
     with pytest.raises(BayaderaError, match="320 features"):
         factory.mcmc_factory(M.logistic_model(384), form="gemm", tensor=True)
+
+
+def test_tcr_mvn_logfn_and_moves(factory, M, oracle):
+    """Resident tensor-core form on a 50-D Gaussian (precision matrix as the MMA's B
+    operand): log densities of the initial and moved walkers against the oracle's FP64
+    density within the split-bf16 bound (term = -x_r eta_r / 2), and the same moves as
+    the fp32 SIMT resident form except for marginal accept decisions."""
+    D, W = 50, 2048
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(D, D))
+    P = (A @ A.T / D + np.eye(D)).astype(np.float32)
+    out = []
+    for tensor in (True, False):
+        sf = factory.mcmc_factory(M.mvn_precision_model(D), form="gemm", tensor=tensor)
+        s = sf.create_sampler(11, W, P.reshape(-1))
+        s.init_position_normal(3, 0.0, 1.0)
+        for phase in range(2):
+            if tensor:
+                pos = s.positions().T.astype(np.float64)
+                lf = s.logfn().astype(np.float64)
+                idx = np.arange(0, W, 32)
+                want = np.array([oracle.logfn64("mvn_precision", P.reshape(-1), 0, D, pos[i])
+                                 for i in idx])
+                x = pos[idx]
+                mag = 0.5 * np.sum(np.abs(x) * (np.abs(x) @ np.abs(P.astype(np.float64)).T), axis=1)
+                tol = (2.0 ** -15 + 4 * D * 2.0 ** -24) * mag + 1e-5 * np.abs(want) + 1e-5
+                err = np.abs(lf[idx] - want)
+                assert np.all(err <= tol), (phase, (err / tol).max())
+            s.burn_in(2, 2.0)
+        out.append(s.positions().copy())
+        s.release()
+        sf.release()
+    differ = np.any(out[0] != out[1], axis=0).sum()
+    assert differ <= W // 25, differ
+
+
+def test_tcr_run_sampler_matches_simt(factory, M):
+    """Resident tensor-core accu path: acceptance rate within 3 binomial s.e. of the SIMT
+    form's, per-step means (last = mean of the walkers)."""
+    D, W = 10, 4096
+    P = np.diag(np.linspace(0.5, 2.0, D)).astype(np.float32)
+    rates = {}
+    for tensor in (True, False):
+        sf = factory.mcmc_factory(M.mvn_precision_model(D), form="gemm", tensor=tensor)
+        s = sf.create_sampler(17, W, P.reshape(-1))
+        s.init_position_normal(2, 0.0, 1.0)
+        s.burn_in(100, 2.0)
+        r = s.run_sampler(200, 2.0, return_means=True)
+        np.testing.assert_allclose(r["means"][:, -1], s.mean(), rtol=1e-5, atol=1e-6)
+        rates[tensor] = r["acceptance_rate"]
+        s.release()
+        sf.release()
+    a = rates[False]
+    assert abs(rates[True] - a) <= 3 * np.sqrt(2 * a * (1 - a) / (W * 200)) + 0.005
