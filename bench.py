@@ -183,7 +183,7 @@ def config():
 
 # ------------------------------------------------------------------ other workloads
 # (measured with --config; the default line above is the 50-D Gaussian job)
-def _workload(name):
+def _workload(name, rows=0):
     """(model factory args, params builder, walkers, burn, run, bins, init, algorithmic
     FLOP and bytes per walker-step, description) of the other benchmark workloads."""
     import torch
@@ -199,7 +199,7 @@ def _workload(name):
                     desc="2-D Gaussian (mu, sigma) posterior, N=10,000 data, prior "
                          "N(0,10^2) x U(0,20)")
     if name == "c3":
-        n, F = 1 << 20, 64
+        n, F = rows or (1 << 20), 64
         rng = np.random.default_rng(0)
         X = rng.standard_normal((n, F), dtype=np.float32)
         beta = rng.normal(0.0, 1.0 / 8.0, F)
@@ -218,7 +218,7 @@ def _workload(name):
                     desc="Bayesian logistic regression, X 1,048,576 x 64 N(0,1), beta* ~ "
                          "N(0,1/64), prior N(0,5^2 I)")
     if name == "c5":
-        n, F = 1 << 24, 256
+        n, F = rows or (1 << 24), 256
         rng = np.random.default_rng(0)
         scale = np.exp(rng.uniform(np.log(0.01), np.log(100.0), F)).astype(np.float32)
         beta = (rng.normal(0.0, 1.0, F) / (scale * 16.0)).astype(np.float32)
@@ -255,7 +255,9 @@ def run_config(args):
     from bayadera_gb300 import _native
     from bayadera_gb300.engine import GB300BayaderaFactory
     torch.cuda.set_device(0)
-    wl = _workload(args.config)
+    wl = _workload(args.config, args.rows)
+    if args.rows:
+        wl["desc"] += " [profiling case: %d rows]" % args.rows
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     f = GB300BayaderaFactory(device=0, wgs=1024, stream=stream.cuda_stream)
@@ -506,6 +508,9 @@ def main():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default): the 50-D Gaussian job; c1, c3, c5: the other "
                          "benchmark workloads, measured GEMM/tiled form vs plain form")
+    ap.add_argument("--rows", type=int, default=0,
+                    help="with --config c3 or c5: data rows instead of the configuration's "
+                         "(a smaller case for profiling); the line then names the row count")
     ap.add_argument("--forms", default="",
                     help="with --config: comma-separated subset of the forms to run "
                          "(tensor, gemm, tiled, plain), e.g. for a profile of one form")
