@@ -492,6 +492,14 @@ __device__ __forceinline__ unsigned short bay_bf16_rn(float x) {
 __device__ __forceinline__ float bay_bf16_float(unsigned short h) {
     return __uint_as_float((unsigned int)h << 16);
 }
+// Two floats as packed bf16 hi + lo pairs (a in the low halves, b in the high halves), each
+// rounded to nearest even by one cvt.rn.bf16x2.f32: hi = bf16(x), lo = bf16(x - hi).
+__device__ __forceinline__ void bay_split_bf16x2(float a, float b, unsigned int& hi,
+                                                 unsigned int& lo) {
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(b), "f"(a));
+    const float ha = __uint_as_float(hi << 16), hb = __uint_as_float(hi & 0xffff0000u);
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(__fsub_rn(b, hb)), "f"(__fsub_rn(a, ha)));
+}
 
 template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions
 __device__ __forceinline__ void bay_gemm_propose_impl(const bay_stretch_params& P) {
@@ -1247,22 +1255,23 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
 #pragma unroll
         for (int c0 = 0; c0 < NE; c0 += CH) {
             float xv[CH], sv[CH];
+            unsigned int wv[CH], dv[CH];
 #pragma unroll
             for (int i = 0; i < CH; ++i) {
                 const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
-                const unsigned int w = e / DIM, d = e - w * DIM;
+                wv[i] = e / DIM;
+                dv[i] = e - wv[i] * DIM;
                 const bool ev = (c0 + i < NE) && e < n_own;
                 xv[i] = ev ? Xt[e] : 0.0f;
-                sv[i] = (!LOGFN_ONLY && ev) ? S[(size_t)sJ[w] * DIM + d] : 0.0f;
+                sv[i] = (!LOGFN_ONLY && ev) ? S[(size_t)sJ[wv[i]] * DIM + dv[i]] : 0.0f;
             }
 #pragma unroll
             for (int i = 0; i < CH; ++i) {
                 const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
                 if ((c0 + i < NE) && e < BAY_TR_W * DIM) {
-                    const unsigned int w = e / DIM, d = e - w * DIM;
                     const float y = LOGFN_ONLY ? xv[i]
-                        : (e < n_own ? __fmaf_rn(sZ[w], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
-                    Yw[w * BAY_TR_DPAD + d] = y;
+                        : (e < n_own ? __fmaf_rn(sZ[wv[i]], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
+                    Yw[wv[i] * BAY_TR_DPAD + dv[i]] = y;
                 }
             }
         }
@@ -1276,17 +1285,10 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
         unsigned int hw[4], lw[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            unsigned int hh[2], ll[2];
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const unsigned int f = c * 64u + u * 8u + 2u * i + j;
-                const float v = f < BAY_GEMM_F ? Yw[w * BAY_TR_DPAD + BAY_GEMM_COEF + f] : 0.0f;
-                const unsigned short h = bay_bf16_rn(v);
-                hh[j] = h;
-                ll[j] = bay_bf16_rn(__fsub_rn(v, bay_bf16_float(h)));
-            }
-            hw[i] = hh[0] | (hh[1] << 16);
-            lw[i] = ll[0] | (ll[1] << 16);
+            const unsigned int f = c * 64u + u * 8u + 2u * i;
+            const float v0 = f < BAY_GEMM_F ? Yw[w * BAY_TR_DPAD + BAY_GEMM_COEF + f] : 0.0f;
+            const float v1 = f + 1u < BAY_GEMM_F ? Yw[w * BAY_TR_DPAD + BAY_GEMM_COEF + f + 1u] : 0.0f;
+            bay_split_bf16x2(v0, v1, hw[i], lw[i]);
         }
         const unsigned int off = c * BAY_TR_ATOM + w * 128u + ((u ^ (w & 7u)) << 4);
         asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(s_a + off), "r"(hw[0]),
@@ -1428,8 +1430,8 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             if (P.means_cap != 0) {
                 __syncthreads();
                 // per-dim sums of the tile's new positions: warp q sums walkers 8 q .. 8 q + 7
-                // of 32 dims (one per lane) in fp32, then the 8 warps combine as compensated
-                // pairs in warp order
+                // of 32 dims (one per lane) in fp32, then the 8 warps' sums in warp order
+                // (64 terms in all; the per-step means add the CTAs' sums in FP64)
                 float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x
                     + blockIdx.x;
                 for (unsigned int d0 = 0; d0 < DIM; d0 += 32u) {
@@ -1445,16 +1447,10 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                     red[warp * 32u + lane] = v;
                     __syncthreads();
                     if (tid < 32u && d0 + tid < DIM) {
-                        bay_cf a;
-                        a.hi = 0.0f;
-                        a.lo = 0.0f;
-                        for (unsigned int q = 0; q < blockDim.x / 32u; ++q) {
-                            bay_cf b;
-                            b.hi = red[q * 32u + tid];
-                            b.lo = 0.0f;
-                            a = bay_cadd(a, b);
-                        }
-                        out[(size_t)(d0 + tid) * gridDim.x] = __fadd_rn(a.hi, a.lo);
+                        float a = 0.0f;
+#pragma unroll
+                        for (unsigned int q = 0; q < 8u; ++q) a = __fadd_rn(a, red[q * 32u + tid]);
+                        out[(size_t)(d0 + tid) * gridDim.x] = a;
                     }
                     __syncthreads();
                 }
