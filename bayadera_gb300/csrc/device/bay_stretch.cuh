@@ -1249,6 +1249,10 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     //    thread keeps a batch of its loads in flight before it uses any of them
     constexpr int NE = (int)((BAY_TR_W * DIM + 255) / 256);   // elements per thread
     constexpr int CH = 16;
+    // accu with one batch of gathered elements per thread: the current rows stay in
+    // registers and are parked in the A region once the MMAs are done (no reload)
+    constexpr bool KEEPX = ACCU && NE <= CH;
+    float xkeep[CH];
     {
         const float* Xt = X + (size_t)k0 * DIM;
         const unsigned int n_own = nt * DIM;
@@ -1273,6 +1277,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                         : (e < n_own ? __fmaf_rn(sZ[wv[i]], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
                     Yw[wv[i] * BAY_TR_DPAD + dv[i]] = y;
                 }
+                if (KEEPX) xkeep[i] = xv[i];
             }
         }
     }
@@ -1344,6 +1349,17 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     __syncthreads();
     bay_tc_fence_after();
     const bool ok = sOk != 0u;
+    float* Xa = (float*)(sm + a_off);   // [64][DPAD] current rows, in the A region (free now)
+    if (KEEPX) {
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+            const unsigned int e = tid + 256u * (unsigned int)i;
+            if (i < NE && e < nt * DIM) {
+                const unsigned int w = e / DIM;
+                Xa[w * BAY_TR_DPAD + (e - w * DIM)] = xkeep[i];
+            }
+        }
+    }
     // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
     //    rows [NP/2 * (w / 4), + NP/2) in 8-column loads; the two halves then combine
     if ((warp & 3u) < 2u) {
@@ -1404,7 +1420,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
         if (tid < BAY_TR_W) sAcc[tid] = accepted ? 1 : 0;
         const int n_acc = __syncthreads_count(accepted);
         float* Xt = X + (size_t)k0 * DIM;
-        if (ACCU) {
+        if (ACCU && !KEEPX) {
             // the statistics need every walker's new position in Yw: the rejected walkers'
             // current rows are loaded in batches (all in flight), the accepted ones stored
 #pragma unroll
@@ -1426,6 +1442,15 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                     }
                 }
             }
+        } else {
+            // accepted walkers' rows to device memory (KEEPX: the current rows of the
+            // rejected ones are already in Xa)
+            for (unsigned int e = tid; e < nt * DIM; e += blockDim.x) {
+                const unsigned int w = e / DIM;
+                if (sAcc[w]) Xt[e] = Yw[w * BAY_TR_DPAD + (e - w * DIM)];
+            }
+        }
+        if (ACCU) {
             if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
             if (P.means_cap != 0) {
                 __syncthreads();
@@ -1441,7 +1466,8 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
 #pragma unroll
                         for (unsigned int i = 0; i < 8u; ++i) {
                             const unsigned int w = 8u * warp + i;
-                            if (w < nt) v = __fadd_rn(v, Yw[w * BAY_TR_DPAD + d]);
+                            if (w < nt) v = __fadd_rn(v, (KEEPX && !sAcc[w]) ? Xa[w * BAY_TR_DPAD + d]
+                                                                            : Yw[w * BAY_TR_DPAD + d]);
                         }
                     }
                     red[warp * 32u + lane] = v;
@@ -1454,11 +1480,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                     }
                     __syncthreads();
                 }
-            }
-        } else {
-            for (unsigned int e = tid; e < nt * DIM; e += blockDim.x) {
-                const unsigned int w = e / DIM;
-                if (sAcc[w]) Xt[e] = Yw[w * BAY_TR_DPAD + (e - w * DIM)];
             }
         }
     }

@@ -282,10 +282,12 @@ def test_tcr_mvn_logfn_and_moves(factory, M, oracle):
     assert differ <= W // 25, differ
 
 
-def test_tcr_run_sampler_matches_simt(factory, M):
+@pytest.mark.parametrize("D", [10, 80])
+def test_tcr_run_sampler_matches_simt(factory, M, D):
     """Resident tensor-core accu path: acceptance rate within 3 binomial s.e. of the SIMT
-    form's, per-step means (last = mean of the walkers)."""
-    D, W = 10, 4096
+    form's, per-step means (last = mean of the walkers).  D = 10 keeps the tile's current
+    rows in registers for the statistics; D = 80 reloads them."""
+    W = 4096
     P = np.diag(np.linspace(0.5, 2.0, D)).astype(np.float32)
     rates = {}
     for tensor in (True, False):
