@@ -23,6 +23,10 @@ FORM_BATCH = 3
 MODEL_ACCEPT_REF = 1
 MODEL_GEMM_STREAMING = 2
 MODEL_GEMM_TENSOR = 4
+DIRECT_UNIFORM = 0
+DIRECT_GAUSSIAN = 1
+DIRECT_EXPONENTIAL = 2
+DIRECT_ERLANG = 3
 HIST_COMPAT_START1 = 1
 HIST_COMPAT_ZERO_LIMITS = 2
 
@@ -116,6 +120,10 @@ _SIGNATURES = {
     "bay_state_import": (C.c_int, [P, P, P, P]),
     "bay_logfn_values": (C.c_int, [P, P]),
     "bay_sampler_set_graphs": (C.c_int, [P, C.c_int]),
+    "bay_sample_direct": (C.c_int, [P, C.c_uint32, P, C.c_uint32, C.c_uint64, P]),
+    "bay_log_density": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
+    "bay_density": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
+    "bay_evidence": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, C.POINTER(C.c_double)]),
     "bay_batch_create": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32, C.POINTER(P)]),
     "bay_batch_release": (C.c_int, [P]),
     "bay_batch_init_position_normal": (C.c_int, [P, P, C.c_float, C.c_float]),

@@ -142,3 +142,32 @@ def histogram(x, cycles=1, bins=0, flags=0):
 def histogram_(x, n):
     """histogram! (core.clj:145-147)."""
     return x.histogram(n)
+
+
+def log_density(dist, x):
+    """log-density (core.clj:105-113): the distribution's logpdf at the points x (n x dim)."""
+    eng = dist.factory.distribution_engine(dist.model)
+    try:
+        return eng.log_density(dist.params, x)
+    finally:
+        eng.release()
+
+
+def density(dist, x):
+    """density (core.clj:105-113)."""
+    eng = dist.factory.distribution_engine(dist.model)
+    try:
+        return eng.density(dist.params, x)
+    finally:
+        eng.release()
+
+
+def evidence(factory, likelihood, data, x):
+    """evidence (core.clj:115-121): the mean likelihood of data over the points x (n x dim),
+    e.g. samples of the prior."""
+    x = np.asarray(x, np.float32)
+    eng = _factory(factory).likelihood_engine(likelihood, x.shape[-1])
+    try:
+        return eng.evidence(data, x)
+    finally:
+        eng.release()

@@ -139,6 +139,9 @@ struct bay_ctx {
     uint64_t allocated = 0;
     std::recursive_mutex mu;
     std::map<void*, size_t> sizes;
+    // the direct samplers' NVRTC module, compiled on first use
+    CUlibrary direct_lib = nullptr;
+    CUkernel k_direct = nullptr;
 
     void* alloc(size_t bytes) {
         if (bytes == 0) bytes = 16;
@@ -188,6 +191,8 @@ struct bay_model {
     // batch form: propose / accept in k_gp / k_ga, rows in k_gr, per-step means here
     CUkernel k_bmeans = nullptr;
     uint32_t row_len = 0;
+    // plain form: the density engines' point kernels
+    CUkernel k_points = nullptr, k_evidence = nullptr;
 };
 
 namespace {
@@ -640,6 +645,7 @@ int bay_ctx_release(bay_ctx* c) {
         c->use();
         cudaStreamSynchronize(c->stream);
         for (auto& kv : c->sizes) cudaFree(kv.first);
+        if (c->direct_lib) g_cu.LibraryUnload(c->direct_lib);
         if (c->own_stream) cudaStreamDestroy(c->stream);
         cudaStreamDestroy(c->capture);
         delete c;
@@ -852,6 +858,12 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                 cu_check(g_cu.LibraryGetKernel(&m->k_bare, m->lib, "bay_stretch_bare"), "GetKernel(bare)");
                 cu_check(g_cu.LibraryGetKernel(&m->k_accu, m->lib, "bay_stretch_accu"), "GetKernel(accu)");
                 cu_check(g_cu.LibraryGetKernel(&m->k_logfn, m->lib, "bay_logfn_all"), "GetKernel(logfn)");
+                if (d->form == BAY_FORM_PLAIN) {
+                    cu_check(g_cu.LibraryGetKernel(&m->k_points, m->lib, "bay_points_logfn"),
+                             "GetKernel(points)");
+                    cu_check(g_cu.LibraryGetKernel(&m->k_evidence, m->lib, "bay_points_evidence"),
+                             "GetKernel(evidence)");
+                }
             }
             if (d->form == BAY_FORM_GEMM) {
                 const char* gp[3] = {"bay_gemm_propose_bare", "bay_gemm_propose_accu",
@@ -1653,3 +1665,4 @@ int bay_logfn_values(bay_sampler* s, float* out) {
 }  // extern "C"
 
 #include "bay_batch_api.inc"
+#include "bay_engines_api.inc"

@@ -1571,6 +1571,47 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
     P.logfn[k] = BAY_LOGFN((unsigned int)P.data_len, P.params_len, P.params, DIM, x);
 }
 
+// Density engines (reference cuda/engines/nvidia-gtx-distribution.cu logpdf/pdf and
+// nvidia-gtx-likelihood.cu loglik/lik): the model's density at n points, x dim x n
+// column-major (point i's coordinates contiguous); exp_out selects the density itself.
+extern "C" __global__ void __launch_bounds__(BAY_CTA)
+bay_points_logfn(unsigned long long n, unsigned int data_len, unsigned int params_len,
+                 const float* params, const float* x, float* out, unsigned int exp_out) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        float p[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p[d] = x[i * DIM + d];
+        const float v = BAY_LOGFN(data_len, params_len, params, DIM, p);
+        out[i] = exp_out ? expf(v) : v;
+    }
+}
+
+// Evidence (nvidia-gtx-likelihood.cu evidence_reduce): per-CTA FP64 sums of exp(density)
+// over the points, each thread's points in order, then a fixed-order tree -> part[cta].
+extern "C" __global__ void __launch_bounds__(BAY_CTA)
+bay_points_evidence(unsigned long long n, unsigned int data_len, unsigned int params_len,
+                    const float* params, const float* x, double* part) {
+    __shared__ double red[BAY_CTA];
+    double s = 0.0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        float p[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) p[d] = x[i * DIM + d];
+        s += (double)expf(BAY_LOGFN(data_len, params_len, params, DIM, p));
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (unsigned int o = 512; o > 0; o >>= 1) {   // BAY_CTA: any multiple of 32 <= 1024
+        if (o < BAY_CTA) {
+            if (threadIdx.x < o && threadIdx.x + o < BAY_CTA) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
 #else
 // ---------------------------------------------------------------- tiled form
 // A CTA owns BAY_WPC walkers; all its threads sweep the data rows, each row read

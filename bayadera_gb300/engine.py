@@ -102,6 +102,28 @@ class GB300BayaderaFactory:
     def acor(self, data_matrix):
         return self.acor_engine.acor(data_matrix)
 
+    # ------------------------------------------------------------ engines (EngineFactory)
+    def distribution_engine(self, model):
+        """distribution-engine (protocols.clj:132-138): log-density / density of the model's
+        logpdf at points."""
+        return GB300DensityEngine(self, model)
+
+    def likelihood_engine(self, likelihood, dim):
+        """likelihood-engine: log-density / density / evidence of a likelihood model at
+        points of dimension dim (data = the params)."""
+        return GB300DensityEngine(self, likelihood, dim=dim)
+
+    def direct_sample(self, kind, seed, params, n):
+        """direct-sampler-engine sample: n samples (a multiple of 4) of uniform, gaussian,
+        exponential or erlang with the given parameters."""
+        kinds = {"uniform": N.DIRECT_UNIFORM, "gaussian": N.DIRECT_GAUSSIAN,
+                 "exponential": N.DIRECT_EXPONENTIAL, "erlang": N.DIRECT_ERLANG}
+        p = np.ascontiguousarray(params, np.float32)
+        out = np.zeros(int(n), np.float32)
+        N.call("bay_sample_direct", self.ctx, kinds[kind], _ptr(p), int(seed) & 0xffffffff,
+               int(n), _ptr(out))
+        return out
+
 
 def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0,
                streaming=False, tensor=False):
@@ -166,6 +188,70 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
     else:
         d.form = N.FORM_PLAIN
     return d, keep
+
+
+_LIK_ADAPTER = """
+extern "C" {
+inline REAL %(name)s(const uint32_t data_len, const uint32_t params_len, const REAL* params,
+                     const uint32_t dim, const REAL* x) {
+    return %(loglik)s(data_len, params, dim, x);
+}
+}
+"""
+
+
+class GB300DensityEngine:
+    """DensityEngine / LikelihoodEngine (protocols.clj:59-72) of a distribution model (its
+    logpdf) or of a likelihood model (its loglik through a 5-argument adapter, points of
+    dimension dim), compiled in the plain form."""
+
+    def __init__(self, factory, model, dim=None):
+        from bayadera_gb300 import models as Mo
+        if isinstance(model, Mo.DeviceLikelihoodModel):
+            if dim is None:
+                raise ValueError("a likelihood engine needs the points' dimension")
+            name = "%s_bay_points" % model.loglik
+            src = model.sources + [_LIK_ADAPTER % {"name": name, "loglik": model.loglik}]
+            dm = Mo.device_distribution_model(src, name=name, logpdf=name, dimension=dim,
+                                              params_size=0)
+        else:
+            dm = Mo.device_distribution_model(model.sources, name=model.name,
+                                              logpdf=model.logpdf, dimension=model.dimension,
+                                              params_size=model.params_size)
+        self.model = model
+        self.dim = dm.dimension
+        self.sf = GB300StretchFactory(factory, dm, form="plain")
+
+    def release(self):
+        self.sf.release()
+
+    def _pts(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        if x.ndim == 1:
+            x = x.reshape(-1, self.dim)
+        if x.shape[-1] != self.dim:
+            raise ValueError("points must be n x %d" % self.dim)
+        return x
+
+    def _call(self, fn, params, x):
+        p = np.ascontiguousarray(params, np.float32).reshape(-1)
+        x = self._pts(x)
+        out = np.zeros(x.shape[0], np.float32)
+        N.call(fn, self.sf.handle, _ptr(p), p.size, _ptr(x), x.shape[0], _ptr(out))
+        return out
+
+    def log_density(self, params, x):
+        return self._call("bay_log_density", params, x)
+
+    def density(self, params, x):
+        return self._call("bay_density", params, x)
+
+    def evidence(self, params, x):
+        p = np.ascontiguousarray(params, np.float32).reshape(-1)
+        x = self._pts(x)
+        r = C.c_double()
+        N.call("bay_evidence", self.sf.handle, _ptr(p), p.size, _ptr(x), x.shape[0], C.byref(r))
+        return r.value
 
 
 def check_model(model, form=None, wgs=1024, accept_ref=False, tensor=False):

@@ -273,6 +273,34 @@ int bay_logfn_values(bay_sampler* s, float* out);
 /* Execution control: CUDA-graph replay of the step loops (default on). */
 int bay_sampler_set_graphs(bay_sampler* s, int enabled);
 
+/* ---------------------------------------------------------------- direct samplers
+ * Replace GTXDirectSamplerEngine.sample (nvidia_gtx.clj:48-63) over
+ * cuda/rng/{uniform,gaussian,exponential,erlang}-sampler.cu: n samples (n a multiple of
+ * 4, the reference's rule) of the distribution with the given parameters and seed, the
+ * reference's Philox stream; params and out host or device memory. */
+enum bay_direct_kind {
+    BAY_DIRECT_UNIFORM = 0,      /* params {lower, upper} */
+    BAY_DIRECT_GAUSSIAN = 1,     /* params {mu, sigma} */
+    BAY_DIRECT_EXPONENTIAL = 2,  /* params {lambda} */
+    BAY_DIRECT_ERLANG = 3        /* params {lambda, k} */
+};
+int bay_sample_direct(bay_ctx* ctx, uint32_t kind, const float* params, uint32_t seed,
+                      uint64_t n, float* out);
+
+/* ---------------------------------------------------------------- density engines
+ * Replace GTXDistributionEngine.log-density / density and GTXLikelihoodEngine
+ * .log-density / density / evidence (nvidia_gtx.clj:67-141): the model's density (its
+ * plain-form logfn; a likelihood is compiled through a 5-argument adapter) at n points,
+ * x dim x n column-major; params = data || hyperparameters.  bay_evidence is the mean of
+ * exp(logfn) over the points (FP64 sums in a fixed order).  The model must be compiled in
+ * the plain form; all arrays host or device memory. */
+int bay_log_density(bay_model* model, const float* params, uint64_t n_params, const float* x,
+                    uint64_t n, float* out);
+int bay_density(bay_model* model, const float* params, uint64_t n_params, const float* x,
+                uint64_t n, float* out);
+int bay_evidence(bay_model* model, const float* params, uint64_t n_params, const float* x,
+                 uint64_t n, double* out);
+
 /* ---------------------------------------------------------------- batched models
  * Many independent models of one BAY_FORM_BATCH family -- each with its own dimension,
  * walkers, data and seed -- advanced together: every half-step of every member is three

@@ -94,6 +94,18 @@ def test_model_check_batch_form(native):
         _check(M.logistic_model(8), "batch")
 
 
+def test_model_check_density_engines(native):
+    """The plain-form modules carry the density engines' point kernels; a likelihood
+    compiles through its 5-argument adapter."""
+    from bayadera_gb300 import models as M
+    from bayadera_gb300.engine import _LIK_ADAPTER
+    lik = M.likelihood_models()["gaussian"]
+    name = "%s_bay_points" % lik.loglik
+    src = lik.sources + [_LIK_ADAPTER % {"name": name, "loglik": lik.loglik}]
+    dm = M.device_distribution_model(src, name=name, logpdf=name, dimension=2, params_size=0)
+    _check(dm, "plain")
+
+
 def test_model_check_tensor_core_form(native):
     """The tcgen05 rows kernels compile for sm_103a across the feature-chunk counts (1 to
     5 chunks of 64, one or two walker sub-tiles per CTA); more than 320 features is an
