@@ -124,6 +124,9 @@ _SIGNATURES = {
     "bay_log_density": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
     "bay_density": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
     "bay_evidence": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, C.POINTER(C.c_double)]),
+    "bay_data_moments": (C.c_int, [P, P, C.c_uint32, C.c_uint64, P, P]),
+    "bay_data_histogram": (C.c_int, [P, P, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, P, P,
+                                     P]),
     "bay_batch_create": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32, C.POINTER(P)]),
     "bay_batch_release": (C.c_int, [P]),
     "bay_batch_init_position_normal": (C.c_int, [P, P, C.c_float, C.c_float]),

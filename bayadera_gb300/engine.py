@@ -113,6 +113,33 @@ class GB300BayaderaFactory:
         points of dimension dim (data = the params)."""
         return GB300DensityEngine(self, likelihood, dim=dim)
 
+    # ------------------------------------------------------------ dataset engine
+    def data_moments(self, x):
+        """data-mean and data-variance of a data matrix x (n points x dim) in FP64."""
+        x = np.ascontiguousarray(x, np.float32)
+        if x.ndim == 1:
+            x = x[:, None]
+        n, dim = x.shape
+        mean = np.zeros(dim)
+        var = np.zeros(dim)
+        N.call("bay_data_moments", self.ctx, _ptr(x), dim, n, _ptr(mean), _ptr(var))
+        return mean, var
+
+    def data_histogram(self, x, bins=0, flags=0):
+        """histogram of a data matrix x (n points x dim): Histogram(limits 2 x dim, pdf and
+        bin ranks bins x dim)."""
+        x = np.ascontiguousarray(x, np.float32)
+        if x.ndim == 1:
+            x = x[:, None]
+        n, dim = x.shape
+        bins = bins or self.wgs
+        lim = np.zeros((dim, 2), np.float32)
+        pdf = np.zeros((dim, bins), np.float32)
+        ranks = np.zeros((dim, bins), np.float32)
+        N.call("bay_data_histogram", self.ctx, _ptr(x), dim, n, bins, flags, _ptr(lim),
+               _ptr(pdf), _ptr(ranks))
+        return Histogram(lim.T, pdf.T, ranks.T)
+
     def direct_sample(self, kind, seed, params, n):
         """direct-sampler-engine sample: n samples (a multiple of 4) of uniform, gaussian,
         exponential or erlang with the given parameters."""

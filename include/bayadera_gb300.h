@@ -301,6 +301,16 @@ int bay_density(bay_model* model, const float* params, uint64_t n_params, const 
 int bay_evidence(bay_model* model, const float* params, uint64_t n_params, const float* x,
                  uint64_t n, double* out);
 
+/* ---------------------------------------------------------------- dataset engine
+ * Replace GTXDatasetEngine.data-mean / data-variance / histogram (nvidia_gtx.clj:145-228):
+ * per-dimension mean and population variance (FP64; mean or variance may be NULL) and the
+ * histogram (limits 2 x dim, pdf and bin ranks bins x dim; counts start at 0 as on the
+ * reference's dataset path) of a data matrix x, dim x n column-major, host or device. */
+int bay_data_moments(bay_ctx* ctx, const float* x, uint32_t dim, uint64_t n, double* mean,
+                     double* variance);
+int bay_data_histogram(bay_ctx* ctx, const float* x, uint32_t dim, uint64_t n, uint32_t bins,
+                       uint32_t flags, float* limits, float* pdf, float* ranks);
+
 /* ---------------------------------------------------------------- batched models
  * Many independent models of one BAY_FORM_BATCH family -- each with its own dimension,
  * walkers, data and seed -- advanced together: every half-step of every member is three

@@ -138,6 +138,28 @@ def extract(ref_root):
                    "sigma0": sbig[0], "sigma0_tol": sbig[1]},
     }
 
+    # ---- HDI utilities (test/clojure/uncomplicate/bayadera/util_test.clj): the fixture
+    # pdf / bin ranks / limits and the asserted hdi-rank-count, hdi-bins, hdi-regions
+    usrc = open(os.path.join(ref_root, "test/clojure/uncomplicate/bayadera/util_test.clj")).read()
+    lims = [float(x) for x in re.search(r"l (\d+)\s+u (\d+)", usrc).groups()]
+    pdf = _nums(re.search(r"tpdf \(fv \[([^\]]*)\]\)", usrc).group(1))
+    rm = re.search(r"tbin-rank \(fv \(op \[([^\]]*)\] \(range (\d+) (\d+)\)\)\)", usrc)
+    rank = _nums(rm.group(1)) + [float(v) for v in range(int(rm.group(2)), int(rm.group(3)))]
+    counts = []
+    for m in re.finditer(r"\(hdi-rank-count (\(/ )?([\d.]+)( tpdf-asum\))? tbin-rank tpdf\) => (\d+)",
+                         usrc):
+        counts.append({"mass": float(m.group(2)), "scaled": bool(m.group(1)),
+                       "want": int(m.group(4))})
+    bins = [{"cnt": int(m.group(1)), "want": _nums(m.group(2))}
+            for m in re.finditer(r"\(hdi-bins tbin-rank (\d+)\) => \[([^\]]*)\]", usrc)]
+    regions = [{"cnt": int(m.group(1)), "cols": int(m.group(2)), "want": _nums(m.group(3)),
+                "tol": float(m.group(4))}
+               for m in re.finditer(r"\(hdi-regions tlimits tbin-rank (\d+)\) \(fge 2 (\d+) \[([^\]]*)\]\)\)\) "
+                                    r"=> \(roughly 0 ([\d.]+)\)", usrc)]
+    g["hdi"] = {"source": "test/clojure/uncomplicate/bayadera/util_test.clj", "limits": lims,
+                "pdf": pdf, "bin_rank": rank, "rank_count": counts, "bins": bins,
+                "regions": regions}
+
     series = {}
     for n in (67, 367, 112640):
         with open(os.path.join(tdir, "acor-data-%d" % n)) as f:

@@ -112,3 +112,20 @@ def test_density_engine_needs_plain_form(factory, M):
         N.call("bay_log_density", sf.handle, C.c_void_p(p.ctypes.data), 5,
                C.c_void_p(x.ctypes.data), 1, C.c_void_p(out.ctypes.data))
     sf.release()
+
+
+def test_dataset_moments_and_histogram(factory, oracle):
+    """Dataset engine on a 3 x 50,000 data matrix: FP64 moments against the oracle's FP64
+    mean and variance, and the histogram (limits, pdf, bin ranks; counts from 0) bit-exact
+    against the oracle's."""
+    rng = np.random.default_rng(4)
+    x = np.stack([rng.normal(2.0, 1.0, 50000), rng.exponential(1.5, 50000),
+                  rng.uniform(-3.0, 5.0, 50000)], axis=1).astype(np.float32)
+    mean, var = factory.data_moments(x)
+    np.testing.assert_allclose(mean, oracle.mean64(x.reshape(-1), 3), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(var, oracle.variance64(x.reshape(-1), 3), rtol=1e-12)
+    h = factory.data_histogram(x, 256)
+    ol, opdf, orank, _ = oracle.histogram([x.reshape(-1)], 3, 256, wgs=256)
+    np.testing.assert_array_equal(h.limits.T.reshape(-1), ol)
+    np.testing.assert_array_equal(h.pdf.T.reshape(-1), opdf)
+    np.testing.assert_array_equal(h.bin_ranks.T.reshape(-1), orank)
