@@ -215,6 +215,7 @@ size_t gemm_smem_bytes(const bay_model* m, uint64_t rows) {
 // the barriers and flags, and 1 KB to align the operands to the 128-byte swizzle's
 // 1024-byte period.  Largest G (fewer re-reads of the matrix), then up to 6 stages.
 constexpr size_t kTcSmemMax = 232448;  // opt-in dynamic shared memory per CTA, sm_100 family
+constexpr uint32_t kTrWalkers = 64;      // walkers per CTA of the resident tensor-core form
 bool tc_plan(uint32_t features, uint32_t aux_len, uint32_t* G, uint32_t* S, size_t* smem) {
     const size_t kc = (features + 63) / 64, auxs = aux_len ? aux_len : 1;
     for (uint32_t g = 2; g >= 1; --g) {
@@ -386,7 +387,7 @@ struct bay_sampler {
 
     uint64_t per_cta() const {
         if (streaming) return 256;  // the accept kernel: one thread per walker
-        if (tcr) return 64;
+        if (tcr) return kTrWalkers;
         return model->form == BAY_FORM_PLAIN ? model->cta : model->wpc;
     }
 
@@ -763,6 +764,7 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
             opts.push_back("-DBAY_GEMM_TC=1");
             opts.push_back("-DBAY_TC_G=" + std::to_string(g.tc_g));
             opts.push_back("-DBAY_TC_STAGES=" + std::to_string(g.tc_stages));
+            opts.push_back("-DBAY_TR_W=" + std::to_string(kTrWalkers) + "u");
         }
         wpc = 64;
     } else if (d->form == BAY_FORM_BATCH) {
@@ -966,11 +968,13 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                 const uint64_t np = (s->gemm_rows + 15) & ~15ull, kc = (m->gemm_features + 63) / 64;
                 const uint64_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1;
                 const uint64_t img = 2 * kc * np * 128 + np * auxs * 4;
-                // image, 2 kc atoms of 64 walker rows (8 KB), then the proposals and the
-                // reduction scratch -- at least 8 KB, which the M = 128 MMA reads past the
-                // last atom (walker rows 64..127, never read back)
-                const uint64_t tail = std::max<uint64_t>(8192, 64ull * (m->dim | 1u) * 4 + 1024);
-                const uint64_t sm = 1024 + ((img + 1023) & ~1023ull) + 2 * kc * 8192 + tail;
+                // image, 2 kc atoms of kTrWalkers walker rows, then the proposals and the
+                // reduction scratch -- at least the part of the M = 128 MMA's 16 KB read that
+                // runs past the last atom (walker rows kTrWalkers..127, never read back)
+                const uint64_t atom = 128ull * kTrWalkers;
+                const uint64_t tail = std::max<uint64_t>(16384 - atom,
+                                                         (uint64_t)kTrWalkers * (m->dim | 1u) * 4 + 1024);
+                const uint64_t sm = 1024 + ((img + 1023) & ~1023ull) + 2 * kc * atom + tail;
                 if (sm <= kGemmMaxSmem) {
                     s->tc = false;
                     s->tcr = true;

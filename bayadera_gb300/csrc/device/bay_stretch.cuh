@@ -1143,8 +1143,10 @@ bay_gemm_rows_tc_logfn(bay_stretch_params P, const __grid_constant__ bay_tmaps T
 // TMEM); then each walker's row terms are read back from its TMEM lane (two warps per
 // lane group, half of the rows each), summed pairwise with a Kahan carry and combined,
 // and the accept step and write-back follow as in the SIMT form.
-#define BAY_TR_W 64u                                    // walkers per CTA
-#define BAY_TR_ATOM 8192u                               // 64 walkers x 64 bf16 (one atom)
+#ifndef BAY_TR_W
+#define BAY_TR_W 64u                                    // walkers per CTA: 64 or 128
+#endif
+#define BAY_TR_ATOM (BAY_TR_W * 128u)                   // BAY_TR_W walkers x 64 bf16 (one atom)
 #define BAY_TR_DPAD (DIM | 1)
 
 __device__ __forceinline__ void bay_tmem_ld8(unsigned int ta, float (&v)[8]) {
@@ -1249,10 +1251,13 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     //    thread keeps a batch of its loads in flight before it uses any of them
     constexpr int NE = (int)((BAY_TR_W * DIM + 255) / 256);   // elements per thread
     constexpr int CH = 16;
-    // accu with one batch of gathered elements per thread: the current rows stay in
-    // registers and are parked in the A region once the MMAs are done (no reload)
-    constexpr bool KEEPX = ACCU && NE <= CH;
-    float xkeep[CH];
+    // accu with few gathered elements per thread (at most 16 with 4 CTAs per SM, 32 with
+    // 2): the current rows stay in registers and are parked in the A region once the MMAs
+    // are done (no reload), when they fit there
+    constexpr int NEMAX = BAY_TR_W <= 64u ? 16 : 32;
+    constexpr bool KEEPX = ACCU && NE <= NEMAX &&
+                           BAY_TR_W * BAY_TR_DPAD * 4u <= 2u * BAY_TC_KC * BAY_TR_ATOM;
+    float xkeep[KEEPX ? NE : 1];
     {
         const float* Xt = X + (size_t)k0 * DIM;
         const unsigned int n_own = nt * DIM;
@@ -1277,7 +1282,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                         : (e < n_own ? __fmaf_rn(sZ[wv[i]], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
                     Yw[wv[i] * BAY_TR_DPAD + dv[i]] = y;
                 }
-                if (KEEPX) xkeep[i] = xv[i];
+                if (KEEPX && c0 + i < NE) xkeep[KEEPX ? c0 + i : 0] = xv[i];
             }
         }
     }
@@ -1352,9 +1357,9 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     float* Xa = (float*)(sm + a_off);   // [64][DPAD] current rows, in the A region (free now)
     if (KEEPX) {
 #pragma unroll
-        for (int i = 0; i < CH; ++i) {
+        for (int i = 0; i < (KEEPX ? NE : 1); ++i) {
             const unsigned int e = tid + 256u * (unsigned int)i;
-            if (i < NE && e < nt * DIM) {
+            if (e < nt * DIM) {
                 const unsigned int w = e / DIM;
                 Xa[w * BAY_TR_DPAD + (e - w * DIM)] = xkeep[i];
             }
@@ -1362,7 +1367,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     }
     // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
     //    rows [NP/2 * (w / 4), + NP/2) in 8-column loads; the two halves then combine
-    if ((warp & 3u) < 2u) {
+    if (32u * (warp & 3u) < BAY_TR_W) {
         const unsigned int wl = 32u * (warp & 3u) + lane;
         const unsigned int h = warp >> 2, half_rows = NP >> 1;
         const unsigned int c0 = h * half_rows;
@@ -1389,9 +1394,9 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
         if (h) {                                        // second half of the rows
             sHalf[wl][0] = sum;
             sHalf[wl][1] = -cmp;
-        } else {                                        // first half: red[wl], red[64 + wl]
+        } else {                                        // first half: red[wl], red[W + wl]
             red[wl] = sum;
-            red[64u + wl] = -cmp;
+            red[BAY_TR_W + wl] = -cmp;
         }
     }
     bay_tc_fence_before();
@@ -1404,7 +1409,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
         t.hi = sW[tid];
         t.lo = 0.0f;
         a.hi = red[tid];
-        a.lo = red[64u + tid];
+        a.lo = red[BAY_TR_W + tid];
         b.hi = sHalf[tid][0];
         b.lo = sHalf[tid][1];
         t = bay_cadd(t, bay_cadd(a, b));
@@ -1454,9 +1459,9 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
             if (P.means_cap != 0) {
                 __syncthreads();
-                // per-dim sums of the tile's new positions: warp q sums walkers 8 q .. 8 q + 7
-                // of 32 dims (one per lane) in fp32, then the 8 warps' sums in warp order
-                // (64 terms in all; the per-step means add the CTAs' sums in FP64)
+                // per-dim sums of the tile's new positions: warp q sums its W / 8 walkers of
+                // 32 dims (one per lane) in fp32, then the 8 warps' sums in warp order (the
+                // per-step means add the CTAs' sums in FP64)
                 float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x
                     + blockIdx.x;
                 for (unsigned int d0 = 0; d0 < DIM; d0 += 32u) {
@@ -1464,8 +1469,8 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                     float v = 0.0f;
                     if (d < DIM) {
 #pragma unroll
-                        for (unsigned int i = 0; i < 8u; ++i) {
-                            const unsigned int w = 8u * warp + i;
+                        for (unsigned int i = 0; i < BAY_TR_W / 8u; ++i) {
+                            const unsigned int w = (BAY_TR_W / 8u) * warp + i;
                             if (w < nt) v = __fadd_rn(v, (KEEPX && !sAcc[w]) ? Xa[w * BAY_TR_DPAD + d]
                                                                             : Yw[w * BAY_TR_DPAD + d]);
                         }

@@ -282,11 +282,12 @@ def test_tcr_mvn_logfn_and_moves(factory, M, oracle):
     assert differ <= W // 25, differ
 
 
-@pytest.mark.parametrize("D", [10, 80])
+@pytest.mark.parametrize("D", [10, 63, 64, 80])
 def test_tcr_run_sampler_matches_simt(factory, M, D):
     """Resident tensor-core accu path: acceptance rate within 3 binomial s.e. of the SIMT
-    form's, per-step means (last = mean of the walkers).  D = 10 keeps the tile's current
-    rows in registers for the statistics; D = 80 reloads them."""
+    form's, per-step means (last = mean of the walkers).  D = 10 and 63 keep the tile's
+    current rows in registers for the statistics; D = 64 (rows of 65 floats, larger than
+    the A region they would be parked in) and D = 80 reload them."""
     W = 4096
     P = np.diag(np.linspace(0.5, 2.0, D)).astype(np.float32)
     rates = {}
