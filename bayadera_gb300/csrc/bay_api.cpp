@@ -53,6 +53,7 @@ struct DriverApi {
     PFN_cuLibraryUnload_v12000 LibraryUnload = nullptr;
     PFN_cuLibraryGetKernel_v12000 LibraryGetKernel = nullptr;
     PFN_cuLaunchKernel_v4000 LaunchKernel = nullptr;
+    PFN_cuLaunchKernelEx_v11060 LaunchKernelEx = nullptr;
     PFN_cuKernelSetAttribute_v12000 KernelSetAttribute = nullptr;
     PFN_cuTensorMapEncodeTiled_v12000 TensorMapEncodeTiled = nullptr;
     bool loaded = false;
@@ -88,6 +89,7 @@ void load_driver_api() {
     resolve("cuLibraryUnload", g_cu.LibraryUnload, 12000);
     resolve("cuLibraryGetKernel", g_cu.LibraryGetKernel, 12000);
     resolve("cuLaunchKernel", g_cu.LaunchKernel, 4000);
+    resolve("cuLaunchKernelEx", g_cu.LaunchKernelEx, 11060);
     resolve("cuKernelSetAttribute", g_cu.KernelSetAttribute, 12000);
     resolve("cuTensorMapEncodeTiled", g_cu.TensorMapEncodeTiled, 12000);
     g_cu.loaded = true;
@@ -468,8 +470,30 @@ struct bay_sampler {
         if (st == ctx->stream) bay::count_launches(1);
         bay_stretch_params p = make_params(half, step_off);
         void* args[] = {&p};
-        CUkernel k = tcr ? model->k_tr[accu ? 1 : 0] : (accu ? model->k_accu : model->k_bare);
-        cu_check(g_cu.LaunchKernel((CUfunction)k, grid(), 1, 1, tcr ? 256 : model->cta, 1, 1,
+        if (tcr) {
+            // programmatic dependent launch: the kernel sets up its barriers and tensor memory,
+            // then waits (griddepcontrol.wait) for the previous kernel of the stream to
+            // complete before it reads anything, so its set-up overlaps that kernel's tail
+            CUlaunchAttribute at[1];
+            at[0].id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+            at[0].value.programmaticStreamSerializationAllowed = 1;
+            CUlaunchConfig cfg{};
+            cfg.gridDimX = grid();
+            cfg.gridDimY = 1;
+            cfg.gridDimZ = 1;
+            cfg.blockDimX = 256;
+            cfg.blockDimY = 1;
+            cfg.blockDimZ = 1;
+            cfg.sharedMemBytes = (unsigned)smem;
+            cfg.hStream = (CUstream)st;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            cu_check(g_cu.LaunchKernelEx(&cfg, (CUfunction)model->k_tr[accu ? 1 : 0], args, nullptr),
+                     "cuLaunchKernelEx(stretch, tensor cores)");
+            return;
+        }
+        CUkernel k = accu ? model->k_accu : model->k_bare;
+        cu_check(g_cu.LaunchKernel((CUfunction)k, grid(), 1, 1, model->cta, 1, 1,
                                    (unsigned)smem, (CUstream)st, args, nullptr),
                  "cuLaunchKernel(stretch)");
     }

@@ -1199,7 +1199,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     const unsigned int k0 = blockIdx.x * BAY_TR_W;
     const unsigned int nk = LOGFN_ONLY ? P.W : P.K;
     const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
-    const unsigned int step = P.ctl->step[kind] + P.step_off;
     const float* hyper = P.params + P.data_len;
     float* X = P.xs + (LOGFN_ONLY ? 0 : (size_t)P.half * P.K * DIM);
     const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM;
@@ -1225,6 +1224,12 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     __syncthreads();
     bay_tc_fence_after();
     const unsigned int tmem = sTmem;
+    // nothing above reads device memory: with a programmatic dependent launch this CTA may
+    // have started before the previous kernel of the stream finished; wait for it (and its
+    // memory) here, then let the next launch start its own set-up
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const unsigned int step = P.ctl->step[kind] + P.step_off;
     if (tid == 0) {
         bay_expect_tx(bar_img, img_bytes);
         asm volatile(
@@ -1251,13 +1256,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     //    thread keeps a batch of its loads in flight before it uses any of them
     constexpr int NE = (int)((BAY_TR_W * DIM + 255) / 256);   // elements per thread
     constexpr int CH = 16;
-    // accu with few gathered elements per thread (at most 16 with 4 CTAs per SM, 32 with
-    // 2): the current rows stay in registers and are parked in the A region once the MMAs
-    // are done (no reload), when they fit there
-    constexpr int NEMAX = BAY_TR_W <= 64u ? 16 : 32;
-    constexpr bool KEEPX = ACCU && NE <= NEMAX &&
-                           BAY_TR_W * BAY_TR_DPAD * 4u <= 2u * BAY_TC_KC * BAY_TR_ATOM;
-    float xkeep[KEEPX ? NE : 1];
     {
         const float* Xt = X + (size_t)k0 * DIM;
         const unsigned int n_own = nt * DIM;
@@ -1282,7 +1280,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                         : (e < n_own ? __fmaf_rn(sZ[wv[i]], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
                     Yw[wv[i] * BAY_TR_DPAD + dv[i]] = y;
                 }
-                if (KEEPX && c0 + i < NE) xkeep[KEEPX ? c0 + i : 0] = xv[i];
             }
         }
     }
@@ -1354,17 +1351,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     __syncthreads();
     bay_tc_fence_after();
     const bool ok = sOk != 0u;
-    float* Xa = (float*)(sm + a_off);   // [64][DPAD] current rows, in the A region (free now)
-    if (KEEPX) {
-#pragma unroll
-        for (int i = 0; i < (KEEPX ? NE : 1); ++i) {
-            const unsigned int e = tid + 256u * (unsigned int)i;
-            if (e < nt * DIM) {
-                const unsigned int w = e / DIM;
-                Xa[w * BAY_TR_DPAD + (e - w * DIM)] = xkeep[i];
-            }
-        }
-    }
     // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
     //    rows [NP/2 * (w / 4), + NP/2) in 8-column loads; the two halves then combine
     if (32u * (warp & 3u) < BAY_TR_W) {
@@ -1425,7 +1411,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
         if (tid < BAY_TR_W) sAcc[tid] = accepted ? 1 : 0;
         const int n_acc = __syncthreads_count(accepted);
         float* Xt = X + (size_t)k0 * DIM;
-        if (ACCU && !KEEPX) {
+        if (ACCU) {
             // the statistics need every walker's new position in Yw: the rejected walkers'
             // current rows are loaded in batches (all in flight), the accepted ones stored
 #pragma unroll
@@ -1448,8 +1434,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                 }
             }
         } else {
-            // accepted walkers' rows to device memory (KEEPX: the current rows of the
-            // rejected ones are already in Xa)
+            // accepted walkers' rows to device memory
             for (unsigned int e = tid; e < nt * DIM; e += blockDim.x) {
                 const unsigned int w = e / DIM;
                 if (sAcc[w]) Xt[e] = Yw[w * BAY_TR_DPAD + (e - w * DIM)];
@@ -1459,31 +1444,33 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
             if (P.means_cap != 0) {
                 __syncthreads();
-                // per-dim sums of the tile's new positions: warp q sums its W / 8 walkers of
-                // 32 dims (one per lane) in fp32, then the 8 warps' sums in warp order (the
-                // per-step means add the CTAs' sums in FP64)
+                // per-dim sums of the tile's new positions in one pass: NG = 256 / DIM groups
+                // (at most 8) of WG consecutive walkers, thread (g, d) sums group g of dim d in
+                // fp32 in walker order, then thread d adds the groups' sums in group order
+                // (the per-step means add the CTAs' sums in FP64)
+                constexpr unsigned int NG = DIM >= 128u ? 1u : (256u / DIM < 8u ? 256u / DIM : 8u);
+                constexpr unsigned int WG = (BAY_TR_W + NG - 1u) / NG;
                 float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x
                     + blockIdx.x;
-                for (unsigned int d0 = 0; d0 < DIM; d0 += 32u) {
-                    const unsigned int d = d0 + lane;
+                for (unsigned int t = tid; t < NG * DIM; t += blockDim.x) {
+                    const unsigned int g = t / DIM, d = t - g * DIM;
                     float v = 0.0f;
-                    if (d < DIM) {
 #pragma unroll
-                        for (unsigned int i = 0; i < BAY_TR_W / 8u; ++i) {
-                            const unsigned int w = (BAY_TR_W / 8u) * warp + i;
-                            if (w < nt) v = __fadd_rn(v, (KEEPX && !sAcc[w]) ? Xa[w * BAY_TR_DPAD + d]
-                                                                            : Yw[w * BAY_TR_DPAD + d]);
-                        }
+                    for (unsigned int i = 0; i < WG; ++i) {
+                        const unsigned int w = g * WG + i;
+                        if (w < nt) v = __fadd_rn(v, Yw[w * BAY_TR_DPAD + d]);
                     }
-                    red[warp * 32u + lane] = v;
+                    if (NG == 1u) out[(size_t)d * gridDim.x] = v;
+                    else red[t] = v;                    // NG * DIM <= 256 floats
+                }
+                if (NG > 1u) {
                     __syncthreads();
-                    if (tid < 32u && d0 + tid < DIM) {
+                    if (tid < DIM) {
                         float a = 0.0f;
 #pragma unroll
-                        for (unsigned int q = 0; q < 8u; ++q) a = __fadd_rn(a, red[q * 32u + tid]);
-                        out[(size_t)(d0 + tid) * gridDim.x] = a;
+                        for (unsigned int g = 0; g < NG; ++g) a = __fadd_rn(a, red[g * DIM + tid]);
+                        out[(size_t)tid * gridDim.x] = a;
                     }
-                    __syncthreads();
                 }
             }
         }

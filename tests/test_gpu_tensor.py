@@ -285,9 +285,8 @@ def test_tcr_mvn_logfn_and_moves(factory, M, oracle):
 @pytest.mark.parametrize("D", [10, 63, 64, 80])
 def test_tcr_run_sampler_matches_simt(factory, M, D):
     """Resident tensor-core accu path: acceptance rate within 3 binomial s.e. of the SIMT
-    form's, per-step means (last = mean of the walkers).  D = 10 and 63 keep the tile's
-    current rows in registers for the statistics; D = 64 (rows of 65 floats, larger than
-    the A region they would be parked in) and D = 80 reload them."""
+    form's, per-step means (last = mean of the walkers).  The per-dim sums run in 256 / D
+    walker groups: 8 groups for D = 10, 4 for D = 63 and 64, 3 for D = 80."""
     W = 4096
     P = np.diag(np.linspace(0.5, 2.0, D)).astype(np.float32)
     rates = {}
