@@ -175,7 +175,7 @@ def run_reference(args):
 def config():
     return {"workload": "mvn50-ar1 (50-D correlated Gaussian, rho 0.9, scales log-U[0.1,10])",
             "dim": DIM, "walkers": WALKERS, "burn_in": BURN, "run": RUN, "bins": BINS,
-            "model_form": "gemm on the tensor cores (128-walker tiles, x'Px as a tcgen05 "
+            "model_form": "gemm on the tensor cores (64-walker tiles, x'Px as a tcgen05 "
                           "split-bf16 product, fp32 accumulation, resident precision matrix)",
             "l2": "flushed between timed steps (256 MiB device write)",
             "parallelism": "replicas"}
@@ -590,7 +590,7 @@ def main():
             t_total = float(t.item())
         return WALKERS * (BURN + RUN) * steps * world / t_total, t_total, results
 
-    # headline: the GEMM form on the tensor cores (128-walker tiles, x'Px as a split-bf16
+    # headline: the GEMM form on the tensor cores (64-walker tiles, x'Px as a split-bf16
     # tcgen05 product against the resident precision matrix)
     samp = sfs["tensor"].create_sampler(seed_base, WALKERS, dP)
     launches0 = _native.launch_count()
