@@ -1168,12 +1168,67 @@ __device__ __forceinline__ void bay_mma_n(unsigned int d, unsigned long long a, 
         ::"r"(d), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
 }
 
+// 8 consecutive floats (dims 8u .. 8u + 7) of a walker row: float4 loads when rows are
+// 16-byte aligned (DIM % 4 == 0), float2 when 8-byte aligned, else scalar; zero past DIM
+// or when !ok (no access at all)
+__device__ __forceinline__ void bay_tr_ld8(const float* row, unsigned int u, bool ok, float (&v)[8]) {
+    const unsigned int d0 = 8u * u;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = 0.0f;
+    if (!ok) return;
+    if (d0 + 8u <= DIM && DIM % 4u == 0u) {
+        const float4 a = *(const float4*)(row + d0), b = *(const float4*)(row + d0 + 4u);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else if (d0 + 8u <= DIM && DIM % 2u == 0u) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 a = *(const float2*)(row + d0 + 2u * i);
+            v[2 * i] = a.x;
+            v[2 * i + 1] = a.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (d0 + i < DIM) v[i] = row[d0 + i];
+    }
+}
+
+// the store counterpart of bay_tr_ld8 (dims past DIM are not written)
+__device__ __forceinline__ void bay_tr_st8(float* row, unsigned int u, const float (&v)[8]) {
+    const unsigned int d0 = 8u * u;
+    if (d0 + 8u <= DIM && DIM % 4u == 0u) {
+        *(float4*)(row + d0) = make_float4(v[0], v[1], v[2], v[3]);
+        *(float4*)(row + d0 + 4u) = make_float4(v[4], v[5], v[6], v[7]);
+    } else if (d0 + 8u <= DIM && DIM % 2u == 0u) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) *(float2*)(row + d0 + 2u * i) = make_float2(v[2 * i], v[2 * i + 1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (d0 + i < DIM) row[d0 + i] = v[i];
+    }
+}
+
+// 16-byte unit u (8 features) of walker row w in an A atom, at unit u ^ (w % 8) of its
+// 128-byte row (the 128B swizzle); hi atoms first, lo atoms BAY_TC_KC atoms later
+__device__ __forceinline__ void bay_tr_put_a(unsigned int s_a, unsigned int w, unsigned int u,
+                                             const unsigned int (&hw)[4], const unsigned int (&lw)[4]) {
+    const unsigned int off = (u >> 3) * BAY_TR_ATOM + w * 128u + (((u & 7u) ^ (w & 7u)) << 4);
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(s_a + off), "r"(hw[0]),
+                 "r"(hw[1]), "r"(hw[2]), "r"(hw[3]) : "memory");
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+                 ::"r"(s_a + BAY_TC_KC * BAY_TR_ATOM + off), "r"(lw[0]), "r"(lw[1]), "r"(lw[2]),
+                 "r"(lw[3]) : "memory");
+}
+
 template <bool ACCU, bool LOGFN_ONLY>
 __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
-    // Shared memory: [matrix image][A: hi atoms, lo atoms (64 walker rows each)][Yw][red].
-    // The MMA runs M = 128: it also reads the 8 KB after each atom's 64 rows (the next atom,
-    // or Yw and the slack after A's last atom) as walker rows 64..127, whose accumulator
-    // lanes are never read; the host reserves at least 8 KB after the last atom.
+    // Shared memory: [matrix image][A: hi atoms, lo atoms (BAY_TR_W walker rows each)][Yw][red].
+    // The MMA runs M = 128 (an M = 64 form was measured no faster): with 64-walker tiles it
+    // also reads the 8 KB after each atom's 64 rows (the next atom, or Yw and the slack
+    // after A's last atom) as walker rows 64..127, whose accumulator lanes are never read;
+    // the host reserves at least 8 KB after the last atom.
     extern __shared__ __align__(1024) unsigned char bay_smem_tr[];
     const unsigned int NP = P.gemm_np;                       // rows padded to 16
     const unsigned int rows = (unsigned int)P.gemm_rows;
@@ -1252,58 +1307,79 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
         sLx[tid] = P.logfn[(size_t)P.half * P.K + k];
     }
     __syncthreads();
-    // 3. Y of the tile (walker-major, odd stride), gathered element-wise (coalesced); each
-    //    thread keeps a batch of its loads in flight before it uses any of them
-    constexpr int NE = (int)((BAY_TR_W * DIM + 255) / 256);   // elements per thread
-    constexpr int CH = 16;
-    {
-        const float* Xt = X + (size_t)k0 * DIM;
-        const unsigned int n_own = nt * DIM;
+    // 3. Y of the tile (walker-major rows of odd stride) from (walker, 8-dim unit) items:
+    //    consecutive threads take consecutive units of a row (the tile's own rows are one
+    //    contiguous block, a partner's row is 4 * DIM contiguous bytes), IB items' loads in
+    //    flight per thread; with the coefficients at dim 0 the same thread splits its unit
+    //    into bf16 hi + lo and writes it to the A operand
+    constexpr unsigned int NU = (DIM + 7u) / 8u;               // 8-dim units of a row
+    constexpr unsigned int NQ = BAY_TR_W * NU;                  // (walker, unit) items
+    constexpr unsigned int IB = 2u;                             // items in flight per thread
+    float* const Xt = X + (size_t)k0 * DIM;
+    for (unsigned int q0 = 0; q0 < NQ; q0 += IB * 256u) {
+        float xv[IB][8], sv[IB][8];
 #pragma unroll
-        for (int c0 = 0; c0 < NE; c0 += CH) {
-            float xv[CH], sv[CH];
-            unsigned int wv[CH], dv[CH];
+        for (unsigned int b = 0; b < IB; ++b) {
+            const unsigned int q = q0 + b * 256u + tid;
+            const unsigned int w = q / NU, u = q - w * NU;
+            const bool ok = q < NQ && w < nt;
+            bay_tr_ld8(Xt + (size_t)w * DIM, u, ok, xv[b]);
+            if (!LOGFN_ONLY) bay_tr_ld8(S + (size_t)sJ[ok ? w : 0u] * DIM, u, ok, sv[b]);
+        }
 #pragma unroll
-            for (int i = 0; i < CH; ++i) {
-                const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
-                wv[i] = e / DIM;
-                dv[i] = e - wv[i] * DIM;
-                const bool ev = (c0 + i < NE) && e < n_own;
-                xv[i] = ev ? Xt[e] : 0.0f;
-                sv[i] = (!LOGFN_ONLY && ev) ? S[(size_t)sJ[wv[i]] * DIM + dv[i]] : 0.0f;
-            }
+        for (unsigned int b = 0; b < IB; ++b) {
+            const unsigned int q = q0 + b * 256u + tid;
+            if (q < NQ) {
+                const unsigned int w = q / NU, u = q - w * NU;
+                float y[8];
+                const float z = LOGFN_ONLY ? 0.0f : sZ[w];
 #pragma unroll
-            for (int i = 0; i < CH; ++i) {
-                const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
-                if ((c0 + i < NE) && e < BAY_TR_W * DIM) {
-                    const float y = LOGFN_ONLY ? xv[i]
-                        : (e < n_own ? __fmaf_rn(sZ[wv[i]], __fsub_rn(xv[i], sv[i]), sv[i]) : 0.0f);
-                    Yw[wv[i] * BAY_TR_DPAD + dv[i]] = y;
+                for (int i = 0; i < 8; ++i) {
+                    y[i] = LOGFN_ONLY ? xv[b][i]
+                                      : (w < nt ? __fmaf_rn(z, __fsub_rn(xv[b][i], sv[b][i]), sv[b][i]) : 0.0f);
+                    if (8u * u + i < DIM) Yw[w * BAY_TR_DPAD + 8u * u + i] = y[i];
                 }
+#if BAY_GEMM_COEF == 0
+                if (u < BAY_TC_KC * 8u) {
+                    unsigned int hw[4], lw[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const unsigned int f = 8u * u + 2u * i;
+                        bay_split_bf16x2(f < BAY_GEMM_F ? y[2 * i] : 0.0f,
+                                         f + 1u < BAY_GEMM_F ? y[2 * i + 1] : 0.0f, hw[i], lw[i]);
+                    }
+                    bay_tr_put_a(s_a, w, u, hw, lw);
+                }
+#endif
             }
         }
     }
+#if BAY_GEMM_COEF == 0
+    // 4. A units past the row's last unit are zero
+    if (BAY_TC_KC * 8u > NU) {
+        constexpr unsigned int NZ = BAY_TC_KC * 8u > NU ? BAY_TC_KC * 8u - NU : 1u;
+        const unsigned int zw[4] = {0u, 0u, 0u, 0u};
+        for (unsigned int q = tid; q < BAY_TR_W * NZ; q += blockDim.x) {
+            const unsigned int w = q / NZ;
+            bay_tr_put_a(s_a, w, NU + (q - w * NZ), zw, zw);
+        }
+    }
+#else
+    // 4. the A operand from Yw (coefficients at dim BAY_GEMM_COEF): 16-byte units of hi, lo
     __syncthreads();
-    // 4. the A operand: each thread writes 16-byte units (8 features) of hi and lo,
-    //    unit u of walker w at unit u ^ (w % 8) of its 128-byte row (the 128B swizzle)
     for (unsigned int q = tid; q < BAY_TR_W * BAY_TC_KC * 8u; q += blockDim.x) {
-        const unsigned int w = q / (BAY_TC_KC * 8u), cu = q - w * (BAY_TC_KC * 8u);
-        const unsigned int c = cu >> 3, u = cu & 7u;
+        const unsigned int w = q / (BAY_TC_KC * 8u), u = q - w * (BAY_TC_KC * 8u);
         unsigned int hw[4], lw[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const unsigned int f = c * 64u + u * 8u + 2u * i;
+            const unsigned int f = u * 8u + 2u * i;
             const float v0 = f < BAY_GEMM_F ? Yw[w * BAY_TR_DPAD + BAY_GEMM_COEF + f] : 0.0f;
             const float v1 = f + 1u < BAY_GEMM_F ? Yw[w * BAY_TR_DPAD + BAY_GEMM_COEF + f + 1u] : 0.0f;
             bay_split_bf16x2(v0, v1, hw[i], lw[i]);
         }
-        const unsigned int off = c * BAY_TR_ATOM + w * 128u + ((u ^ (w & 7u)) << 4);
-        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(s_a + off), "r"(hw[0]),
-                     "r"(hw[1]), "r"(hw[2]), "r"(hw[3]) : "memory");
-        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
-                     ::"r"(s_a + BAY_TC_KC * BAY_TR_ATOM + off), "r"(lw[0]), "r"(lw[1]), "r"(lw[2]),
-                     "r"(lw[3]) : "memory");
+        bay_tr_put_a(s_a, w, u, hw, lw);
     }
+#endif
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // A visible to the MMAs
     __syncthreads();
     // 5. one thread: wait for the image, issue the MMAs, commit; the others precompute
@@ -1410,34 +1486,49 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     if (!LOGFN_ONLY) {
         if (tid < BAY_TR_W) sAcc[tid] = accepted ? 1 : 0;
         const int n_acc = __syncthreads_count(accepted);
-        float* Xt = X + (size_t)k0 * DIM;
         if (ACCU) {
             // the statistics need every walker's new position in Yw: the rejected walkers'
-            // current rows are loaded in batches (all in flight), the accepted ones stored
+            // current rows are loaded (IB units in flight per thread), the accepted ones
+            // stored
+            for (unsigned int q0 = 0; q0 < NQ; q0 += IB * 256u) {
+                float xv[IB][8];
 #pragma unroll
-            for (int c0 = 0; c0 < NE; c0 += CH) {
-                float xv[CH];
-#pragma unroll
-                for (int i = 0; i < CH; ++i) {
-                    const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
-                    const bool ev = (c0 + i < NE) && e < nt * DIM && !sAcc[e / DIM];
-                    xv[i] = ev ? Xt[e] : 0.0f;
+                for (unsigned int b = 0; b < IB; ++b) {
+                    const unsigned int q = q0 + b * 256u + tid;
+                    const unsigned int w = q / NU, u = q - w * NU;
+                    bay_tr_ld8(Xt + (size_t)w * DIM, u, q < NQ && w < nt && !sAcc[w < BAY_TR_W ? w : 0u],
+                               xv[b]);
                 }
 #pragma unroll
-                for (int i = 0; i < CH; ++i) {
-                    const unsigned int e = tid + 256u * (unsigned int)(c0 + i);
-                    if ((c0 + i < NE) && e < nt * DIM) {
-                        const unsigned int w = e / DIM, d = e - w * DIM;
-                        if (sAcc[w]) Xt[e] = Yw[w * BAY_TR_DPAD + d];
-                        else Yw[w * BAY_TR_DPAD + d] = xv[i];
+                for (unsigned int b = 0; b < IB; ++b) {
+                    const unsigned int q = q0 + b * 256u + tid;
+                    const unsigned int w = q / NU, u = q - w * NU;
+                    if (q < NQ && w < nt) {
+                        float* yr = &Yw[w * BAY_TR_DPAD + 8u * u];
+                        if (sAcc[w]) {
+                            float y[8];
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) y[i] = 8u * u + i < DIM ? yr[i] : 0.0f;
+                            bay_tr_st8(Xt + (size_t)w * DIM, u, y);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < 8; ++i)
+                                if (8u * u + i < DIM) yr[i] = xv[b][i];
+                        }
                     }
                 }
             }
         } else {
             // accepted walkers' rows to device memory
-            for (unsigned int e = tid; e < nt * DIM; e += blockDim.x) {
-                const unsigned int w = e / DIM;
-                if (sAcc[w]) Xt[e] = Yw[w * BAY_TR_DPAD + (e - w * DIM)];
+            for (unsigned int q = tid; q < NQ; q += blockDim.x) {
+                const unsigned int w = q / NU, u = q - w * NU;
+                if (w < nt && sAcc[w]) {
+                    const float* yr = &Yw[w * BAY_TR_DPAD + 8u * u];
+                    float y[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) y[i] = 8u * u + i < DIM ? yr[i] : 0.0f;
+                    bay_tr_st8(Xt + (size_t)w * DIM, u, y);
+                }
             }
         }
         if (ACCU) {

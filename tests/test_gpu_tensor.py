@@ -127,6 +127,70 @@ def test_tc_eta_exact_split_products(factory, M, rows, F, W):
     sf.release()
 
 
+LINEAR_OFS_SRC = r"""
+#include <stdint.h>
+extern "C" {
+inline REAL NAME_logpdf(const uint32_t data_len, const uint32_t hyper_len,
+                        const REAL* params, const uint32_t dim, const REAL* x) {
+    const uint32_t nf = dim - COEF, row = nf + 1, n = data_len / row;
+    REAL res = 0.0f;
+    for (uint32_t i = 0; i < n; ++i) {
+        const REAL* r = params + (uint64_t)i * row;
+        REAL eta = 0.0f;
+        for (uint32_t f = 0; f < nf; ++f) eta = fmaf(r[f], x[COEF + f], eta);
+        res += eta * r[nf];
+    }
+    return res;
+}
+inline void NAME_prep(const REAL* h, const uint32_t hl, const uint32_t dim, const REAL* x,
+                      REAL* prep) {}
+inline REAL NAME_term(const REAL eta, const REAL* aux, const uint64_t row, const REAL* x,
+                      const REAL* prep) {
+    return eta * aux[0];
+}
+inline REAL NAME_walker(const uint64_t rows, const REAL* h, const uint32_t hl,
+                        const uint32_t dim, const REAL* x) {
+    return 0.0f;
+}
+}
+"""
+
+
+@pytest.mark.parametrize("rows,F,coef,W", [(100, 20, 1, 300), (64, 64, 3, 130)])
+def test_tcr_exact_split_products_coefficient_offset(factory, M, rows, F, coef, W):
+    """Resident form with the coefficients at walker dims coef .. coef + F - 1 (the A
+    operand taken from the staged rows, not from the gather): the exact split-product sum
+    as in the test above."""
+    name = "tclo%d" % coef
+    src = LINEAR_OFS_SRC.replace("NAME", name).replace("COEF", str(coef))
+    g = {"prep": name + "_prep", "term": name + "_term", "walker": name + "_walker",
+         "features": F, "coef": coef, "block": "data", "ld": F + 1, "offset": 0,
+         "aux_col": F, "aux_len": 1}
+    model = M.device_distribution_model(src, name=name, logpdf=name + "_logpdf",
+                                        dimension=F + coef, params_size=1, gemm=g)
+    rng = np.random.default_rng(rows + F + coef)
+    X = sixteen_bit(rng, (rows, F), 1.0)
+    w = sixteen_bit(rng, rows, 1.0)
+    pos = sixteen_bit(rng, (W, F + coef), 0.5)
+    params = np.concatenate([np.concatenate([X, w[:, None]], axis=1).reshape(-1),
+                             np.zeros(1, np.float32)]).astype(np.float32)
+    sf = factory.mcmc_factory(model, form="gemm", tensor=True)
+    s = sf.create_sampler(3, W, params)
+    s.init_position(pos)
+    got = s.logfn().astype(np.float64)
+    xh, xl = split(X)
+    bh, bl = split(pos[:, coef:])
+    eta = bh @ xh.T + bl @ xh.T + bh @ xl.T
+    want = eta @ w.astype(np.float64)
+    mag = (np.abs(pos[:, coef:]).astype(np.float64) @ np.abs(X).T.astype(np.float64)) @ \
+        np.abs(w).astype(np.float64)
+    tol = 4 * F * 2.0 ** -24 * mag + 2.0 ** -22 * (np.abs(eta) @ np.abs(w).astype(np.float64)) + 1e-30
+    err = np.abs(got - want)
+    assert np.all(err <= tol), (err / tol).max()
+    s.release()
+    sf.release()
+
+
 def _regression(rng, n, F, kind):
     X = rng.normal(size=(n, F)).astype(np.float32)
     beta = rng.normal(scale=1.0 / np.sqrt(F), size=F)
