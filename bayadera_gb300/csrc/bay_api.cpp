@@ -56,6 +56,8 @@ struct DriverApi {
     PFN_cuLaunchKernelEx_v11060 LaunchKernelEx = nullptr;
     PFN_cuKernelSetAttribute_v12000 KernelSetAttribute = nullptr;
     PFN_cuTensorMapEncodeTiled_v12000 TensorMapEncodeTiled = nullptr;
+    PFN_cuKernelGetFunction_v12000 KernelGetFunction = nullptr;
+    PFN_cuOccupancyMaxActiveBlocksPerMultiprocessor_v6050 OccupancyMaxActiveBlocks = nullptr;
     bool loaded = false;
 };
 DriverApi g_cu;
@@ -92,6 +94,8 @@ void load_driver_api() {
     resolve("cuLaunchKernelEx", g_cu.LaunchKernelEx, 11060);
     resolve("cuKernelSetAttribute", g_cu.KernelSetAttribute, 12000);
     resolve("cuTensorMapEncodeTiled", g_cu.TensorMapEncodeTiled, 12000);
+    resolve("cuKernelGetFunction", g_cu.KernelGetFunction, 12000);
+    resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", g_cu.OccupancyMaxActiveBlocks, 6050);
     g_cu.loaded = true;
 }
 
@@ -187,7 +191,8 @@ struct bay_model {
     // shared-memory stages, dynamic shared memory
     CUkernel k_gt[2] = {nullptr, nullptr};
     // GEMM form on the tensor cores with the matrix resident: [bare, accu, logfn]
-    CUkernel k_tr[3] = {nullptr, nullptr, nullptr};
+    CUkernel k_tr[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // bare, accu, logfn,
+                                                                         // persistent bare, accu
     uint32_t tc_g = 0, tc_stages = 0;
     size_t tc_smem = 0;
     // batch form: propose / accept in k_gp / k_ga, rows in k_gr, per-step means here
@@ -217,7 +222,8 @@ size_t gemm_smem_bytes(const bay_model* m, uint64_t rows) {
 // the barriers and flags, and 1 KB to align the operands to the 128-byte swizzle's
 // 1024-byte period.  Largest G (fewer re-reads of the matrix), then up to 6 stages.
 constexpr size_t kTcSmemMax = 232448;  // opt-in dynamic shared memory per CTA, sm_100 family
-constexpr uint32_t kTrWalkers = 64;      // walkers per CTA of the resident tensor-core form
+constexpr uint32_t kTrWalkers = 64;
+constexpr uint32_t kTrGroups = 4;   // tile groups (256 threads each) per persistent CTA      // walkers per CTA of the resident tensor-core form
 bool tc_plan(uint32_t features, uint32_t aux_len, uint32_t* G, uint32_t* S, size_t* smem) {
     const size_t kc = (features + 63) / 64, auxs = aux_len ? aux_len : 1;
     for (uint32_t g = 2; g >= 1; --g) {
@@ -381,7 +387,12 @@ struct bay_sampler {
     // streaming on the tensor cores: bf16 hi + lo matrix [rows_pad][tc_fp], coefficient
     // operand [tc_wpad][tc_fp] (hi, lo), the aux values in gemm_lay [rows_pad][aux]
     bool tc = false;
-    bool tcr = false;   // tensor cores, matrix resident (one launch per half-step)
+    bool tcr = false;   // tensor cores, matrix resident (one launch per half-step, or
+                        // one persistent cooperative launch per chunk of steps)
+    bool persistent = false;    // tcr: the persistent form (when tr_smem != 0); measured
+                                // slower than programmatic dependent launches, so opt-in
+    uint32_t tr_grid = 0;       // tcr: CTAs of the persistent form (all co-resident)
+    size_t tr_smem = 0;         // tcr: dynamic shared memory of a persistent CTA
     uint32_t tc_fp = 0;
     uint64_t tc_rows_pad = 0, tc_wpad = 0;
     unsigned short *tc_xh = nullptr, *tc_xl = nullptr, *s_bh = nullptr, *s_bl = nullptr;
@@ -519,10 +530,51 @@ struct bay_sampler {
 
     // m <= kChunk steps: the kernel pairs with step offsets 0..m-1, the per-step means
     // of the accu steps (from the per-CTA sums), then the device step counter += m.
+    // persistent tcr: clear the grid barrier's words, then one cooperative launch of m steps
+    void launch_persistent(bool accu, uint32_t m, cudaStream_t st) {
+        static_assert(offsetof(bay_ctl, gbar_count) == 128 && offsetof(bay_ctl, abort) == 260,
+                      "grid barrier words of bay_ctl");
+        cuda_check(cudaMemsetAsync(&ctl->gbar_count, 0,
+                                   offsetof(bay_ctl, abort) + sizeof(unsigned int) - offsetof(bay_ctl, gbar_count),
+                                   st),
+                   "memset(grid barrier)");
+        if (st == ctx->stream) bay::count_launches(1);
+        bay_stretch_params p = make_params(0, 0);
+        void* args[] = {&p, &m};
+        CUlaunchAttribute at[1];
+        at[0].id = CU_LAUNCH_ATTRIBUTE_COOPERATIVE;
+        at[0].value.cooperative = 1;
+        CUlaunchConfig cfg{};
+        cfg.gridDimX = tr_grid;
+        cfg.gridDimY = 1;
+        cfg.gridDimZ = 1;
+        cfg.blockDimX = 256 * kTrGroups;
+        cfg.blockDimY = 1;
+        cfg.blockDimZ = 1;
+        cfg.sharedMemBytes = (unsigned)tr_smem;
+        cfg.hStream = (CUstream)st;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cu_check(g_cu.LaunchKernelEx(&cfg, (CUfunction)model->k_tr[accu ? 4 : 3], args, nullptr),
+                 "cuLaunchKernelEx(stretch, persistent)");
+    }
+
+    bool use_persistent() const { return tcr && persistent && tr_grid != 0; }
+
+    // kernels one run_chunk of m steps launches
+    uint32_t chunk_launches(bool accu, uint32_t m) const {
+        const uint32_t moves = use_persistent() ? 1u : (streaming ? 6u : 2u) * m;
+        return moves + 1u + ((accu && means_cap) ? 1u : 0u);
+    }
+
     void run_chunk(bool accu, uint32_t m, cudaStream_t st) {
-        for (uint32_t i = 0; i < m; ++i) {
-            launch_half(accu, 0, i, st);
-            launch_half(accu, 1, i, st);
+        if (use_persistent()) {
+            launch_persistent(accu, m, st);
+        } else {
+            for (uint32_t i = 0; i < m; ++i) {
+                launch_half(accu, 0, i, st);
+                launch_half(accu, 1, i, st);
+            }
         }
         if (accu && means_cap)
             cuda_check(bay::launch_reduce_means(ctl, part, means,
@@ -571,8 +623,7 @@ struct bay_sampler {
             }
             for (; done + kChunk <= n; done += kChunk) {
                 cuda_check(cudaGraphLaunch(ex, ctx->stream), "cudaGraphLaunch");
-                bay::count_launches((streaming ? 6 : 2) * kChunk + 1 +
-                                    ((accu && means_cap) ? 1 : 0));
+                bay::count_launches(chunk_launches(accu, kChunk));
             }
         }
         while (done < n) {
@@ -916,12 +967,17 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                         cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                          (int)m->tc_smem, k, dev),
                                  "cuKernelSetAttribute(smem)");
-                    const char* tr[3] = {"bay_tcr_bare", "bay_tcr_accu", "bay_tcr_logfn"};
-                    for (int i = 0; i < 3; ++i) {
+                    const char* tr[5] = {"bay_tcr_bare", "bay_tcr_accu", "bay_tcr_logfn",
+                                         "bay_tcr_run_bare", "bay_tcr_run_accu"};
+                    for (int i = 0; i < 5; ++i) {
                         cu_check(g_cu.LibraryGetKernel(&m->k_tr[i], m->lib, tr[i]), "GetKernel(tcr)");
                         cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                          (int)kGemmMaxSmem, m->k_tr[i], dev),
                                  "cuKernelSetAttribute(smem)");
+                        // the whole carveout as shared memory: 4 CTAs of about 50 KB per SM
+                        cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT,
+                                                         100, m->k_tr[i], dev),
+                                 "cuKernelSetAttribute(carveout)");
                     }
                 }
             }
@@ -992,18 +1048,26 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                 const uint64_t np = (s->gemm_rows + 15) & ~15ull, kc = (m->gemm_features + 63) / 64;
                 const uint64_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1;
                 const uint64_t img = 2 * kc * np * 128 + np * auxs * 4;
-                // image, 2 kc atoms of kTrWalkers walker rows, then the proposals and the
-                // reduction scratch -- at least the part of the M = 128 MMA's 16 KB read that
-                // runs past the last atom (walker rows kTrWalkers..127, never read back)
+                // image, then per tile group 2 kc atoms of kTrWalkers walker rows, the
+                // proposals and the reduction scratch -- at least the part of the M = 128
+                // MMA's 16 KB read that runs past the last atom (walker rows kTrWalkers..127,
+                // never read back); the group stride is BAY_TR_GREG of the kernel
                 const uint64_t atom = 128ull * kTrWalkers;
-                const uint64_t tail = std::max<uint64_t>(16384 - atom,
-                                                         (uint64_t)kTrWalkers * (m->dim | 1u) * 4 + 1024);
-                const uint64_t sm = 1024 + ((img + 1023) & ~1023ull) + 2 * kc * atom + tail;
-                if (sm <= kGemmMaxSmem) {
+                const uint64_t tail = (std::max<uint64_t>(16384 - atom,
+                                                          (uint64_t)kTrWalkers * (m->dim | 1u) * 4 + 1024) +
+                                       1023) & ~1023ull;
+                const uint64_t greg = 2 * kc * atom + tail;
+                const uint64_t base = 1024 + ((img + 1023) & ~1023ull);
+                if (base + greg <= kGemmMaxSmem) {
                     s->tc = false;
                     s->tcr = true;
-                    s->smem = (size_t)sm;
+                    s->smem = (size_t)(base + greg);
                     s->gemm_np = (uint32_t)np;
+                    // persistent form: kTrGroups groups per CTA, their accumulators within
+                    // the SM's 512 TMEM columns
+                    const uint64_t ncols = np <= 32 ? 32 : np <= 64 ? 64 : np <= 128 ? 128 : 256;
+                    const uint64_t smp = base + kTrGroups * greg;
+                    if (kTrGroups * ncols <= 512 && smp <= kGemmMaxSmem) s->tr_smem = (size_t)smp;
                 }
             }
             s->streaming = s->tc || (!s->tcr && ((m->flags & BAY_MODEL_GEMM_STREAMING) ||
@@ -1099,6 +1163,21 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                     encode_bf16_map(&s->tc_maps.bl, s->s_bl, s->tc_fp, s->tc_wpad);
                 }
             } else if (s->tcr) {
+                // persistent form: one CTA of kTrGroups tile groups per SM (all co-resident:
+                // a cooperative launch), no more CTAs than tiles
+                if (s->tr_smem) {
+                    CUfunction f = nullptr;
+                    cu_check(g_cu.KernelGetFunction(&f, m->k_tr[3]), "cuKernelGetFunction(tcr)");
+                    int per_sm = 0;
+                    cu_check(g_cu.OccupancyMaxActiveBlocks(&per_sm, f, 256 * kTrGroups, s->tr_smem),
+                             "cuOccupancy(tcr)");
+                    int n_sm = 0;
+                    cuda_check(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, c->device),
+                               "cudaDeviceGetAttribute(SMs)");
+                    // one CTA per SM: its TMEM columns are the only ones a resident CTA holds
+                    if (per_sm >= 1)
+                        s->tr_grid = (uint32_t)std::min<uint64_t>(s->grid(), (uint64_t)n_sm);
+                }
                 const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
                 const uint32_t kc = (m->gemm_features + 63) / 64;
                 const size_t img = 2ull * kc * s->gemm_np * 128 + (size_t)s->gemm_np * auxs * 4;
@@ -1200,6 +1279,23 @@ int bay_sampler_set_graphs(bay_sampler* s, int enabled) {
     return guarded([&] {
         if (!s) fail(BAY_ERR_ARG, "NULL sampler");
         s->graphs = enabled != 0;
+    });
+}
+
+int bay_sampler_set_persistent(bay_sampler* s, int enabled) {
+    return guarded([&] {
+        if (!s) fail(BAY_ERR_ARG, "NULL sampler");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        if (s->persistent == (enabled != 0)) return;
+        s->persistent = enabled != 0;
+        // the captured chunks launch the other form's kernels: capture again
+        for (cudaGraphExec_t* g : {&s->g_bare, &s->g_accu})
+            if (*g) {
+                cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+                cudaGraphExecDestroy(*g);
+                *g = nullptr;
+            }
     });
 }
 

@@ -45,7 +45,12 @@ struct bay_ctl {
     unsigned int ticket[2];
     unsigned long long accepted;
     unsigned int status;
-    unsigned int pad;
+    unsigned int pad0[21];
+    unsigned int gbar_count;   // byte 128
+    unsigned int pad1[31];
+    unsigned int gbar_gen;     // byte 256
+    unsigned int abort;
+    unsigned int pad2[30];
 };
 
 // per member (host-built, read-only on the device)

@@ -50,7 +50,12 @@ struct bay_ctl {
     unsigned int ticket[2];         // last-CTA tickets of the accu reductions
     unsigned long long accepted;    // accu: accepted proposals since the last reset
     unsigned int status;            // nonzero: a device-detected error
-    unsigned int pad;
+    unsigned int pad0[21];
+    unsigned int gbar_count;        // grid barrier of the persistent form (byte 128): arrivals
+    unsigned int pad1[31];
+    unsigned int gbar_gen;          //   (unused; byte 256)
+    unsigned int abort;             //   abandon flag; count and abort are cleared before each launch
+    unsigned int pad2[30];
 };
 
 struct bay_stretch_params {
@@ -1170,7 +1175,9 @@ __device__ __forceinline__ void bay_mma_n(unsigned int d, unsigned long long a, 
 
 // 8 consecutive floats (dims 8u .. 8u + 7) of a walker row: float4 loads when rows are
 // 16-byte aligned (DIM % 4 == 0), float2 when 8-byte aligned, else scalar; zero past DIM
-// or when !ok (no access at all)
+// or when !ok (no access at all).  In the persistent form other CTAs rewrote the rows
+// since this SM last read them: the grid barrier's acquire orders these loads after those
+// writes.
 __device__ __forceinline__ void bay_tr_ld8(const float* row, unsigned int u, bool ok, float (&v)[8]) {
     const unsigned int d0 = 8u * u;
 #pragma unroll
@@ -1222,13 +1229,94 @@ __device__ __forceinline__ void bay_tr_put_a(unsigned int s_a, unsigned int w, u
                  "r"(lw[3]) : "memory");
 }
 
-template <bool ACCU, bool LOGFN_ONLY>
-__device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
-    // Shared memory: [matrix image][A: hi atoms, lo atoms (BAY_TR_W walker rows each)][Yw][red].
+// Grid barrier k (k = 1, 2, ... within a launch) of a cooperative launch (every CTA
+// resident): each CTA adds 1 to the arrival count (a release reduction, no reply awaited)
+// and waits until the count reaches k * nblocks; the count only grows during a launch.
+// Bounded: a CTA that waits longer than BAY_TC_WAIT_NS raises ctl->abort and status bit 4;
+// a raised abort ends every wait at once.  Returns false when the launch is being
+// abandoned.  The count and the abort word are cleared before each launch.
+__device__ __forceinline__ bool bay_grid_barrier(bay_ctl* ctl, unsigned int nblocks, unsigned int k) {
+    __shared__ unsigned int s_go;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int go = 1u;
+        volatile unsigned int* ab = &ctl->abort;
+        if (*ab) {
+            go = 0u;
+        } else {
+            const unsigned int target = k * nblocks;
+            __threadfence();                               // the CTA's writes before its arrival
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&ctl->gbar_count) : "memory");
+            unsigned long long t0 = bay_globaltimer();
+            for (unsigned int it = 0;; ++it) {
+                unsigned int c;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(&ctl->gbar_count) : "memory");
+                if (c >= target) break;
+                __nanosleep(32);
+                if ((it & 63u) == 63u) {
+                    if (*ab) {
+                        go = 0u;
+                        break;
+                    }
+                    if (bay_globaltimer() - t0 > BAY_TC_WAIT_NS) {
+                        *ab = 1u;
+                        atomicOr(&ctl->status, 4u);
+                        go = 0u;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+        }
+        s_go = go;
+    }
+    __syncthreads();
+    return s_go != 0u;
+}
+
+// Named barrier of one 256-thread tile group (ids 1..4; id 0 is the CTA's __syncthreads)
+__device__ __forceinline__ void bay_gsync(unsigned int g) {
+    asm volatile("bar.sync %0, 256;" ::"r"(g + 1u) : "memory");
+}
+__device__ __forceinline__ int bay_gsync_count(unsigned int g, bool p) {
+    int n;
+    asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n bar.red.popc.u32 %0, %1, 256, q;\n}\n"
+                 : "=r"(n) : "r"(g + 1u), "r"((unsigned int)p) : "memory");
+    return n;
+}
+__device__ __forceinline__ bool bay_gsync_and(unsigned int g, bool p) {
+    unsigned int r;
+    asm volatile("{\n .reg .pred q, o;\n setp.ne.u32 q, %2, 0;\n bar.red.and.pred o, %1, 256, q;\n"
+                 " selp.u32 %0, 1, 0, o;\n}\n"
+                 : "=r"(r) : "r"(g + 1u), "r"((unsigned int)p) : "memory");
+    return r != 0u;
+}
+
+// Shared memory of one tile group after the A atoms: the proposals Yw [BAY_TR_W][DPAD] and
+// 256 floats of reduction scratch, at least the 8 KB past the last atom that the M = 128
+// MMA reads (walker rows 64..127 of a 64-walker tile, never read back); 1 KB multiple.
+#define BAY_TR_TAIL_RAW ((BAY_TR_W * BAY_TR_DPAD * 4u + 1024u) > (16384u - BAY_TR_ATOM) \
+                         ? (BAY_TR_W * BAY_TR_DPAD * 4u + 1024u) : (16384u - BAY_TR_ATOM))
+#define BAY_TR_TAIL ((BAY_TR_TAIL_RAW + 1023u) & ~1023u)
+#define BAY_TR_GREG (2u * BAY_TC_KC * BAY_TR_ATOM + BAY_TR_TAIL)   // bytes per tile group
+
+// The resident tensor-core form.  A CTA holds G independent tile groups of 256 threads
+// (G = 1: an ordinary CTA); each group has its own A operand, proposals, scratch, MMA
+// barrier and TMEM columns, and syncs on its own named barrier; the matrix image is shared.
+// PERSIST = false: one half-step (P.half, P.step_off), tile blockIdx.x (G = 1), launched
+// with programmatic dependent launch.  PERSIST = true: a cooperative launch of m steps
+// (both halves each, step offsets P.step_off .. + m - 1) over a grid of co-resident CTAs
+// whose groups take tiles (g * gridDim.x + blockIdx.x) + k * gridDim.x * G of every half-step, with
+// a grid barrier between half-steps; barriers, TMEM and the image are set up once.  Every
+// tile computes what the per-launch form computes (same statistics slots), so the two
+// forms give identical results.  A group whose bounded wait gives up raises ctl->abort
+// and goes on to the next grid barrier, where the whole launch stops.
+template <bool ACCU, bool LOGFN_ONLY, bool PERSIST, unsigned int G>
+__device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, unsigned int m) {
+    // Shared memory: [matrix image][group 0: A hi atoms, lo atoms, Yw, red][group 1 ...].
     // The MMA runs M = 128 (an M = 64 form was measured no faster): with 64-walker tiles it
-    // also reads the 8 KB after each atom's 64 rows (the next atom, or Yw and the slack
-    // after A's last atom) as walker rows 64..127, whose accumulator lanes are never read;
-    // the host reserves at least 8 KB after the last atom.
+    // also reads the 8 KB after each atom's 64 rows (the next atom, or the group's Yw) as
+    // walker rows 64..127, whose accumulator lanes are never read.
     extern __shared__ __align__(1024) unsigned char bay_smem_tr[];
     const unsigned int NP = P.gemm_np;                       // rows padded to 16
     const unsigned int rows = (unsigned int)P.gemm_rows;
@@ -1236,77 +1324,103 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     const unsigned int pad = ((raw + 1023u) & ~1023u) - raw;
     unsigned char* sm = bay_smem_tr + pad;
     const unsigned int img_bytes = 2u * BAY_TC_KC * NP * 128u + NP * BAY_AUXS * 4u;
-    const unsigned int a_off = (img_bytes + 1023u) & ~1023u;
-    const unsigned int s_img = raw + pad, s_a = s_img + a_off;
+    const unsigned int a_off0 = (img_bytes + 1023u) & ~1023u;
+    const unsigned int s_img = raw + pad;
     const float* Aux = (const float*)(sm + 2u * BAY_TC_KC * NP * 128u);     // [NP][AUXS]
-    float* Yw = (float*)(sm + a_off + 2u * BAY_TC_KC * BAY_TR_ATOM);         // [64][DPAD]
-    float* red = Yw + BAY_TR_W * BAY_TR_DPAD;                                // [8][32]
-    __shared__ float sZ[BAY_TR_W], sU2[BAY_TR_W], sW[BAY_TR_W], sLx[BAY_TR_W];
-    __shared__ unsigned int sJ[BAY_TR_W];
-    __shared__ float sPrep[BAY_TR_W][BAY_PREP_LEN];
-    __shared__ float sHalf[BAY_TR_W][2];
-    __shared__ unsigned char sAcc[BAY_TR_W];
-    __shared__ __align__(8) unsigned long long sBar[2];
-    __shared__ unsigned int sTmem, sOk;
+    __shared__ float sZ[G][BAY_TR_W], sU2[G][BAY_TR_W], sW[G][BAY_TR_W], sLx[G][BAY_TR_W];
+    __shared__ unsigned int sJ[G][BAY_TR_W];
+    __shared__ float sPrep[G][BAY_TR_W][BAY_PREP_LEN];
+    __shared__ float sHalf[G][BAY_TR_W][2];
+    __shared__ unsigned char sAcc[G][BAY_TR_W];
+    __shared__ __align__(8) unsigned long long sBar[1 + G];
+    __shared__ unsigned int sTmem, sOk[G];
 
     const unsigned int kind = ACCU ? 1u : 0u;
-    const unsigned int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    const unsigned int k0 = blockIdx.x * BAY_TR_W;
+    const unsigned int g = G == 1u ? 0u : threadIdx.x >> 8;                // tile group
+    const unsigned int tid = threadIdx.x & 255u, warp = tid >> 5, lane = tid & 31u;
     const unsigned int nk = LOGFN_ONLY ? P.W : P.K;
-    const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
+    const unsigned int ntiles = (nk + BAY_TR_W - 1u) / BAY_TR_W;
     const float* hyper = P.params + P.data_len;
-    float* X = P.xs + (LOGFN_ONLY ? 0 : (size_t)P.half * P.K * DIM);
-    const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM;
+    const unsigned int a_off = a_off0 + g * BAY_TR_GREG;
+    const unsigned int s_a = s_img + a_off;
+    float* Yw = (float*)(sm + a_off + 2u * BAY_TC_KC * BAY_TR_ATOM);         // [W][DPAD]
+    float* red = Yw + BAY_TR_W * BAY_TR_DPAD;                                // [256]
     const unsigned int bar_img = (unsigned int)__cvta_generic_to_shared(&sBar[0]);
-    const unsigned int bar_mma = (unsigned int)__cvta_generic_to_shared(&sBar[1]);
+    const unsigned int bar_mma = (unsigned int)__cvta_generic_to_shared(&sBar[1 + g]);
     unsigned int* status = &P.ctl->status;
     const unsigned int ncols = NP <= 32u ? 32u : (NP <= 64u ? 64u : (NP <= 128u ? 128u : 256u));
 
-    // 1. barriers, TMEM, and the matrix image's bulk copy (overlaps the proposals)
-    if (tid == 0) {
+    // 1. barriers, TMEM (G x ncols columns), and the matrix image's bulk copy
+    if (threadIdx.x == 0) {
         bay_mbar_init(bar_img, 1u);
-        bay_mbar_init(bar_mma, 1u);
+        for (unsigned int q = 0; q < G; ++q)
+            bay_mbar_init((unsigned int)__cvta_generic_to_shared(&sBar[1 + q]), 1u);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    if (warp == 0) {
+    if (threadIdx.x < 32u) {
         const unsigned int dst = (unsigned int)__cvta_generic_to_shared(&sTmem);
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(dst), "r"(ncols) : "memory");
+                     ::"r"(dst), "r"(ncols * G) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     bay_tc_fence_before();
     __syncthreads();
     bay_tc_fence_after();
-    const unsigned int tmem = sTmem;
-    // nothing above reads device memory: with a programmatic dependent launch this CTA may
-    // have started before the previous kernel of the stream finished; wait for it (and its
-    // memory) here, then let the next launch start its own set-up
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    const unsigned int step = P.ctl->step[kind] + P.step_off;
-    if (tid == 0) {
+    const unsigned int tmem = sTmem + g * ncols;
+    if (!PERSIST) {
+        // nothing above reads device memory: with a programmatic dependent launch this CTA
+        // may have started before the previous kernel of the stream finished; wait for it
+        // (and its memory) here, then let the next launch start its own set-up
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
         bay_expect_tx(bar_img, img_bytes);
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
             ::"r"(s_img), "l"(P.gemm_lay), "r"(img_bytes), "r"(bar_img) : "memory");
     }
+    unsigned int mma_par = 0u;                  // phase parity of bar_mma's next completion
+    const unsigned int nsteps = PERSIST ? m : 1u;
+    const unsigned int h_lo = (PERSIST && !LOGFN_ONLY) ? 0u : P.half;
+    const unsigned int h_hi = (PERSIST && !LOGFN_ONLY) ? 2u : P.half + 1u;
+    // control words, constant during a launch
+    const unsigned int step0 = P.ctl->step[kind], seed0 = P.ctl->seed[kind];
+    const float a_str = P.ctl->a, beta = ACCU ? 1.0f : P.ctl->beta;
+    // tiles g * gridDim.x + blockIdx.x, + G * gridDim.x, ...: consecutive tiles on
+    // different SMs, every SM busy when the tiles outnumber the CTAs
+    const unsigned int tile0 = g * gridDim.x + blockIdx.x;
+    const unsigned int tstride = PERSIST ? gridDim.x * G : ntiles;
+    bool go = true;
+    for (unsigned int si = 0; si < nsteps && go; ++si) {
+    for (unsigned int half = h_lo; half < h_hi && go; ++half) {
+    if (PERSIST && (si | (half - h_lo)) != 0u)
+        go = bay_grid_barrier(P.ctl, gridDim.x, 2u * si + (half - h_lo));
+    if (!go) break;
+    const unsigned int step_off = P.step_off + si;
+    const unsigned int step = step0 + step_off;
+    float* X = P.xs + (LOGFN_ONLY ? 0 : (size_t)half * P.K * DIM);
+    const float* S = P.xs + (size_t)(1u - half) * P.K * DIM;
+    for (unsigned int tile = tile0; tile < ntiles; tile += tstride) {
+    const unsigned int k0 = tile * BAY_TR_W;
+    const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
     // 2. proposals (Philox, z, partner) of the tile
     if (!LOGFN_ONLY && tid < nt) {
         const unsigned int k = k0 + tid;
-        const unsigned int stream = ACCU ? (P.half ? 2222u : 1111u) : (P.half ? 4444u : 3333u);
+        const unsigned int stream = ACCU ? (half ? 2222u : 1111u) : (half ? 4444u : 3333u);
         bay_u4 c;
         c.x = k;
         c.y = step;
         c.z = stream;
         c.w = 0xbeeff00du;
-        const bay_u4 r = bay_philox4x32_10(c, P.ctl->seed[kind] + P.half, 0xdecafbadu);
-        sZ[tid] = bay_stretch_z(P.ctl->a, bay_u01(r.y));
-        sJ[tid] = bay_partner(bay_u01(r.x), P.K);
-        sU2[tid] = bay_u01(r.z);
-        sLx[tid] = P.logfn[(size_t)P.half * P.K + k];
+        const bay_u4 r = bay_philox4x32_10(c, seed0 + half, 0xdecafbadu);
+        sZ[g][tid] = bay_stretch_z(a_str, bay_u01(r.y));
+        sJ[g][tid] = bay_partner(bay_u01(r.x), P.K);
+        sU2[g][tid] = bay_u01(r.z);
+        sLx[g][tid] = P.logfn[(size_t)half * P.K + k];
     }
-    __syncthreads();
+    bay_gsync(g);
     // 3. Y of the tile (walker-major rows of odd stride) from (walker, 8-dim unit) items:
     //    consecutive threads take consecutive units of a row (the tile's own rows are one
     //    contiguous block, a partner's row is 4 * DIM contiguous bytes), IB items' loads in
@@ -1324,7 +1438,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             const unsigned int w = q / NU, u = q - w * NU;
             const bool ok = q < NQ && w < nt;
             bay_tr_ld8(Xt + (size_t)w * DIM, u, ok, xv[b]);
-            if (!LOGFN_ONLY) bay_tr_ld8(S + (size_t)sJ[ok ? w : 0u] * DIM, u, ok, sv[b]);
+            if (!LOGFN_ONLY) bay_tr_ld8(S + (size_t)sJ[g][ok ? w : 0u] * DIM, u, ok, sv[b]);
         }
 #pragma unroll
         for (unsigned int b = 0; b < IB; ++b) {
@@ -1332,7 +1446,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             if (q < NQ) {
                 const unsigned int w = q / NU, u = q - w * NU;
                 float y[8];
-                const float z = LOGFN_ONLY ? 0.0f : sZ[w];
+                const float z = LOGFN_ONLY ? 0.0f : sZ[g][w];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     y[i] = LOGFN_ONLY ? xv[b][i]
@@ -1359,15 +1473,15 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     if (BAY_TC_KC * 8u > NU) {
         constexpr unsigned int NZ = BAY_TC_KC * 8u > NU ? BAY_TC_KC * 8u - NU : 1u;
         const unsigned int zw[4] = {0u, 0u, 0u, 0u};
-        for (unsigned int q = tid; q < BAY_TR_W * NZ; q += blockDim.x) {
+        for (unsigned int q = tid; q < BAY_TR_W * NZ; q += 256u) {
             const unsigned int w = q / NZ;
             bay_tr_put_a(s_a, w, NU + (q - w * NZ), zw, zw);
         }
     }
 #else
     // 4. the A operand from Yw (coefficients at dim BAY_GEMM_COEF): 16-byte units of hi, lo
-    __syncthreads();
-    for (unsigned int q = tid; q < BAY_TR_W * BAY_TC_KC * 8u; q += blockDim.x) {
+    bay_gsync(g);
+    for (unsigned int q = tid; q < BAY_TR_W * BAY_TC_KC * 8u; q += 256u) {
         const unsigned int w = q / (BAY_TC_KC * 8u), u = q - w * (BAY_TC_KC * 8u);
         unsigned int hw[4], lw[4];
 #pragma unroll
@@ -1381,10 +1495,10 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
     }
 #endif
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // A visible to the MMAs
-    __syncthreads();
+    bay_gsync(g);
     // 5. one thread: wait for the image, issue the MMAs, commit; the others precompute
     if (tid == 0) {
-        unsigned int ok = bay_tc_wait(bar_img, 0u, nullptr, status) ? 1u : 0u;
+        unsigned int ok = bay_tc_wait(bar_img, 0u, nullptr, status) ? 1u : 0u;   // once done, stays
         if (ok) {
             bay_tc_fence_after();
             const unsigned int idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((NP >> 3) << 17) |
@@ -1405,7 +1519,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             }
         }
         bay_mma_commit(bar_mma);   // also arrives with nothing issued (a failed wait)
-        sOk = ok;
+        sOk[g] = ok;
     }
     if (tid < BAY_TR_W) {
         float pr[BAY_PREP_LEN];
@@ -1417,16 +1531,17 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             wt = BAY_GEMM_WALKER(P.gemm_rows, hyper, P.params_len, DIM, &Yw[tid * BAY_TR_DPAD]);
         }
 #pragma unroll
-        for (int i = 0; i < BAY_PREP_LEN; ++i) sPrep[tid][i] = pr[i];
-        sW[tid] = wt;
+        for (int i = 0; i < BAY_PREP_LEN; ++i) sPrep[g][tid][i] = pr[i];
+        sW[g][tid] = wt;
     }
     // every thread waits for the MMAs (bounded; the commit arrives even if none were issued)
     // and observes the image copy itself before reading the aux values it brought
-    bay_tc_wait(bar_mma, 0u, nullptr, status);
-    bay_tc_wait(bar_img, 0u, nullptr, status);
-    __syncthreads();
+    const bool mma_done = bay_tc_wait(bar_mma, mma_par, nullptr, status);
+    mma_par ^= 1u;
+    const bool img_done = bay_tc_wait(bar_img, 0u, nullptr, status);
+    // one verdict for the whole CTA (a wait that gave up in any thread fails the tile)
+    const bool ok = bay_gsync_and(g, mma_done && img_done) && sOk[g] != 0u;
     bay_tc_fence_after();
-    const bool ok = sOk != 0u;
     // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
     //    rows [NP/2 * (w / 4), + NP/2) in 8-column loads; the two halves then combine
     if (32u * (warp & 3u) < BAY_TR_W) {
@@ -1442,7 +1557,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
 #pragma unroll
             for (unsigned int i = 0; i < 8u; ++i) {
                 const unsigned int r = c0 + j0 + i;
-                v[i] = r < rows ? BAY_GEMM_TERM(v[i], &Aux[r * BAY_AUXS], (uint64_t)r, xw, sPrep[wl]) : 0.0f;
+                v[i] = r < rows ? BAY_GEMM_TERM(v[i], &Aux[r * BAY_AUXS], (uint64_t)r, xw, sPrep[g][wl]) : 0.0f;
             }
 #pragma unroll
             for (unsigned int s2 = 4u; s2 >= 1u; s2 >>= 1)
@@ -1454,38 +1569,38 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             sum = t;
         }
         if (h) {                                        // second half of the rows
-            sHalf[wl][0] = sum;
-            sHalf[wl][1] = -cmp;
+            sHalf[g][wl][0] = sum;
+            sHalf[g][wl][1] = -cmp;
         } else {                                        // first half: red[wl], red[W + wl]
             red[wl] = sum;
             red[BAY_TR_W + wl] = -cmp;
         }
     }
     bay_tc_fence_before();
-    __syncthreads();
+    bay_gsync(g);
     // 7. accept (one thread per walker), write-back, statistics
     bool accepted = false;
     if (tid < nt && ok) {
         const unsigned int k = k0 + tid;
         bay_cf t, a, b;
-        t.hi = sW[tid];
+        t.hi = sW[g][tid];
         t.lo = 0.0f;
         a.hi = red[tid];
         a.lo = red[BAY_TR_W + tid];
-        b.hi = sHalf[tid][0];
-        b.lo = sHalf[tid][1];
+        b.hi = sHalf[g][tid][0];
+        b.lo = sHalf[g][tid][1];
         t = bay_cadd(t, bay_cadd(a, b));
         const float ly = __fadd_rn(t.hi, t.lo);
         if (LOGFN_ONLY) {
             P.logfn[k] = ly;
         } else {
-            accepted = bay_accept(sU2[tid], sZ[tid], ly, sLx[tid], ACCU ? 1.0f : P.ctl->beta);
-            if (accepted) P.logfn[(size_t)P.half * P.K + k] = ly;
+            accepted = bay_accept(sU2[g][tid], sZ[g][tid], ly, sLx[g][tid], beta);
+            if (accepted) P.logfn[(size_t)half * P.K + k] = ly;
         }
     }
     if (!LOGFN_ONLY) {
-        if (tid < BAY_TR_W) sAcc[tid] = accepted ? 1 : 0;
-        const int n_acc = __syncthreads_count(accepted);
+        if (tid < BAY_TR_W) sAcc[g][tid] = accepted ? 1 : 0;
+        const int n_acc = bay_gsync_count(g, accepted);
         if (ACCU) {
             // the statistics need every walker's new position in Yw: the rejected walkers'
             // current rows are loaded (IB units in flight per thread), the accepted ones
@@ -1496,7 +1611,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                 for (unsigned int b = 0; b < IB; ++b) {
                     const unsigned int q = q0 + b * 256u + tid;
                     const unsigned int w = q / NU, u = q - w * NU;
-                    bay_tr_ld8(Xt + (size_t)w * DIM, u, q < NQ && w < nt && !sAcc[w < BAY_TR_W ? w : 0u],
+                    bay_tr_ld8(Xt + (size_t)w * DIM, u, q < NQ && w < nt && !sAcc[g][w < BAY_TR_W ? w : 0u],
                                xv[b]);
                 }
 #pragma unroll
@@ -1505,7 +1620,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                     const unsigned int w = q / NU, u = q - w * NU;
                     if (q < NQ && w < nt) {
                         float* yr = &Yw[w * BAY_TR_DPAD + 8u * u];
-                        if (sAcc[w]) {
+                        if (sAcc[g][w]) {
                             float y[8];
 #pragma unroll
                             for (int i = 0; i < 8; ++i) y[i] = 8u * u + i < DIM ? yr[i] : 0.0f;
@@ -1520,9 +1635,9 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
             }
         } else {
             // accepted walkers' rows to device memory
-            for (unsigned int q = tid; q < NQ; q += blockDim.x) {
+            for (unsigned int q = tid; q < NQ; q += 256u) {
                 const unsigned int w = q / NU, u = q - w * NU;
-                if (w < nt && sAcc[w]) {
+                if (w < nt && sAcc[g][w]) {
                     const float* yr = &Yw[w * BAY_TR_DPAD + 8u * u];
                     float y[8];
 #pragma unroll
@@ -1534,16 +1649,15 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
         if (ACCU) {
             if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
             if (P.means_cap != 0) {
-                __syncthreads();
+                bay_gsync(g);
                 // per-dim sums of the tile's new positions in one pass: NG = 256 / DIM groups
                 // (at most 8) of WG consecutive walkers, thread (g, d) sums group g of dim d in
                 // fp32 in walker order, then thread d adds the groups' sums in group order
                 // (the per-step means add the CTAs' sums in FP64)
                 constexpr unsigned int NG = DIM >= 128u ? 1u : (256u / DIM < 8u ? 256u / DIM : 8u);
                 constexpr unsigned int WG = (BAY_TR_W + NG - 1u) / NG;
-                float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x
-                    + blockIdx.x;
-                for (unsigned int t = tid; t < NG * DIM; t += blockDim.x) {
+                float* out = P.part + ((size_t)step_off * 2 + half) * DIM * ntiles + tile;
+                for (unsigned int t = tid; t < NG * DIM; t += 256u) {
                     const unsigned int g = t / DIM, d = t - g * DIM;
                     float v = 0.0f;
 #pragma unroll
@@ -1551,38 +1665,62 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P) {
                         const unsigned int w = g * WG + i;
                         if (w < nt) v = __fadd_rn(v, Yw[w * BAY_TR_DPAD + d]);
                     }
-                    if (NG == 1u) out[(size_t)d * gridDim.x] = v;
+                    if (NG == 1u) out[(size_t)d * ntiles] = v;
                     else red[t] = v;                    // NG * DIM <= 256 floats
                 }
                 if (NG > 1u) {
-                    __syncthreads();
+                    bay_gsync(g);
                     if (tid < DIM) {
                         float a = 0.0f;
 #pragma unroll
                         for (unsigned int g = 0; g < NG; ++g) a = __fadd_rn(a, red[g * DIM + tid]);
-                        out[(size_t)tid * gridDim.x] = a;
+                        out[(size_t)tid * ntiles] = a;
                     }
                 }
             }
         }
     }
-    // 8. release TMEM (every MMA completed before the epilogue read it)
-    if (warp == 0) {
-        __syncwarp();
+    if (PERSIST) {
+        // the next tile rewrites Yw, red and the A operand, and its MMAs the accumulator
+        bay_tc_fence_before();
+        bay_gsync(g);
+    }
+    if (!ok) {
+        // a bounded wait gave up: no more tiles; the persistent form raises the abort flag
+        // and still meets the next grid barrier, which then stops the whole launch
+        if (PERSIST && tid == 0) *(volatile unsigned int*)&P.ctl->abort = 1u;
+        break;
+    }
+    }   // tiles
+    }   // halves
+    }   // steps
+    // 8. release TMEM (every MMA completed before the epilogue read it); the image copy has
+    //    landed (a group waited for it, or the bounded wait here)
+    if (threadIdx.x == 0) bay_tc_wait(bar_img, 0u, nullptr, status);
+    bay_tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32u) {
         bay_tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"(ncols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(sTmem),
+                     "r"(ncols * G) : "memory");
     }
 }
 
 extern "C" __global__ void __launch_bounds__(256) bay_tcr_bare(bay_stretch_params P) {
-    bay_stretch_tcr<false, false>(P);
+    bay_stretch_tcr<false, false, false, 1u>(P, 1u);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_tcr_accu(bay_stretch_params P) {
-    bay_stretch_tcr<true, false>(P);
+    bay_stretch_tcr<true, false, false, 1u>(P, 1u);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_tcr_logfn(bay_stretch_params P) {
-    bay_stretch_tcr<false, true>(P);
+    bay_stretch_tcr<false, true, false, 1u>(P, 1u);
+}
+// persistent: one CTA of 4 tile groups per SM (1,024 threads, 64 registers each)
+extern "C" __global__ void __launch_bounds__(1024, 1) bay_tcr_run_bare(bay_stretch_params P, unsigned int m) {
+    bay_stretch_tcr<false, false, true, 4u>(P, m);
+}
+extern "C" __global__ void __launch_bounds__(1024, 1) bay_tcr_run_accu(bay_stretch_params P, unsigned int m) {
+    bay_stretch_tcr<true, false, true, 4u>(P, m);
 }
 #endif  // BAY_GEMM_TC
 

@@ -450,6 +450,11 @@ class GB300Stretch:
     def set_graphs(self, enabled):
         N.call("bay_sampler_set_graphs", self.handle, 1 if enabled else 0)
 
+    def set_persistent(self, enabled):
+        """Resident tensor-core GEMM form: one persistent cooperative launch per chunk of
+        steps, or one launch per half-step (default); both give the same results."""
+        N.call("bay_sampler_set_persistent", self.handle, 1 if enabled else 0)
+
     # ---------------------------------------------------------------- MCMC
     def init(self, seed):
         N.call("bay_init", self.handle, seed & 0xffffffff)

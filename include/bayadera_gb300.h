@@ -272,6 +272,11 @@ int bay_logfn_values(bay_sampler* s, float* out);
 
 /* Execution control: CUDA-graph replay of the step loops (default on). */
 int bay_sampler_set_graphs(bay_sampler* s, int enabled);
+/* Execution control of the resident tensor-core GEMM form: one persistent cooperative
+ * launch per chunk of steps with a grid barrier between half-steps, or one launch per
+ * half-step with programmatic dependent launch (default: faster on GB300).  Both give the
+ * same results; other forms ignore it. */
+int bay_sampler_set_persistent(bay_sampler* s, int enabled);
 
 /* ---------------------------------------------------------------- direct samplers
  * Replace GTXDirectSamplerEngine.sample (nvidia_gtx.clj:48-63) over

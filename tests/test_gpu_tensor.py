@@ -366,3 +366,32 @@ def test_tcr_run_sampler_matches_simt(factory, M, D):
         sf.release()
     a = rates[False]
     assert abs(rates[True] - a) <= 3 * np.sqrt(2 * a * (1 - a) / (W * 200)) + 0.005
+
+
+@pytest.mark.parametrize("D,W", [(50, 4096), (10, 89600), (64, 2 * (64 * 5 + 17))])
+def test_tcr_persistent_matches_per_launch(factory, M, D, W):
+    """Resident tensor-core form: the persistent cooperative launch (a chunk of steps per
+    launch, grid barriers between half-steps, several tiles per CTA when the tiles
+    outnumber the resident CTAs: 700 tiles for 89,600 walkers) and one launch per
+    half-step give bit-identical positions, log densities, per-step means and acceptance
+    (a partial last tile in the third case)."""
+    rng = np.random.default_rng(D)
+    A = rng.normal(size=(D, D))
+    P = (A @ A.T / D + np.eye(D)).astype(np.float32)
+    out = {}
+    for persist in (True, False):
+        sf = factory.mcmc_factory(M.mvn_precision_model(D), form="gemm", tensor=True)
+        s = sf.create_sampler(23, W, P.reshape(-1))
+        s.set_persistent(persist)
+        s.init_position_normal(4, 0.0, 1.0)
+        s.burn_in(40, 2.0)
+        r = s.run_sampler(37, 2.0, return_means=True)
+        out[persist] = (s.positions().copy(), s.logfn().copy(), r["means"].copy(),
+                        r["acceptance_rate"])
+        s.release()
+        sf.release()
+    a, b = out[True], out[False]
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    np.testing.assert_array_equal(a[2], b[2])
+    assert a[3] == b[3]
