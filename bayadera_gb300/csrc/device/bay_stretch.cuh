@@ -1658,11 +1658,11 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
                 constexpr unsigned int WG = (BAY_TR_W + NG - 1u) / NG;
                 float* out = P.part + ((size_t)step_off * 2 + half) * DIM * ntiles + tile;
                 for (unsigned int t = tid; t < NG * DIM; t += 256u) {
-                    const unsigned int g = t / DIM, d = t - g * DIM;
+                    const unsigned int wg = t / DIM, d = t - wg * DIM;    // walker group, dim
                     float v = 0.0f;
 #pragma unroll
                     for (unsigned int i = 0; i < WG; ++i) {
-                        const unsigned int w = g * WG + i;
+                        const unsigned int w = wg * WG + i;
                         if (w < nt) v = __fadd_rn(v, Yw[w * BAY_TR_DPAD + d]);
                     }
                     if (NG == 1u) out[(size_t)d * ntiles] = v;
@@ -1673,7 +1673,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
                     if (tid < DIM) {
                         float a = 0.0f;
 #pragma unroll
-                        for (unsigned int g = 0; g < NG; ++g) a = __fadd_rn(a, red[g * DIM + tid]);
+                        for (unsigned int wg = 0; wg < NG; ++wg) a = __fadd_rn(a, red[wg * DIM + tid]);
                         out[(size_t)tid * ntiles] = a;
                     }
                 }
