@@ -191,8 +191,7 @@ struct bay_model {
     // shared-memory stages, dynamic shared memory
     CUkernel k_gt[2] = {nullptr, nullptr};
     // GEMM form on the tensor cores with the matrix resident: [bare, accu, logfn]
-    CUkernel k_tr[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // bare, accu, logfn,
-                                                                         // persistent bare, accu
+    CUkernel k_tr[5] = {};   // bare, accu, logfn, persistent bare, persistent accu
     uint32_t tc_g = 0, tc_stages = 0;
     size_t tc_smem = 0;
     // batch form: propose / accept in k_gp / k_ga, rows in k_gr, per-step means here
