@@ -148,6 +148,22 @@ def cpu_sample(steps_budget_s=12.0, walkers=WALKERS):
             "sample": "%d ensemble steps of the %d-walker 50-D job (%.1f s)" % (n, walkers, dt)}
 
 
+def max_over_ranks(t, dist, device):
+    """The timed region's length, maximised over the ranks: the slowest replica bounds the
+    whole job.  One rank (dist None) returns t unchanged."""
+    if dist is None:
+        return float(t)
+    import torch
+    x = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def replica_throughput(jobs, world, t_total):
+    """Whole-job walker-steps/s of `world` replicas that each ran `jobs` full jobs."""
+    return WALKERS * (BURN + RUN) * jobs * world / t_total
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -583,12 +599,8 @@ def main():
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
         barrier()
-        t_total = sum(times)
-        if dist is not None:
-            t = torch.tensor([t_total], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            t_total = float(t.item())
-        return WALKERS * (BURN + RUN) * steps * world / t_total, t_total, results
+        t_total = max_over_ranks(sum(times), dist, "cuda")
+        return replica_throughput(steps, world, t_total), t_total, results
 
     # headline: the GEMM form on the tensor cores (64-walker tiles, x'Px as a split-bf16
     # tcgen05 product against the resident precision matrix)
