@@ -191,7 +191,7 @@ struct bay_model {
     // shared-memory stages, dynamic shared memory
     CUkernel k_gt[2] = {nullptr, nullptr};
     // GEMM form on the tensor cores with the matrix resident: [bare, accu, logfn]
-    CUkernel k_tr[5] = {};   // bare, accu, logfn, persistent bare, persistent accu
+    CUkernel k_tr[6] = {};   // bare, accu, logfn, persistent bare, persistent accu, statistics
     uint32_t tc_g = 0, tc_stages = 0;
     size_t tc_smem = 0;
     // batch form: propose / accept in k_gp / k_ga, rows in k_gr, per-step means here
@@ -560,10 +560,14 @@ struct bay_sampler {
 
     bool use_persistent() const { return tcr && persistent && tr_grid != 0; }
 
+    // per-launch resident tensor-core accu steps sum each half-step's positions in the
+    // next launch; the chunk's last half-step has a statistics launch of its own
+    bool tail_stats(bool accu) const { return accu && means_cap && tcr && !use_persistent(); }
+
     // kernels one run_chunk of m steps launches
     uint32_t chunk_launches(bool accu, uint32_t m) const {
         const uint32_t moves = use_persistent() ? 1u : (streaming ? 6u : 2u) * m;
-        return moves + 1u + ((accu && means_cap) ? 1u : 0u);
+        return moves + 1u + ((accu && means_cap) ? 1u : 0u) + (tail_stats(accu) ? 1u : 0u);
     }
 
     void run_chunk(bool accu, uint32_t m, cudaStream_t st) {
@@ -573,6 +577,14 @@ struct bay_sampler {
             for (uint32_t i = 0; i < m; ++i) {
                 launch_half(accu, 0, i, st);
                 launch_half(accu, 1, i, st);
+            }
+            if (tail_stats(accu)) {
+                if (st == ctx->stream) bay::count_launches(1);
+                bay_stretch_params p = make_params(1, m - 1);
+                void* args[] = {&p};
+                cu_check(g_cu.LaunchKernel((CUfunction)model->k_tr[5], grid(), 1, 1, 256, 1, 1, 0,
+                                           (CUstream)st, args, nullptr),
+                         "cuLaunchKernel(statistics)");
             }
         }
         if (accu && means_cap)
@@ -966,9 +978,9 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                         cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                          (int)m->tc_smem, k, dev),
                                  "cuKernelSetAttribute(smem)");
-                    const char* tr[5] = {"bay_tcr_bare", "bay_tcr_accu", "bay_tcr_logfn",
-                                         "bay_tcr_run_bare", "bay_tcr_run_accu"};
-                    for (int i = 0; i < 5; ++i) {
+                    const char* tr[6] = {"bay_tcr_bare", "bay_tcr_accu", "bay_tcr_logfn",
+                                         "bay_tcr_run_bare", "bay_tcr_run_accu", "bay_tcr_stats"};
+                    for (int i = 0; i < 6; ++i) {
                         cu_check(g_cu.LibraryGetKernel(&m->k_tr[i], m->lib, tr[i]), "GetKernel(tcr)");
                         cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                          (int)kGemmMaxSmem, m->k_tr[i], dev),
@@ -1053,7 +1065,7 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                 // never read back); the group stride is BAY_TR_GREG of the kernel
                 const uint64_t atom = 128ull * kTrWalkers;
                 const uint64_t tail = (std::max<uint64_t>(16384 - atom,
-                                                          (uint64_t)kTrWalkers * (m->dim | 1u) * 4 + 1024) +
+                                                          (uint64_t)kTrWalkers * (m->dim | 1u) * 4 + 2048) +
                                        1023) & ~1023ull;
                 const uint64_t greg = 2 * kc * atom + tail;
                 const uint64_t base = 1024 + ((img + 1023) & ~1023ull);

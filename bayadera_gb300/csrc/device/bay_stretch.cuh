@@ -1293,12 +1293,48 @@ __device__ __forceinline__ bool bay_gsync_and(unsigned int g, bool p) {
 }
 
 // Shared memory of one tile group after the A atoms: the proposals Yw [BAY_TR_W][DPAD] and
-// 256 floats of reduction scratch, at least the 8 KB past the last atom that the M = 128
-// MMA reads (walker rows 64..127 of a 64-walker tile, never read back); 1 KB multiple.
-#define BAY_TR_TAIL_RAW ((BAY_TR_W * BAY_TR_DPAD * 4u + 1024u) > (16384u - BAY_TR_ATOM) \
-                         ? (BAY_TR_W * BAY_TR_DPAD * 4u + 1024u) : (16384u - BAY_TR_ATOM))
+// 2 x 256 floats of reduction scratch, at least the 8 KB past the last atom that the
+// M = 128 MMA reads (walker rows 64..127 of a 64-walker tile, never read back); 1 KB
+// multiple.
+#define BAY_TR_TAIL_RAW ((BAY_TR_W * BAY_TR_DPAD * 4u + 2048u) > (16384u - BAY_TR_ATOM) \
+                         ? (BAY_TR_W * BAY_TR_DPAD * 4u + 2048u) : (16384u - BAY_TR_ATOM))
 #define BAY_TR_TAIL ((BAY_TR_TAIL_RAW + 1023u) & ~1023u)
 #define BAY_TR_GREG (2u * BAY_TC_KC * BAY_TR_ATOM + BAY_TR_TAIL)   // bytes per tile group
+
+// The statistics of a tile: per-dim sums of its walkers' positions in a fixed order.
+// BAY_TR_NG walker groups (256 / DIM, at most 8; one for DIM >= 128) of BAY_TR_WG
+// consecutive walkers; thread (wg, d) sums its group in fp32 in walker order (pass 1, into
+// scr[wg * DIM + d], or straight to out[d * ntiles] with one group), then thread d adds the
+// groups' sums in group order (pass 2).  The per-step means add the tiles' sums in FP64.
+#define BAY_TR_NG (DIM >= 128u ? 1u : (256u / DIM < 8u ? 256u / DIM : 8u))
+#define BAY_TR_WG ((BAY_TR_W + BAY_TR_NG - 1u) / BAY_TR_NG)
+
+// pass 1 over the rows in device memory (rows of DIM floats, nt walkers), threads 0..255
+__device__ __forceinline__ void bay_tr_sums_pass1(const float* rows, unsigned int nt, unsigned int tid,
+                                                  float* scr, float* out, unsigned int ntiles) {
+    for (unsigned int t = tid; t < BAY_TR_NG * DIM; t += 256u) {
+        const unsigned int wg = t / DIM, d = t - wg * DIM;
+        float v = 0.0f;
+#pragma unroll
+        for (unsigned int i = 0; i < BAY_TR_WG; ++i) {
+            const unsigned int w = wg * BAY_TR_WG + i;
+            if (w < nt) v = __fadd_rn(v, rows[(size_t)w * DIM + d]);
+        }
+        if (BAY_TR_NG == 1u) out[(size_t)d * ntiles] = v;
+        else scr[t] = v;
+    }
+}
+
+// pass 2 (after a barrier that follows pass 1)
+__device__ __forceinline__ void bay_tr_sums_pass2(unsigned int tid, const float* scr, float* out,
+                                                  unsigned int ntiles) {
+    if (BAY_TR_NG > 1u && tid < DIM) {
+        float a = 0.0f;
+#pragma unroll
+        for (unsigned int wg = 0; wg < BAY_TR_NG; ++wg) a = __fadd_rn(a, scr[wg * DIM + tid]);
+        out[(size_t)tid * ntiles] = a;
+    }
+}
 
 // The resident tensor-core form.  A CTA holds G independent tile groups of 256 threads
 // (G = 1: an ordinary CTA); each group has its own A operand, proposals, scratch, MMA
@@ -1345,6 +1381,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     const unsigned int s_a = s_img + a_off;
     float* Yw = (float*)(sm + a_off + 2u * BAY_TC_KC * BAY_TR_ATOM);         // [W][DPAD]
     float* red = Yw + BAY_TR_W * BAY_TR_DPAD;                                // [256]
+    float* red2 = red + 256;                                                 // [256]
     const unsigned int bar_img = (unsigned int)__cvta_generic_to_shared(&sBar[0]);
     const unsigned int bar_mma = (unsigned int)__cvta_generic_to_shared(&sBar[1 + g]);
     unsigned int* status = &P.ctl->status;
@@ -1534,6 +1571,17 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
         for (int i = 0; i < BAY_PREP_LEN; ++i) sPrep[g][tid][i] = pr[i];
         sW[g][tid] = wt;
     }
+    // accu, one launch per half-step: while the MMAs run, the statistics of the previous
+    // half-step -- this tile of the other half, final since the previous launch completed
+    // and not written by this one: (step_off, 0) from the launch of half 1, (step_off - 1,
+    // 1) from the launch of half 0 (the chunk's last one has a launch of its own)
+    const bool prev_stats = ACCU && !PERSIST && P.means_cap != 0 && (half == 1u || step_off > 0u);
+    float* const prev_out = prev_stats
+        ? P.part + ((size_t)(half == 1u ? step_off : step_off - 1u) * 2 + (1u - half)) * DIM * ntiles + tile
+        : nullptr;
+    if (prev_stats)
+        bay_tr_sums_pass1(P.xs + (size_t)(1u - half) * P.K * DIM + (size_t)k0 * DIM, nt, tid,
+                          red2, prev_out, ntiles);
     // every thread waits for the MMAs (bounded; the commit arrives even if none were issued)
     // and observes the image copy itself before reading the aux values it brought
     const bool mma_done = bay_tc_wait(bar_mma, mma_par, nullptr, status);
@@ -1578,6 +1626,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     }
     bay_tc_fence_before();
     bay_gsync(g);
+    if (prev_stats) bay_tr_sums_pass2(tid, red2, prev_out, ntiles);
     // 7. accept (one thread per walker), write-back, statistics
     bool accepted = false;
     if (tid < nt && ok) {
@@ -1601,7 +1650,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     if (!LOGFN_ONLY) {
         if (tid < BAY_TR_W) sAcc[g][tid] = accepted ? 1 : 0;
         const int n_acc = bay_gsync_count(g, accepted);
-        if (ACCU) {
+        if (ACCU && PERSIST) {
             // the statistics need every walker's new position in Yw: the rejected walkers'
             // current rows are loaded (IB units in flight per thread), the accepted ones
             // stored
@@ -1648,35 +1697,23 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
         }
         if (ACCU) {
             if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
-            if (P.means_cap != 0) {
+            if (PERSIST && P.means_cap != 0) {
+                // the statistics of the tile's new positions (Yw) at the end of the tile
                 bay_gsync(g);
-                // per-dim sums of the tile's new positions in one pass: NG = 256 / DIM groups
-                // (at most 8) of WG consecutive walkers, thread (g, d) sums group g of dim d in
-                // fp32 in walker order, then thread d adds the groups' sums in group order
-                // (the per-step means add the CTAs' sums in FP64)
-                constexpr unsigned int NG = DIM >= 128u ? 1u : (256u / DIM < 8u ? 256u / DIM : 8u);
-                constexpr unsigned int WG = (BAY_TR_W + NG - 1u) / NG;
                 float* out = P.part + ((size_t)step_off * 2 + half) * DIM * ntiles + tile;
-                for (unsigned int t = tid; t < NG * DIM; t += 256u) {
-                    const unsigned int wg = t / DIM, d = t - wg * DIM;    // walker group, dim
+                for (unsigned int t = tid; t < BAY_TR_NG * DIM; t += 256u) {
+                    const unsigned int wg = t / DIM, d = t - wg * DIM;
                     float v = 0.0f;
 #pragma unroll
-                    for (unsigned int i = 0; i < WG; ++i) {
-                        const unsigned int w = wg * WG + i;
+                    for (unsigned int i = 0; i < BAY_TR_WG; ++i) {
+                        const unsigned int w = wg * BAY_TR_WG + i;
                         if (w < nt) v = __fadd_rn(v, Yw[w * BAY_TR_DPAD + d]);
                     }
-                    if (NG == 1u) out[(size_t)d * ntiles] = v;
-                    else red[t] = v;                    // NG * DIM <= 256 floats
+                    if (BAY_TR_NG == 1u) out[(size_t)d * ntiles] = v;
+                    else red[t] = v;
                 }
-                if (NG > 1u) {
-                    bay_gsync(g);
-                    if (tid < DIM) {
-                        float a = 0.0f;
-#pragma unroll
-                        for (unsigned int wg = 0; wg < NG; ++wg) a = __fadd_rn(a, red[wg * DIM + tid]);
-                        out[(size_t)tid * ntiles] = a;
-                    }
-                }
+                bay_gsync(g);
+                bay_tr_sums_pass2(tid, red, out, ntiles);
             }
         }
     }
@@ -1714,6 +1751,18 @@ extern "C" __global__ void __launch_bounds__(256) bay_tcr_accu(bay_stretch_param
 }
 extern "C" __global__ void __launch_bounds__(256) bay_tcr_logfn(bay_stretch_params P) {
     bay_stretch_tcr<false, true, false, 1u>(P, 1u);
+}
+// the statistics of the last half-step of a chunk (half P.half, step P.step_off): one CTA
+// per tile, the same sums as the stretch launches
+extern "C" __global__ void __launch_bounds__(256) bay_tcr_stats(bay_stretch_params P) {
+    __shared__ float scr[256];
+    const unsigned int tile = blockIdx.x, ntiles = gridDim.x, k0 = tile * BAY_TR_W;
+    const unsigned int nt = P.K - k0 < BAY_TR_W ? P.K - k0 : BAY_TR_W;
+    float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * ntiles + tile;
+    bay_tr_sums_pass1(P.xs + (size_t)P.half * P.K * DIM + (size_t)k0 * DIM, nt, threadIdx.x, scr,
+                      out, ntiles);
+    __syncthreads();
+    bay_tr_sums_pass2(threadIdx.x, scr, out, ntiles);
 }
 // persistent: one CTA of 4 tile groups per SM (1,024 threads, 64 registers each)
 extern "C" __global__ void __launch_bounds__(1024, 1) bay_tcr_run_bare(bay_stretch_params P, unsigned int m) {
