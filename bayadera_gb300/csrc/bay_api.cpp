@@ -531,7 +531,7 @@ struct bay_sampler {
     // of the accu steps (from the per-CTA sums), then the device step counter += m.
     // persistent tcr: clear the grid barrier's words, then one cooperative launch of m steps
     void launch_persistent(bool accu, uint32_t m, cudaStream_t st) {
-        static_assert(offsetof(bay_ctl, gbar_count) == 128 && offsetof(bay_ctl, abort) == 260,
+        static_assert(offsetof(bay_ctl, gbar_count) == 128 && offsetof(bay_ctl, abort) == 256,
                       "grid barrier words of bay_ctl");
         cuda_check(cudaMemsetAsync(&ctl->gbar_count, 0,
                                    offsetof(bay_ctl, abort) + sizeof(unsigned int) - offsetof(bay_ctl, gbar_count),

@@ -18,9 +18,8 @@ struct bay_ctl {
     unsigned int pad0[21];
     unsigned int gbar_count;   // byte 128
     unsigned int pad1[31];
-    unsigned int gbar_gen;     // byte 256
-    unsigned int abort;
-    unsigned int pad2[30];
+    unsigned int abort;        // byte 256
+    unsigned int pad2[31];
 };
 
 // Must match struct bay_stretch_params in device/bay_stretch.cuh.

@@ -53,9 +53,8 @@ struct bay_ctl {
     unsigned int pad0[21];
     unsigned int gbar_count;        // grid barrier of the persistent form (byte 128): arrivals
     unsigned int pad1[31];
-    unsigned int gbar_gen;          //   (unused; byte 256)
-    unsigned int abort;             //   abandon flag; count and abort are cleared before each launch
-    unsigned int pad2[30];
+    unsigned int abort;             //   abandon flag (byte 256); both cleared before each launch
+    unsigned int pad2[31];
 };
 
 struct bay_stretch_params {
