@@ -121,6 +121,7 @@ _SIGNATURES = {
     "bay_logfn_values": (C.c_int, [P, P]),
     "bay_sampler_set_graphs": (C.c_int, [P, C.c_int]),
     "bay_sampler_set_persistent": (C.c_int, [P, C.c_int]),
+    "bay_sampler_test_barrier_timeout": (C.c_int, [P, C.c_int]),
     "bay_sample_direct": (C.c_int, [P, C.c_uint32, P, C.c_uint32, C.c_uint64, P]),
     "bay_log_density": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),
     "bay_density": (C.c_int, [P, P, C.c_uint64, P, C.c_uint64, P]),

@@ -373,7 +373,8 @@ struct bay_sampler {
                    "cudaMemcpy(status)");
         cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
         if (st) fail(BAY_ERR_DEVICE, std::string("a kernel gave up waiting for ") +
-                                         ((st & 2u) ? "its tensor-core pipeline" : "its shared-memory copy") +
+                                         ((st & 4u) ? "the other CTAs of its launch (grid barrier)"
+                                          : (st & 2u) ? "its tensor-core pipeline" : "its shared-memory copy") +
                                          " (device status " + std::to_string(st) + ")");
     }
 
@@ -392,6 +393,8 @@ struct bay_sampler {
                                 // slower than programmatic dependent launches, so opt-in
     uint32_t tr_grid = 0;       // tcr: CTAs of the persistent form (all co-resident)
     size_t tr_smem = 0;         // tcr: dynamic shared memory of a persistent CTA
+    uint32_t gbar_extra = 0;    // tcr persistent: arrivals the grid barriers wait for beyond
+                                // the grid (1 in tests of the bounded wait)
     uint32_t tc_fp = 0;
     uint64_t tc_rows_pad = 0, tc_wpad = 0;
     unsigned short *tc_xh = nullptr, *tc_xl = nullptr, *s_bh = nullptr, *s_bl = nullptr;
@@ -468,7 +471,7 @@ struct bay_sampler {
         p.s_bh = s_bh;
         p.s_bl = s_bl;
         p.tc_fp = tc_fp;
-        p.tc_pad = 0;
+        p.gbar_extra = gbar_extra;
         return p;
     }
 
@@ -1290,6 +1293,24 @@ int bay_sampler_set_graphs(bay_sampler* s, int enabled) {
     return guarded([&] {
         if (!s) fail(BAY_ERR_ARG, "NULL sampler");
         s->graphs = enabled != 0;
+    });
+}
+
+int bay_sampler_test_barrier_timeout(bay_sampler* s, int enabled) {
+    return guarded([&] {
+        if (!s) fail(BAY_ERR_ARG, "NULL sampler");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        s->ctx->use();
+        const uint32_t extra = enabled ? 1u : 0u;
+        if (s->gbar_extra == extra) return;
+        s->gbar_extra = extra;
+        // the captured chunks hold the old parameter: capture again
+        for (cudaGraphExec_t* g : {&s->g_bare, &s->g_accu})
+            if (*g) {
+                cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
+                cudaGraphExecDestroy(*g);
+                *g = nullptr;
+            }
     });
 }
 

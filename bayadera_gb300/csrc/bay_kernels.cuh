@@ -53,7 +53,7 @@ struct bay_stretch_params {
     unsigned short* s_bh;
     unsigned short* s_bl;
     unsigned int tc_fp;
-    unsigned int tc_pad;
+    unsigned int gbar_extra;
 };
 
 enum {

@@ -94,7 +94,8 @@ struct bay_stretch_params {
     unsigned short* s_bh;
     unsigned short* s_bl;
     unsigned int tc_fp;
-    unsigned int tc_pad;
+    unsigned int gbar_extra;        // persistent form: arrivals its grid barriers wait for beyond
+                                    // the grid (0; 1 makes them run out, for tests)
 };
 
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
@@ -1233,8 +1234,10 @@ __device__ __forceinline__ void bay_tr_put_a(unsigned int s_a, unsigned int w, u
 // and waits until the count reaches k * nblocks; the count only grows during a launch.
 // Bounded: a CTA that waits longer than BAY_TC_WAIT_NS raises ctl->abort and status bit 4;
 // a raised abort ends every wait at once.  Returns false when the launch is being
-// abandoned.  The count and the abort word are cleared before each launch.
-__device__ __forceinline__ bool bay_grid_barrier(bay_ctl* ctl, unsigned int nblocks, unsigned int k) {
+// abandoned.  The count and the abort word are cleared before each launch.  `extra`
+// arrivals beyond the grid (nonzero only in tests) make every barrier run out.
+__device__ __forceinline__ bool bay_grid_barrier(bay_ctl* ctl, unsigned int nblocks, unsigned int k,
+                                                 unsigned int extra) {
     __shared__ unsigned int s_go;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1243,7 +1246,7 @@ __device__ __forceinline__ bool bay_grid_barrier(bay_ctl* ctl, unsigned int nblo
         if (*ab) {
             go = 0u;
         } else {
-            const unsigned int target = k * nblocks;
+            const unsigned int target = k * nblocks + extra;
             __threadfence();                               // the CTA's writes before its arrival
             asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&ctl->gbar_count) : "memory");
             unsigned long long t0 = bay_globaltimer();
@@ -1432,7 +1435,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     for (unsigned int si = 0; si < nsteps && go; ++si) {
     for (unsigned int half = h_lo; half < h_hi && go; ++half) {
     if (PERSIST && (si | (half - h_lo)) != 0u)
-        go = bay_grid_barrier(P.ctl, gridDim.x, 2u * si + (half - h_lo));
+        go = bay_grid_barrier(P.ctl, gridDim.x, 2u * si + (half - h_lo), P.gbar_extra);
     if (!go) break;
     const unsigned int step_off = P.step_off + si;
     const unsigned int step = step0 + step_off;

@@ -455,6 +455,12 @@ class GB300Stretch:
         steps, or one launch per half-step (default); both give the same results."""
         N.call("bay_sampler_set_persistent", self.handle, 1 if enabled else 0)
 
+    def arm_barrier_timeout(self, enabled):
+        """Testing the device failure path: the persistent form's grid barriers wait for one
+        CTA more than the launch has, run out after their bounded wait and set the status
+        word (the next status check raises)."""
+        N.call("bay_sampler_test_barrier_timeout", self.handle, 1 if enabled else 0)
+
     # ---------------------------------------------------------------- MCMC
     def init(self, seed):
         N.call("bay_init", self.handle, seed & 0xffffffff)

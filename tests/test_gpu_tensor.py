@@ -395,3 +395,34 @@ def test_tcr_persistent_matches_per_launch(factory, M, D, W):
     np.testing.assert_array_equal(a[1], b[1])
     np.testing.assert_array_equal(a[2], b[2])
     assert a[3] == b[3]
+
+
+def test_tcr_grid_barrier_runs_out_and_context_recovers(factory, M):
+    """Device failure path without a fault: armed, the persistent form's grid barriers wait
+    for one CTA more than the launch has; every CTA gives up after its bounded wait (2 s),
+    raises the abort flag and the status word, and the launch ends.  The host reads the
+    status (BAY_ERR_DEVICE, naming the grid barrier); a new sampler on the same context
+    then runs normally."""
+    import time
+    from bayadera_gb300._native import BayaderaError, BAY_ERR_DEVICE
+    D, W = 10, 4096
+    P = np.diag(np.linspace(0.5, 2.0, D)).astype(np.float32)
+    sf = factory.mcmc_factory(M.mvn_precision_model(D), form="gemm", tensor=True)
+    s = sf.create_sampler(31, W, P.reshape(-1))
+    s.set_persistent(True)
+    s.init_position_normal(2, 0.0, 1.0)
+    s.arm_barrier_timeout(True)
+    t0 = time.perf_counter()
+    with pytest.raises(BayaderaError, match="grid barrier") as e:
+        s.run_sampler(8, 2.0)
+    assert e.value.code == BAY_ERR_DEVICE
+    assert time.perf_counter() - t0 < 60.0
+    s.release()
+    s = sf.create_sampler(31, W, P.reshape(-1))
+    s.set_persistent(True)
+    s.init_position_normal(2, 0.0, 1.0)
+    r = s.run_sampler(40, 2.0, return_means=True)
+    assert 0.2 < r["acceptance_rate"] < 0.9
+    np.testing.assert_allclose(r["means"][:, -1], s.mean(), rtol=1e-5, atol=1e-6)
+    s.release()
+    sf.release()
