@@ -15,6 +15,7 @@
 #include <cctype>
 #include <cmath>
 #include <cstdio>
+#include <nvtx3/nvToolsExt.h>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -47,6 +48,15 @@ void cuda_check(cudaError_t e, const char* what) {
 
 // Driver-API entry points, resolved through the runtime at first context creation so
 // that the library loads (and compile-checks models) on machines without a driver.
+// NVTX range over a public call (header-only NVTX 3: inert unless a profiler attaches), so
+// a trace shows which library call issued which kernels
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 struct DriverApi {
     PFN_cuGetErrorString_v6000 GetErrorString = nullptr;
     PFN_cuLibraryLoadData_v12000 LibraryLoadData = nullptr;
@@ -899,6 +909,7 @@ int bay_model_check(const bay_model_desc* d, uint32_t wgs) {
 }
 
 int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
+    NvtxRange trace_("bay_model_compile");
     return guarded([&] {
         if (!c || !d || !out) fail(BAY_ERR_ARG, "NULL argument");
         *out = nullptr;
@@ -1245,11 +1256,13 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
 
 int bay_sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const float* params,
                        uint64_t n_params, bay_sampler** out) {
+    NvtxRange trace_("bay_sampler_create");
     return sampler_create(m, seed, walkers, params, n_params, false, out);
 }
 
 int bay_sampler_create_device(bay_model* m, uint32_t seed, uint64_t walkers, const float* d_params,
                               uint64_t n_params, bay_sampler** out) {
+    NvtxRange trace_("bay_sampler_create_device");
     return sampler_create(m, seed, walkers, d_params, n_params, true, out);
 }
 
@@ -1353,6 +1366,7 @@ int bay_init(bay_sampler* s, uint32_t seed) {
 }
 
 int bay_init_position_limits(bay_sampler* s, uint32_t seed, const float* limits) {
+    NvtxRange trace_("bay_init_position_limits");
     return guarded([&] {
         if (!s || !limits) fail(BAY_ERR_ARG, "NULL argument");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
@@ -1377,6 +1391,7 @@ int bay_init_position_limits(bay_sampler* s, uint32_t seed, const float* limits)
 }
 
 int bay_init_position_normal(bay_sampler* s, uint32_t seed, float mean, float sd) {
+    NvtxRange trace_("bay_init_position_normal");
     return guarded([&] {
         if (!s) fail(BAY_ERR_ARG, "NULL sampler");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
@@ -1390,6 +1405,7 @@ int bay_init_position_normal(bay_sampler* s, uint32_t seed, float mean, float sd
 }
 
 int bay_init_position_copy(bay_sampler* s, const bay_sampler* src) {
+    NvtxRange trace_("bay_init_position_copy");
     return guarded([&] {
         if (!s || !src) fail(BAY_ERR_ARG, "NULL argument");
         if (src->D != s->D || src->W != s->W)
@@ -1408,6 +1424,7 @@ int bay_init_position_copy(bay_sampler* s, const bay_sampler* src) {
 }
 
 int bay_init_position_host(bay_sampler* s, const float* positions) {
+    NvtxRange trace_("bay_init_position_host");
     return guarded([&] {
         if (!s || !positions) fail(BAY_ERR_ARG, "NULL argument");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
@@ -1423,6 +1440,7 @@ int bay_init_position_host(bay_sampler* s, const float* positions) {
 }
 
 int bay_burn_in(bay_sampler* s, uint64_t n, float a) {
+    NvtxRange trace_("bay_burn_in");
     return guarded([&] {
         if (!s) fail(BAY_ERR_ARG, "NULL sampler");
         if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
@@ -1436,6 +1454,7 @@ int bay_burn_in(bay_sampler* s, uint64_t n, float a) {
 }
 
 int bay_anneal(bay_sampler* s, const float* temps, uint64_t n, float a) {
+    NvtxRange trace_("bay_anneal");
     return guarded([&] {
         if (!s || (n && !temps)) fail(BAY_ERR_ARG, "NULL argument");
         if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
@@ -1514,6 +1533,7 @@ int acor_device(bay_ctx* c, const float* d_series, uint32_t D, uint64_t n, doubl
 }  // namespace
 
 int bay_acc_rate(bay_sampler* s, float a, double* rate) {
+    NvtxRange trace_("bay_acc_rate");
     return guarded([&] {
         if (!s || !rate) fail(BAY_ERR_ARG, "NULL argument");
         if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
@@ -1537,6 +1557,7 @@ int bay_acc_rate(bay_sampler* s, float a, double* rate) {
 
 int bay_run_sampler(bay_sampler* s, uint64_t n, float a, bay_run_result* res, double* tau,
                     double* mean, double* sigma, float* means_out) {
+    NvtxRange trace_("bay_run_sampler");
     return guarded([&] {
         if (!s || !res) fail(BAY_ERR_ARG, "NULL argument");
         if (!(a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
@@ -1566,6 +1587,7 @@ int bay_run_sampler(bay_sampler* s, uint64_t n, float a, bay_run_result* res, do
 }
 
 int bay_sample(bay_sampler* s, uint64_t n_cols, float* out) {
+    NvtxRange trace_("bay_sample");
     return guarded([&] {
         if (!s || (n_cols && !out)) fail(BAY_ERR_ARG, "NULL argument");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
@@ -1588,6 +1610,7 @@ int bay_sample(bay_sampler* s, uint64_t n_cols, float* out) {
 }
 
 static int moments_out(bay_sampler* s, double* out, int which) {
+    NvtxRange trace_(which ? "bay_variance" : "bay_mean");
     return guarded([&] {
         if (!s || !out) fail(BAY_ERR_ARG, "NULL argument");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
@@ -1618,6 +1641,7 @@ int bay_sd(bay_sampler* s, double* out) {
 
 int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags, float* limits,
                   float* pdf, float* ranks) {
+    NvtxRange trace_("bay_histogram");
     return guarded([&] {
         if (!s || !limits || !pdf || !ranks) fail(BAY_ERR_ARG, "NULL argument");
         if (cycles == 0) fail(BAY_ERR_ARG, "cycles must be >= 1");
@@ -1684,6 +1708,7 @@ int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags
 
 int bay_acor(bay_ctx* c, const float* series, uint32_t D, uint64_t n, double* tau, double* mean,
              double* sigma, uint32_t* lag) {
+    NvtxRange trace_("bay_acor");
     int rc = BAY_OK;
     const int g = guarded([&] {
         if (!c || !series) fail(BAY_ERR_ARG, "NULL argument");
@@ -1713,6 +1738,7 @@ int bay_acor(bay_ctx* c, const float* series, uint32_t D, uint64_t n, double* ta
 // the work space is the library's fixed device scratch (BAY_ACOR_NOALLOC_MAX_DOUBLES).
 int bay_acor_noalloc(bay_ctx* c, const float* d_series, uint32_t D, uint64_t n, double* tau,
                      double* mean, double* sigma, uint32_t* lag_out) {
+    NvtxRange trace_("bay_acor_noalloc");
     return guarded([&] {
         if (!c || !d_series) fail(BAY_ERR_ARG, "NULL argument");
         if (D == 0) fail(BAY_ERR_ARG, "dim must be >= 1");
@@ -1745,6 +1771,7 @@ int bay_acor_noalloc(bay_ctx* c, const float* d_series, uint32_t D, uint64_t n, 
 }
 
 int bay_state_export(bay_sampler* s, float* positions, float* logfn, uint32_t* rng) {
+    NvtxRange trace_("bay_state_export");
     return guarded([&] {
         if (!s) fail(BAY_ERR_ARG, "NULL sampler");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
@@ -1774,6 +1801,7 @@ int bay_state_export(bay_sampler* s, float* positions, float* logfn, uint32_t* r
 
 int bay_state_import(bay_sampler* s, const float* positions, const float* logfn,
                      const uint32_t* rng) {
+    NvtxRange trace_("bay_state_import");
     return guarded([&] {
         if (!s || !positions || !logfn || !rng) fail(BAY_ERR_ARG, "NULL argument");
         std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
