@@ -1,0 +1,111 @@
+"""The models the benchmark configs run, as the oracle states them (FP64 and fp32), against
+independent numpy formulas of the same densities; the host-side parameter encodings
+(hierarchical rows) and the cooling schedules of anneal! / mix! (mcmc.clj:43-53).  CPU."""
+import math
+
+import numpy as np
+import pytest
+
+
+def _rel(a, b):
+    return abs(a - b) / max(1.0, abs(b))
+
+
+def test_mvn_precision(oracle):
+    rng = np.random.default_rng(1)
+    D = 12
+    A = rng.normal(size=(D, D))
+    P = (A @ A.T / D + np.eye(D)).astype(np.float32)
+    for _ in range(5):
+        x = rng.normal(size=D)
+        want = -0.5 * x @ P.astype(np.float64) @ x
+        assert _rel(oracle.logfn64("mvn_precision", P.reshape(-1), 0, D, x), want) < 1e-12
+        assert _rel(oracle.logfn32("mvn_precision", P.reshape(-1), 0, D, x.astype(np.float32)),
+                    want) < 1e-5
+
+
+def test_logistic(oracle):
+    rng = np.random.default_rng(2)
+    n, F = 300, 7
+    X = rng.normal(size=(n, F)).astype(np.float32)
+    y = (rng.random(n) < 0.5).astype(np.float32)
+    h0 = 5.0
+    params = np.concatenate([np.concatenate([X, y[:, None]], axis=1).reshape(-1),
+                             np.array([h0], np.float32)])
+    for _ in range(5):
+        b = rng.normal(scale=0.5, size=F)
+        eta = X.astype(np.float64) @ b
+        want = np.sum(y * eta - np.logaddexp(0.0, eta)) - b @ b / (2 * h0 * h0)
+        assert _rel(oracle.logfn64("logistic", params, n * (F + 1), F, b), want) < 1e-12
+        assert _rel(oracle.logfn32("logistic", params, n * (F + 1), F, b.astype(np.float32)),
+                    want) < 1e-4
+
+
+def test_robust_t(oracle):
+    rng = np.random.default_rng(3)
+    n, F = 200, 5
+    X = rng.normal(size=(n, F)).astype(np.float32)
+    y = (X @ rng.normal(size=F) + 0.5 * rng.standard_t(4, n)).astype(np.float32)
+    nu, bsd, lsd = 4.0, 10.0, 1.0
+    params = np.concatenate([np.concatenate([X, y[:, None]], axis=1).reshape(-1),
+                             np.array([nu, bsd, lsd], np.float32)])
+    for _ in range(5):
+        x = np.concatenate([rng.normal(size=F), [rng.normal(scale=0.3)]])
+        b, ls = x[:F], x[F]
+        r = (y - X.astype(np.float64) @ b) / math.exp(ls)
+        want = (np.sum(-0.5 * (nu + 1) * np.log1p(r * r / nu)) - n * ls
+                - b @ b / (2 * bsd * bsd) - ls * ls / (2 * lsd * lsd))
+        assert _rel(oracle.logfn64("robust_t", params, n * (F + 1), F + 1, x), want) < 1e-12
+        assert _rel(oracle.logfn32("robust_t", params, n * (F + 1), F + 1, x.astype(np.float32)),
+                    want) < 1e-4
+
+
+def test_gaussian_posterior(oracle):
+    rng = np.random.default_rng(4)
+    data = rng.normal(3.0, 2.0, 400).astype(np.float32)
+    h = np.array([0.0, 10.0, 0.0, 20.0], np.float32)
+    params = np.concatenate([data, h])
+    d = data.astype(np.float64)
+    for mu, sg in ((2.5, 1.7), (3.1, 2.2), (-1.0, 0.5)):
+        lik = np.sum(-(d - mu) ** 2 / (2 * sg * sg)) - d.size * (math.log(sg) + 0.5 * math.log(2 * math.pi))
+        prior = (-(mu - 0.0) ** 2 / (2 * 100.0) - math.log(10.0) - 0.5 * math.log(2 * math.pi)
+                 - math.log(20.0))
+        want = lik + prior
+        assert _rel(oracle.logfn64("gaussian_posterior", params, d.size, 2, np.array([mu, sg])),
+                    want) < 1e-11
+    # sigma outside the uniform prior's support: log density -inf (or NaN for sigma <= 0)
+    assert oracle.logfn64("gaussian_posterior", params, d.size, 2, np.array([1.0, 25.0])) == -math.inf
+
+
+def test_hierarchical_rows_encoding(oracle):
+    """models.hierarchical_rows_params + the hrows density against the hierarchical model
+    written out group by group."""
+    from bayadera_gb300 import models as M
+    rng = np.random.default_rng(5)
+    J = 6
+    ys = [rng.normal(j, 1.0, 10 + 4 * j) for j in range(J)]
+    sig = rng.uniform(0.5, 2.0, J)
+    h0, h1 = 10.0, 1.0
+    params, rows = M.hierarchical_rows_params(ys, sig, h0, h1)
+    assert rows == sum(len(y) for y in ys) and params.size == 3 * rows + 2
+    for _ in range(5):
+        theta = rng.normal(size=J)
+        mu, lt = rng.normal(), rng.normal(scale=0.3)
+        x = np.concatenate([theta, [mu, lt]])
+        want = 0.0
+        for j in range(J):
+            yj = np.asarray(ys[j], np.float32).astype(np.float64)
+            s2 = float(np.float32(-0.5 / (float(sig[j]) ** 2)))     # the encoded coefficient
+            want += s2 * np.sum((yj - theta[j]) ** 2)
+        tau2 = math.exp(2 * lt)
+        want += np.sum(-(theta - mu) ** 2 / (2 * tau2)) - J * lt - mu * mu / (2 * h0 * h0) \
+            - lt * lt / (2 * h1 * h1)
+        assert _rel(oracle.logfn64("hrows", params, 3 * rows, J + 2, x), want) < 1e-11
+
+
+def test_cooling_schedules():
+    """mcmc.clj:43-53: sqrt-n, pow-n and minus-n of a temperature at step i."""
+    from bayadera_gb300 import mcmc
+    assert mcmc.minus_n(10)(3) == 7
+    assert mcmc.sqrt_n(10)(1) == pytest.approx(3.0)
+    assert mcmc.pow_n(2.0)(10)(4) == pytest.approx(36.0)
