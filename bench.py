@@ -656,9 +656,16 @@ def main():
     res, mean, var, hist = results
     ac = res["autocorrelation"]
     within = None
+    within_tmax = None
     err_sd = None
     if ac is not None:
         within = int(np.sum(np.abs(ac.mean) <= 3 * ac.sigma))
+        # the same test with each dimension's standard error taken at the largest tau of the
+        # run (sigma scales with sqrt(tau)): acor's per-dimension tau from n / tau ~ 6
+        # correlation times is itself low for some dimensions
+        tau = np.asarray(ac.tau, np.float64)
+        se_tmax = np.asarray(ac.sigma) * np.sqrt(np.max(tau) / np.maximum(tau, 1e-30))
+        within_tmax = int(np.sum(np.abs(ac.mean) <= 3 * se_tmax))
         # the run mean's distance from the analytic mean 0, in posterior standard deviations
         err_sd = float(np.max(np.abs(ac.mean) / np.sqrt(np.diag(sigma))))
 
@@ -689,7 +696,8 @@ def main():
             "clocks": clocks.summary(),
             "result": {"acceptance_rate": res["acceptance_rate"],
                        "tau_max": float(np.max(ac.tau)) if ac is not None else None,
-                       "means_within_3se": within, "dims": DIM,
+                       "means_within_3se": within,
+                       "means_within_3se_at_tau_max": within_tmax, "dims": DIM,
                        "max_abs_mean_over_posterior_sd": err_sd},
         }
         print(json.dumps(line))
