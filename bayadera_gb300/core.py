@@ -96,6 +96,66 @@ class DistributionCreator:
         self.sampler_factory.release()
 
 
+class Dataset:
+    """DatasetImpl (impl.clj:25-45): a data matrix (n points x dim) whose mean, variance,
+    sd and histogram come from the dataset engine (nvidia_gtx.clj:145-228)."""
+
+    def __init__(self, factory, data):
+        x = np.ascontiguousarray(data, np.float32)
+        if x.ndim == 1:
+            x = x[:, None]
+        if x.ndim != 2 or x.size == 0:
+            raise ValueError("The engine can not support this data: a non-empty n x dim matrix.")
+        self.factory = factory
+        self.data = x
+
+    def mean(self):
+        return self.factory.data_moments(self.data)[0]
+
+    def variance(self):
+        return self.factory.data_moments(self.data)[1]
+
+    def sd(self):
+        return np.sqrt(self.variance())
+
+    def histogram(self, cycles=1, bins=0, flags=0):
+        return self.factory.data_histogram(self.data, bins, flags)
+
+
+def dataset(*args):
+    """dataset (core.clj:31-45): dataset(data) or dataset(factory, data)."""
+    if len(args) == 2:
+        return Dataset(_factory(args[0]), args[1])
+    return Dataset(_factory(None), args[0])
+
+
+class Likelihood:
+    """LikelihoodImpl (impl.clj): a likelihood model with its engine; the engine is compiled
+    for the dimension of the points it is evaluated at (the prior sample's)."""
+
+    def __init__(self, factory, model):
+        self.factory = factory
+        self.model = model
+        self._engines = {}
+
+    def engine(self, dim):
+        if dim not in self._engines:
+            self._engines[dim] = self.factory.likelihood_engine(self.model, dim)
+        return self._engines[dim]
+
+    def release(self):
+        for e in self._engines.values():
+            e.release()
+        self._engines.clear()
+
+
+def likelihood(*args):
+    """likelihood (core.clj:58-66): likelihood(model) or likelihood(factory, model)."""
+    if len(args) == 2:
+        return Likelihood(_factory(args[0]), args[1])
+    return Likelihood(_factory(None), args[0])
+
+
 def posterior_model(likelihood, prior, name=None):
     """posterior-model (core.clj:49-56)."""
     return M.device_posterior_model(prior, name or "posterior", likelihood)
@@ -121,6 +181,14 @@ def sampler(dist, options=None):
 
 def sample(samp, n=None):
     return samp.sample(n)
+
+
+def sample_(samp, out):
+    """sample! (core.clj:131-137): fill a contiguous dim x n matrix with n samples."""
+    if not (isinstance(out, np.ndarray) and out.ndim == 2 and out.flags.c_contiguous):
+        raise ValueError("Data has to be a contiguous matrix.")
+    out[...] = samp.sample(out.shape[1])
+    return out
 
 
 def mean(x):
@@ -162,11 +230,17 @@ def density(dist, x):
         eng.release()
 
 
-def evidence(factory, likelihood, data, x):
-    """evidence (core.clj:115-121): the mean likelihood of data over the points x (n x dim),
-    e.g. samples of the prior."""
+def evidence(*args):
+    """evidence (core.clj:115-121): the mean likelihood of data over the points of a prior
+    sample (n x dim).  evidence(lik, data, prior_sample) with lik from likelihood(...), as
+    the reference; or evidence(factory, likelihood_model, data, prior_sample)."""
+    if len(args) == 3:
+        lik, data, x = args
+        x = np.asarray(x, np.float32)
+        return lik.engine(x.shape[-1]).evidence(data, x)
+    factory, model, data, x = args
     x = np.asarray(x, np.float32)
-    eng = _factory(factory).likelihood_engine(likelihood, x.shape[-1])
+    eng = _factory(factory).likelihood_engine(model, x.shape[-1])
     try:
         return eng.evidence(data, x)
     finally:

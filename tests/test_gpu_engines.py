@@ -129,3 +129,28 @@ def test_dataset_moments_and_histogram(factory, oracle):
     np.testing.assert_array_equal(h.limits.T.reshape(-1), ol)
     np.testing.assert_array_equal(h.pdf.T.reshape(-1), opdf)
     np.testing.assert_array_equal(h.bin_ranks.T.reshape(-1), orank)
+
+
+def test_core_dataset_likelihood_evidence(factory, M):
+    """The reference-shaped core API over the engines: dataset(...) moments and histogram
+    equal the dataset engine's; evidence(likelihood(model), data, prior_sample) equals the
+    likelihood engine's evidence."""
+    from bayadera_gb300 import core
+    rng = np.random.default_rng(6)
+    x = np.stack([rng.normal(1.0, 2.0, 20000), rng.exponential(1.0, 20000)], axis=1).astype(np.float32)
+    ds = core.dataset(factory, x)
+    m, v = factory.data_moments(x)
+    np.testing.assert_array_equal(core.mean(ds), m)
+    np.testing.assert_array_equal(core.variance(ds), v)
+    np.testing.assert_allclose(core.sd(ds), np.sqrt(v))
+    h = core.histogram(ds, 1, 128)
+    h2 = factory.data_histogram(x, 128)
+    np.testing.assert_array_equal(h.pdf, h2.pdf)
+    y = rng.normal(0.5, 1.0, 20).astype(np.float32)
+    pts = np.stack([rng.normal(0.5, 0.5, 1000), rng.uniform(0.6, 1.6, 1000)], axis=1).astype(np.float32)
+    lik = core.likelihood(factory, M.likelihood_models()["gaussian"])
+    ev = core.evidence(lik, y, pts)
+    eng = factory.likelihood_engine(M.likelihood_models()["gaussian"], 2)
+    assert ev == eng.evidence(y, pts)
+    eng.release()
+    lik.release()

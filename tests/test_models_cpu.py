@@ -134,3 +134,43 @@ def test_oracle_stretch_samples_a_correlated_gaussian(oracle):
     m = means.astype(np.float64)                    # (D, steps) ensemble means
     se = m.std(axis=1) * np.sqrt(50.0 / m.shape[1])  # tau <= 50 steps for this target
     assert np.all(np.abs(m.mean(axis=1)) <= 5 * se + 1e-3 * s)
+
+
+def test_core_host_wrappers_without_gpu():
+    """core.py's reference-shaped wrappers, checked with stand-in engines: dataset rejects
+    an empty matrix, sample! fills a contiguous matrix and rejects a strided one, and
+    evidence(lik, data, prior_sample) evaluates through the likelihood's engine for the
+    prior sample's dimension."""
+    from bayadera_gb300 import core as c
+
+    with pytest.raises(ValueError, match="can not support"):
+        c.Dataset(object(), np.zeros((0, 3)))
+
+    class FakeSampler:
+        def sample(self, n):
+            return np.arange(2 * n, dtype=np.float32).reshape(2, n)
+
+    out = np.zeros((2, 4), np.float32)
+    c.sample_(FakeSampler(), out)
+    assert out.tolist() == [[0, 1, 2, 3], [4, 5, 6, 7]]
+    with pytest.raises(ValueError, match="contiguous"):
+        c.sample_(FakeSampler(), np.zeros((2, 8), np.float32)[:, ::2])
+
+    class FakeEngine:
+        def __init__(self, dim):
+            self.dim = dim
+
+        def evidence(self, data, x):
+            return float(self.dim * 100 + len(data) + x.shape[0])
+
+        def release(self):
+            pass
+
+    class FakeFactory:
+        def likelihood_engine(self, model, dim):
+            return FakeEngine(dim)
+
+    lik = c.Likelihood(FakeFactory(), "model")
+    assert c.evidence(lik, [1.0, 2.0, 3.0], np.zeros((5, 2))) == 2 * 100 + 3 + 5
+    assert set(lik._engines) == {2}
+    lik.release()
