@@ -1,5 +1,7 @@
 """Direct samplers and density / likelihood / evidence engines against the reference's
 golden vectors (nvidia_gtx_test.clj direct samplers), the oracle, and FP64 numpy."""
+import math
+
 import numpy as np
 import pytest
 
@@ -154,3 +156,34 @@ def test_core_dataset_likelihood_evidence(factory, M):
     assert ev == eng.evidence(y, pts)
     eng.release()
     lik.release()
+
+
+def test_library_distributions_sample_and_density(factory):
+    """library.py on the GPU: log densities at points against scipy (rtol 2e-5); direct
+    samplers (uniform, Gaussian, exponential, Erlang) and the MCMC samplers the reference
+    warms up (Student's t, beta, gamma) give sample means and variances near the closed
+    forms (5 sigma of the sample-mean error, 10 % on the variance)."""
+    st = pytest.importorskip("scipy.stats")
+    from bayadera_gb300 import core, library as L
+    cases = [
+        (L.uniform(factory, -1.0, 3.0), lambda x: st.uniform.logpdf(x, -1.0, 4.0), [-0.5, 0.0, 2.9]),
+        (L.gaussian(factory, 1.0, 2.0), lambda x: st.norm.logpdf(x, 1.0, 2.0), [-1.0, 0.5, 4.0]),
+        (L.exponential(factory, 2.5), lambda x: st.expon.logpdf(x, scale=0.4), [0.1, 0.7, 2.0]),
+        (L.erlang(factory, 2.0, 3), lambda x: st.gamma.logpdf(x, 3, scale=0.5), [0.3, 1.5, 4.0]),
+        (L.student_t(factory, 5.0, 1.0, 2.0), lambda x: st.t.logpdf(x, 5.0, 1.0, 2.0), [-3.0, 1.2, 6.0]),
+        (L.beta(factory, 2.0, 3.0), lambda x: st.beta.logpdf(x, 2.0, 3.0), [0.1, 0.4, 0.9]),
+        (L.gamma(factory, 1.5, 3.0), lambda x: st.gamma.logpdf(x, 3.0, scale=1.5), [0.5, 2.0, 9.0]),
+    ]
+    for d, ref, pts in cases:
+        got = d.log_density(pts)
+        np.testing.assert_allclose(got, ref(np.array(pts)), rtol=2e-5, atol=2e-5)
+        if d.direct is not None:
+            x = core.sample(d.sampler({"seed": 3}), 1 << 18)[0].astype(np.float64)
+        else:
+            s = d.sampler({"seed": 3, "walkers": 1 << 15, "warm_up": 256})
+            x = core.sample(s, 1 << 15)[0].astype(np.float64)
+            s.release()
+        n_eff = x.size if d.direct is not None else x.size / 8.0
+        assert abs(x.mean() - d.mean()) <= 5.0 * d.sd() / math.sqrt(n_eff), (d.name, x.mean())
+        assert abs(x.var() - d.variance()) <= 0.1 * d.variance(), (d.name, x.var())
+        d.release()

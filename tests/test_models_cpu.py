@@ -174,3 +174,38 @@ def test_core_host_wrappers_without_gpu():
     assert c.evidence(lik, [1.0, 2.0, 3.0], np.zeros((5, 2))) == 2 * 100 + 3 + 5
     assert set(lik._engines) == {2}
     lik.release()
+
+
+def test_library_parameters_and_moments():
+    """library.py: the parameter vectors' log-normalising constants (the densities' log
+    normaliser read by the device models) and the closed-form moments against scipy."""
+    st = pytest.importorskip("scipy.stats")
+    from bayadera_gb300 import library as L
+    t = L.student_t(None, 5.0, 1.0, 2.0)
+    x = 0.7
+    unscaled = -0.5 * (5.0 + 1.0) * math.log1p(((x - 1.0) / 2.0) ** 2 / 5.0)
+    assert unscaled + float(np.float64(t.params[3])) == pytest.approx(st.t.logpdf(x, 5.0, 1.0, 2.0), rel=1e-6)
+    assert (t.mean(), t.variance()) == pytest.approx((st.t.mean(5.0, 1.0, 2.0), st.t.var(5.0, 1.0, 2.0)))
+    b = L.beta(None, 2.0, 3.0)
+    assert (1.0 * math.log(0.4) + 2.0 * math.log(0.6) + b.params[2]) == pytest.approx(
+        st.beta.logpdf(0.4, 2.0, 3.0), rel=1e-6)
+    assert b.mean() == pytest.approx(st.beta.mean(2.0, 3.0))
+    assert b.variance() == pytest.approx(st.beta.var(2.0, 3.0))
+    assert b.median() == pytest.approx(st.beta.median(2.0, 3.0), rel=1e-12)    # exact case
+    assert L.beta(None, 3.0, 2.0).median() == pytest.approx(st.beta.median(3.0, 2.0), rel=1e-12)
+    g = L.gamma(None, 1.5, 3.0)
+    assert (2.0 * math.log(2.0) - 2.0 / 1.5 + g.params[2]) == pytest.approx(
+        st.gamma.logpdf(2.0, 3.0, scale=1.5), rel=1e-6)
+    assert (g.mean(), g.variance(), g.mode()) == pytest.approx((4.5, 6.75, 3.0))
+    e = L.erlang(None, 2.0, 4)
+    assert (3.0 * math.log(1.3) - 2.0 * 1.3 + e.params[2]) == pytest.approx(
+        st.gamma.logpdf(1.3, 4, scale=0.5), rel=1e-6)
+    x = L.exponential(None, 2.5)
+    assert (x.mean(), x.variance(), x.median()) == pytest.approx((0.4, 0.16, math.log(2) / 2.5))
+    assert L.uniform(None, -1.0, 3.0).variance() == pytest.approx(16.0 / 12.0)
+    for bad in (lambda: L.uniform(None, 1.0, 1.0), lambda: L.gaussian(None, 0.0, 0.0),
+                lambda: L.student_t(None, -1.0), lambda: L.beta(None, 0.0, 1.0),
+                lambda: L.gamma(None, 1.0, 0.0), lambda: L.exponential(None, 0.0),
+                lambda: L.erlang(None, 1.0, 0)):
+        with pytest.raises(ValueError, match="illegal"):
+            bad()
