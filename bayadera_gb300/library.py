@@ -15,6 +15,7 @@ gives the closed-form mean, mode, median and variance.
         x = core.sample(s, 8192)
 """
 import math
+import random
 
 import numpy as np
 
@@ -103,7 +104,6 @@ class LibraryDistribution:
     def _seed(self, options):
         if options and options.get("seed") is not None:
             return int(options["seed"])
-        import random
         return random.SystemRandom().getrandbits(31)
 
     def sampler(self, options=None):
