@@ -138,6 +138,20 @@ def extract(ref_root):
                    "sigma0": sbig[0], "sigma0_tol": sbig[1]},
     }
 
+    # ---- posterior engine, beta-binomial model (nvidia_gtx_test.clj:133-159): n, z, a, b,
+    # the points (range 0.001 1 0.001) as a 1 x 200 matrix, the constant that separates the
+    # posterior's log density from the conjugate beta's, and the binomial evidence
+    i = src.index('"Nvidia GTX posterior engine with Beta-Binomial model."')
+    nz = {k: float(re.compile(r"\b%s (\d+)" % k).search(src, i).group(1)) for k in ("n", "z", "a", "b")}
+    pm = re.compile(r"\(ge neanderthal-factory 1 (\d+) \(range ([\d.]+) ([\d.]+) ([\d.]+)\)\)").search(src, i)
+    const = re.compile(r"x-beta-log-pdf\) (-?[\d.]+)\)\) => \(roughly 0\.0 ([\d.]+)\)").search(src, i)
+    ev = re.compile(r"\(evidence binomial-lik-engine lik-params x\) => (-?[\d.]+E-?\d+)").search(src, i)
+    g["beta_binomial"] = {"n": nz["n"], "z": nz["z"], "a": nz["a"], "b": nz["b"],
+                          "points": int(pm.group(1)), "start": float(pm.group(2)),
+                          "step": float(pm.group(4)),
+                          "log_ratio": float(const.group(1)), "log_ratio_tol": float(const.group(2)),
+                          "evidence": float(ev.group(1))}
+
     # ---- HDI utilities (test/clojure/uncomplicate/bayadera/util_test.clj): the fixture
     # pdf / bin ranks / limits and the asserted hdi-rank-count, hdi-bins, hdi-regions
     usrc = open(os.path.join(ref_root, "test/clojure/uncomplicate/bayadera/util_test.clj")).read()

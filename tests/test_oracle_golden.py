@@ -156,3 +156,27 @@ def test_histogram_normalised(oracle):
     width = (limits[1::2] - limits[0::2]) / 256
     np.testing.assert_allclose((pdf * width[:, None]).sum(axis=1), 1.0, rtol=1e-5)
     assert counts.sum() == 3 * 4096
+
+
+def test_beta_binomial_posterior_and_evidence(golden):
+    """nvidia_gtx_test.clj:133-159 as the device models state it: the beta-binomial
+    posterior's log density (binomial loglik of (n, z) without the coefficient + the beta
+    prior with library.py's parameter vector) minus the conjugate Beta(a + z, b + n - z)'s
+    is the golden constant at every point, and the likelihood engine's evidence (the mean of
+    exp(loglik) over the points) is the golden value."""
+    import math
+    from bayadera_gb300 import library as L
+    g = golden["beta_binomial"]
+    n, z, a, b = g["n"], g["z"], g["a"], g["b"]
+    x = (g["start"] + g["step"] * np.arange(g["points"])).astype(np.float32).astype(np.float64)
+    prior = L.beta(None, a, b).params.astype(np.float64)
+    conj = L.beta(None, a + z, b + n - z).params.astype(np.float64)
+
+    def beta_log(p, t):
+        return (p[0] - 1.0) * np.log(t) + (p[1] - 1.0) * np.log1p(-t) + p[2]
+
+    loglik = z * np.log(x) + (n - z) * np.log1p(-x)
+    post = loglik + beta_log(prior, x)
+    diff = post - beta_log(conj, x)
+    assert np.linalg.norm(diff - g["log_ratio"]) / math.sqrt(x.size) <= g["log_ratio_tol"]
+    assert np.mean(np.exp(loglik)) == pytest.approx(g["evidence"], rel=1e-5)
