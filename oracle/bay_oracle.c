@@ -168,7 +168,7 @@ void bo_init_walkers_normal(uint32_t dim, uint64_t walkers, uint32_t seed, float
 }
 
 /* ======================= models ========================================
- * FP32 forms follow the reference's sources (cuda/distributions/*.cu) with
+ * FP32 forms follow the reference's sources (cuda/distributions/<name>.cu) with
  * serial fp32 sums; FP64 forms are the same densities in double. */
 #define LOG_SQRT_2PI_F 0.9189385332046727f
 #define LOG_SQRT_2PI 0.91893853320467274178

@@ -41,7 +41,7 @@ extern "C" {
 void bo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 float bo_u01_oo_32_24(uint32_t i);
 
-/* ---------------- direct samplers (cuda/rng/*-sampler.cu) ---------------- */
+/* ---------------- direct samplers (cuda/rng/<kind>-sampler.cu) ---------------- */
 void bo_sample_uniform(uint32_t n, float lower, float upper, uint32_t seed, float* out);
 void bo_sample_gaussian(uint32_t n, float mu, float sigma, uint32_t seed, float* out);
 void bo_sample_exponential(uint32_t n, float lambda, uint32_t seed, float* out);
