@@ -70,6 +70,9 @@ def test_model_check_builtin_library(native):
     prior = M.distribution_models()["gaussian"]
     for name, lik in M.likelihood_models().items():
         _check(M.device_posterior_model(prior, "post_" + name, lik))
+    # the reference's beta-binomial posterior (nvidia_gtx_test.clj:133-159)
+    _check(M.device_posterior_model(M.distribution_models()["beta"], "beta_binomial",
+                                    M.likelihood_models()["binomial"]))
 
 
 def test_model_check_benchmark_models(native):
