@@ -270,17 +270,19 @@ int bay_state_import(bay_sampler* s, const float* positions, const float* logfn,
 /* Log densities of the current walkers (walkers floats). */
 int bay_logfn_values(bay_sampler* s, float* out);
 
-/* Execution control: CUDA-graph replay of the step loops (default on). */
+/* Execution control (no reference counterpart: the reference launches every half-step
+ * from the JVM).  CUDA-graph replay of the step loops (default on). */
 int bay_sampler_set_graphs(bay_sampler* s, int enabled);
-/* Execution control of the resident tensor-core GEMM form: one persistent cooperative
- * launch per chunk of steps with a grid barrier between half-steps, or one launch per
- * half-step with programmatic dependent launch (default: faster on GB300).  Both give the
- * same results; other forms ignore it. */
+/* Execution control of the resident tensor-core GEMM form (no reference counterpart):
+ * one persistent cooperative launch per chunk of steps with a grid barrier between
+ * half-steps, or one launch per half-step with programmatic dependent launch (default:
+ * faster on GB300).  Both give the same results; other forms ignore it. */
 int bay_sampler_set_persistent(bay_sampler* s, int enabled);
-/* Testing the device failure path: with enabled != 0 the persistent form's grid barriers
- * wait for one more CTA than the launch has, so every CTA gives up after its bounded wait
- * (2 s), raises the abort flag and the status word, and the launch ends; the next status
- * check returns BAY_ERR_DEVICE.  No fault, trap or unbounded wait is involved. */
+/* Testing the device failure path (no reference counterpart): with enabled != 0 the
+ * persistent form's grid barriers wait for one more CTA than the launch has, so every CTA
+ * gives up after its bounded wait (2 s), raises the abort flag and the status word, and
+ * the launch ends; the next status check returns BAY_ERR_DEVICE.  No fault, trap or
+ * unbounded wait is involved. */
 int bay_sampler_test_barrier_timeout(bay_sampler* s, int enabled);
 
 /* ---------------------------------------------------------------- direct samplers
