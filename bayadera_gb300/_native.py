@@ -23,12 +23,15 @@ FORM_BATCH = 3
 MODEL_ACCEPT_REF = 1
 MODEL_GEMM_STREAMING = 2
 MODEL_GEMM_TENSOR = 4
+MODEL_STRETCH_REF = 8
+MODEL_PARTNER_ELEMENT = 16
 DIRECT_UNIFORM = 0
 DIRECT_GAUSSIAN = 1
 DIRECT_EXPONENTIAL = 2
 DIRECT_ERLANG = 3
 HIST_COMPAT_START1 = 1
 HIST_COMPAT_ZERO_LIMITS = 2
+HIST_COMPAT_FASTDIV = 4
 
 
 class BayaderaError(RuntimeError):

@@ -126,13 +126,28 @@ int guarded(F&& f) {
     }
 }
 
-bool is_device_ptr(const void* p) {
+// Decides where a caller's pointer lives: device memory that the kernels of a context on
+// `device` may read (true), or host memory that is staged through a copy (false).  Device
+// memory of another GPU is refused with BAY_ERR_ARG before anything is launched: without
+// peer access a kernel reading it faults.
+bool ptr_on_device(int type, int ptr_device, int device) {
+    if (type == cudaMemoryTypeDevice) {
+        if (ptr_device != device)
+            fail(BAY_ERR_ARG, "the array lies in device memory of device " +
+                                  std::to_string(ptr_device) + ", but the context runs on device " +
+                                  std::to_string(device));
+        return true;
+    }
+    return type == cudaMemoryTypeManaged;
+}
+
+bool is_device_ptr(const void* p, int device) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    return ptr_on_device((int)a.type, a.device, device);
 }
 
 // Process-wide cache of NVRTC output: identical (source, options) compile once.
@@ -158,6 +173,12 @@ struct bay_ctx {
     // the direct samplers' NVRTC module, compiled on first use
     CUlibrary direct_lib = nullptr;
     CUkernel k_direct = nullptr;
+    // device address of bay_acor_noalloc's fixed scratch array on this context's device,
+    // looked up when the context is created (the array itself is never allocated)
+    double* acor_scratch = nullptr;
+    // histogram bin counts with the fast division (BAY_HIST_COMPAT_FASTDIV): one NVRTC
+    // module per bin count, compiled on first use
+    std::map<uint32_t, std::pair<CUlibrary, CUkernel>> hist_fastdiv;
 
     void* alloc(size_t bytes) {
         if (bytes == 0) bytes = 16;
@@ -729,6 +750,8 @@ int bay_ctx_create(const bay_ctx_opts* opts, bay_ctx** out) {
             }
             cuda_check(cudaStreamCreateWithFlags(&c->capture, cudaStreamNonBlocking),
                        "cudaStreamCreate(capture)");
+            cuda_check(bay::acor_noalloc_scratch(&c->acor_scratch),
+                       "cudaGetSymbolAddress(acor scratch)");
         } catch (...) {
             if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
             if (c->capture) cudaStreamDestroy(c->capture);
@@ -746,6 +769,7 @@ int bay_ctx_release(bay_ctx* c) {
         cudaStreamSynchronize(c->stream);
         for (auto& kv : c->sizes) cudaFree(kv.first);
         if (c->direct_lib) g_cu.LibraryUnload(c->direct_lib);
+        for (auto& kv : c->hist_fastdiv) g_cu.LibraryUnload(kv.second.first);
         if (c->own_stream) cudaStreamDestroy(c->stream);
         cudaStreamDestroy(c->capture);
         delete c;
@@ -817,6 +841,13 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
     opts.push_back("-DBAY_CTA=" + std::to_string(cta));
     opts.push_back(std::string("-DBAY_ACCEPT_REF=") +
                    ((d->flags & BAY_MODEL_ACCEPT_REF) ? "1" : "0"));
+    opts.push_back(std::string("-DBAY_STRETCH_REF=") +
+                   ((d->flags & BAY_MODEL_STRETCH_REF) ? "1" : "0"));
+    if (d->flags & BAY_MODEL_PARTNER_ELEMENT) {
+        if (d->form != BAY_FORM_PLAIN && d->form != BAY_FORM_TILED)
+            fail(BAY_ERR_ARG, "BAY_MODEL_PARTNER_ELEMENT applies to the plain and tiled forms");
+        opts.push_back("-DBAY_PARTNER_ELEMENT=1");
+    }
     uint32_t wpc = 1;
     if (d->form == BAY_FORM_PLAIN) {
         if (!valid_ident(d->logfn)) fail(BAY_ERR_ARG, "logfn must name a C function");
@@ -1495,6 +1526,51 @@ uint64_t read_accepted(bay_sampler* s) {
     return v;
 }
 
+// Bin counts of dimension-major values (dm[d * W + w]) into counts[d * bins + b]: the
+// IEEE-division kernel, or with BAY_HIST_COMPAT_FASTDIV the reference's expression under
+// -use_fast_math (device/bay_hist_fastdiv.cuh; one NVRTC module per bin count and
+// context, compiled on first use).
+void hist_count(bay_ctx* c, uint32_t flags, const float* dm, uint32_t D, uint64_t W,
+                uint32_t bins, const float* lim, uint32_t* counts) {
+    if (D > 65535) fail(BAY_ERR_ARG, "histograms of at most 65535 dimensions");
+    if (!(flags & BAY_HIST_COMPAT_FASTDIV)) {
+        cuda_check(bay::launch_hist_count(dm, D, W, bins, lim, counts, c->stream), "histogram");
+        return;
+    }
+    CUkernel k = nullptr;
+    auto it = c->hist_fastdiv.find(bins);
+    if (it != c->hist_fastdiv.end()) {
+        k = it->second.second;
+    } else {
+        std::string src = "\n#line 1 \"bay_hist_fastdiv.cuh\"\n";
+        src += bay_embedded_hist_fastdiv;
+        const std::vector<std::string> opts = {"-arch=sm_103a", "-use_fast_math", "-default-device",
+                                               "-std=c++17",
+                                               "-DBAY_HIST_BINS=" + std::to_string(bins)};
+        std::vector<char> cubin = nvrtc_compile(src, opts);
+        CUlibrary lib = nullptr;
+        cu_check(g_cu.LibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+                 "cuLibraryLoadData(histogram)");
+        const CUresult r = g_cu.LibraryGetKernel(&k, lib, "bay_hist_count_fastdiv");
+        if (r != CUDA_SUCCESS) {
+            g_cu.LibraryUnload(lib);
+            cu_check(r, "GetKernel(histogram)");
+        }
+        c->hist_fastdiv[bins] = std::make_pair(lib, k);
+    }
+    const float* xp = dm;
+    unsigned int dd = D;
+    unsigned long long ww = W;
+    const float* lp = lim;
+    unsigned int* cp = counts;
+    void* args[] = {&xp, &dd, &ww, &lp, &cp};
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(64, (W + 255) / 256));
+    cu_check(g_cu.LaunchKernel((CUfunction)k, gx, D, 1, 256, 1, 1, 0, (CUstream)c->stream, args,
+                               nullptr),
+             "cuLaunchKernel(histogram, fast division)");
+    bay::count_launches(1);
+}
+
 uint32_t acor_lag(uint64_t n, uint32_t wgs) {
     uint64_t l = n / 5;
     if (wgs < l) l = wgs;
@@ -1624,7 +1700,7 @@ static int moments_out(bay_sampler* s, double* out, int which) {
                    "cudaMemcpy(moments)");
         cuda_check(cudaStreamSynchronize(s->ctx->stream), "sync");
         s->check_status();
-        if (which == 2 && !is_device_ptr(out))
+        if (which == 2 && !is_device_ptr(out, s->ctx->device))
             for (uint32_t d = 0; d < s->D; ++d) out[d] = std::sqrt(out[d]);
     });
 }
@@ -1632,7 +1708,12 @@ static int moments_out(bay_sampler* s, double* out, int which) {
 int bay_mean(bay_sampler* s, double* out) { return moments_out(s, out, 0); }
 int bay_variance(bay_sampler* s, double* out) { return moments_out(s, out, 1); }
 int bay_sd(bay_sampler* s, double* out) {
-    if (out && is_device_ptr(out)) {
+    bool dev = false;
+    const int g = guarded([&] {
+        if (s && out) dev = is_device_ptr(out, s->ctx->device);
+    });
+    if (g != BAY_OK) return g;
+    if (dev) {
         g_err = "bay_sd writes host memory only";
         return BAY_ERR_ARG;
     }
@@ -1684,15 +1765,12 @@ int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags
         cuda_check(bay::launch_fill_u32(s->counts, (flags & BAY_HIST_COMPAT_START1) ? 1u : 0u,
                                         (uint64_t)bins * s->D, c->stream),
                    "fill");
-        cuda_check(bay::launch_hist_count(dm, s->D, s->W, bins, d_lim, s->counts, c->stream),
-                   "histogram");
+        hist_count(c, flags, dm, s->D, s->W, bins, d_lim, s->counts);
         if (cycles > 1) {
             s->set_a_beta(s->a, 1.0f);
             for (uint32_t i = 1; i < cycles; ++i) {
                 s->steps(false, 1);
-                cuda_check(bay::launch_hist_count(s->dim_major(), s->D, s->W, bins, d_lim,
-                                                  s->counts, c->stream),
-                           "histogram");
+                hist_count(c, flags, s->dim_major(), s->D, s->W, bins, d_lim, s->counts);
             }
             s->iteration_counter += cycles - 1;
         }
@@ -1715,7 +1793,7 @@ int bay_acor(bay_ctx* c, const float* series, uint32_t D, uint64_t n, double* ta
         if (D == 0) fail(BAY_ERR_ARG, "dim must be >= 1");
         std::lock_guard<std::recursive_mutex> lk(c->mu);
         c->use();
-        if (is_device_ptr(series)) {
+        if (is_device_ptr(series, c->device)) {
             rc = acor_device(c, series, D, n, tau, mean, sigma, lag);
             return;
         }
@@ -1742,7 +1820,7 @@ int bay_acor_noalloc(bay_ctx* c, const float* d_series, uint32_t D, uint64_t n, 
     return guarded([&] {
         if (!c || !d_series) fail(BAY_ERR_ARG, "NULL argument");
         if (D == 0) fail(BAY_ERR_ARG, "dim must be >= 1");
-        if (!is_device_ptr(d_series))
+        if (!is_device_ptr(d_series, c->device))
             fail(BAY_ERR_ARG, "bay_acor_noalloc needs the series in device memory");
         const uint64_t need = (uint64_t)D * n + 3ull * D;
         if (n > 0xffffffffull || need > BAY_ACOR_NOALLOC_MAX_DOUBLES)
@@ -1757,8 +1835,7 @@ int bay_acor_noalloc(bay_ctx* c, const float* d_series, uint32_t D, uint64_t n, 
                                   ") must not be less than " + std::to_string(lag * 5) + ".");
         std::lock_guard<std::recursive_mutex> lk(c->mu);
         c->use();
-        double* work = nullptr;
-        cuda_check(bay::acor_noalloc_scratch(c->device, &work), "cudaGetSymbolAddress(acor scratch)");
+        double* work = c->acor_scratch;
         double* res = work + (size_t)D * n;
         cuda_check(bay::launch_acor(d_series, D, (uint32_t)n, c->wgs, lag, work, res, res + D,
                                     res + 2 * D, c->stream),

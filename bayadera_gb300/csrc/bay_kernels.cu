@@ -3,7 +3,6 @@
 // ranks, acor, and the device-resident control block.  The per-model fused stretch
 // kernels are in device/bay_stretch.cuh (NVRTC).
 #include <atomic>
-#include <mutex>
 
 #include "bay_kernels.cuh"
 #include "device/bay_rng.cuh"
@@ -564,21 +563,13 @@ cudaError_t launch_acor(const float* series, uint32_t D, uint32_t n, uint32_t wg
     return cudaGetLastError();
 }
 
-cudaError_t acor_noalloc_scratch(int device, double** ptr) {
-    // Host code must not use g_acor_noalloc_scratch's name as an address: it is a
-    // host-side stand-in.  The device address comes from cudaGetSymbolAddress, looked up
-    // once per device with that device current (the caller made it current).
-    static std::mutex mu;
-    static double* cache[64] = {nullptr};
-    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> g(mu);
-    if (!cache[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_acor_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        cache[device] = static_cast<double*>(p);
-    }
-    *ptr = cache[device];
+cudaError_t acor_noalloc_scratch(double** ptr) {
+    // In host code g_acor_noalloc_scratch names a host-side stand-in, not the array: its
+    // device address comes from cudaGetSymbolAddress, with the device current.
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_acor_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    *ptr = static_cast<double*>(p);
     return cudaSuccess;
 }
 

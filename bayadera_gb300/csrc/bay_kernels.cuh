@@ -129,9 +129,9 @@ cudaError_t launch_acor(const float* series, uint32_t D, uint32_t n, uint32_t wg
                         double* work, double* tau, double* mean, double* sigma, cudaStream_t s);
 // Fixed scratch of bay_acor_noalloc: dim * n + 3 * dim doubles at most (8 MiB).
 #define BAY_ACOR_NOALLOC_MAX_DOUBLES (1u << 20)
-// Device address of that scratch on `device` (which must be current); looked up with
-// cudaGetSymbolAddress on the first call per device.  Allocates nothing.
-cudaError_t acor_noalloc_scratch(int device, double** ptr);
+// Device address of that scratch on the current device (cudaGetSymbolAddress; loads the
+// library's module on that device if it is not loaded yet).  Allocates nothing.
+cudaError_t acor_noalloc_scratch(double** ptr);
 // Kernels enqueued through this library in this process (graph nodes counted at replay).
 unsigned long long launch_count();
 void count_launches(unsigned long long n);

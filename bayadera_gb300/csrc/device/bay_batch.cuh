@@ -91,13 +91,11 @@ struct bay_batch_params {
     unsigned int half, step_off, means_cap, n_members;
 };
 
-// log u <= (dim - 1) log z + beta (ly - lx) in FP64; a non-finite proposal is rejected
+// log u <= (dim - 1) log z + beta (ly - lx), decided as in FP64 (bay_accept_log); a
+// non-finite proposal is rejected
 __device__ __forceinline__ bool bay_batch_accept(float u2, float z, float ly, float lx,
                                                  float beta, unsigned int dim) {
-    if (!isfinite(ly)) return false;
-    const double lq = (double)(dim - 1) * (double)__logf(z)
-        + (double)beta * ((double)ly - (double)lx);
-    return (double)__logf(u2) <= lq;
+    return bay_accept_log(u2, z, ly, lx, beta, dim - 1);
 }
 
 struct bay_bcf {
@@ -115,8 +113,17 @@ __device__ __forceinline__ bay_bcf bay_bcadd(bay_bcf a, bay_bcf b) {
     return r;
 }
 
+#ifndef BAY_STRETCH_REF
+#define BAY_STRETCH_REF 0
+#endif
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
+    // the stretch kernels' form (device/bay_stretch.cuh): fixed operation order, 1/a IEEE
+    // or, with BAY_STRETCH_REF, the fast division of the reference's build
+#if BAY_STRETCH_REF
+    const float inv_a = 1.0f / a;
+#else
     const float inv_a = __fdiv_rn(1.0f, a);
+#endif
     const float c1 = __fadd_rn(__fsub_rn(a, 2.0f), inv_a);
     const float c2 = __fmul_rn(2.0f, __fsub_rn(1.0f, inv_a));
     return __fadd_rn(__fmaf_rn(__fmul_rn(c1, u1), u1, __fmul_rn(c2, u1)), inv_a);

@@ -8,6 +8,8 @@
 // bay_u01: the reference's u01fpt_oo_32_24 (cuda/rng/uniform-sampler.cu:11-13),
 // (0.5 + (i >> 9)) * 2^-23, an exactly representable value in (0, 1).
 //
+// bay_accept_log: the stretch move's accept test, shared by every kernel form.
+//
 // This header is compiled both by nvcc (into libbayadera_gb300.so) and by NVRTC
 // (prepended to every fused stretch kernel), so it uses no host headers.
 #pragma once
@@ -41,6 +43,34 @@ __device__ __forceinline__ bay_u4 bay_philox4x32_10(bay_u4 c, unsigned int k0, u
 __device__ __forceinline__ float bay_u01(unsigned int i) {
     // (0.5 + (i >> 9)) * 2^-23: both steps are exact in fp32.
     return __fmul_rn(__fadd_rn(0.5f, (float)(i >> 9)), 1.1920928955078125E-7f);
+}
+
+// The stretch move's Metropolis test (Goodman & Weare 2010, eq. 7) in log space:
+// accept iff log u <= dm1 log z + beta (ly - lx), dm1 = dimension - 1; a non-finite
+// proposal density is rejected.  The decision is that of the test in FP64 with FP64 logs.
+// An fp32 evaluation with the fast logs decides whenever its two sides differ by more than
+// a bound on its error; inside that band (a few walkers in 10^5) the FP64 logs decide.  So
+// the decision does not depend on the fast logs' rounding (a CPU restatement with FP64 logs
+// reproduces it), and the common path has no FP64 arithmetic.
+//   fp32 errors: __logf at most 2^-21.41 absolute on [0.5, 2] and 3 ulp elsewhere, i.e.
+//   below 2^-21.41 (1 + |log|); ly - lx and the product with beta each rounded once, below
+//   2^-23 |beta| (|ly| + |lx|); the fma and the subtraction of tol below 2^-23 of |rhs| and
+//   tol.  tol is at least twice their sum.  Non-finite sides make the band test false
+//   (inf - inf), so those cases go to the FP64 comparison too.
+__device__ __forceinline__ bool bay_accept_log(float u2, float z, float ly, float lx, float beta,
+                                               unsigned int dm1) {
+    if (!isfinite(ly)) return false;
+    const float fd = (float)dm1;
+    const float lz = __logf(z);
+    const float lhs = __logf(u2);
+    const float dl = beta * (ly - lx);
+    const float rhs = fmaf(fd, lz, dl);
+    const float tol = 0x1p-20f * (1.0f + fabsf(lhs) + fd * (1.0f + fabsf(lz)) + fabsf(rhs))
+        + 0x1p-21f * fabsf(beta) * (fabsf(ly) + fabsf(lx));
+    if (lhs < rhs - tol) return true;
+    if (lhs > rhs + tol) return false;
+    const double dl64 = (double)beta * ((double)ly - (double)lx);
+    return log((double)u2) <= (double)dm1 * log((double)z) + dl64;
 }
 
 #endif

@@ -25,7 +25,15 @@
 //     BAY_ROW_LEN, BAY_PREP_LEN, BAY_WPC (walkers per CTA)
 //   BAY_CTA        threads per CTA
 //   BAY_ACCEPT_REF 1: accept if u <= z^(D-1) exp(beta dl) in fp32 (the reference's
-//                  formula); 0 (default): log u <= (D-1) log z + beta dl in FP64.
+//                  formula); 0 (default): log u <= (D-1) log z + beta dl, decided as in
+//                  FP64 (bay_accept_log).
+//   BAY_STRETCH_REF 1: the stretch factor's 1/a by the compiler's fast division (the
+//                  reference's build flavour, -use_fast_math); 0 (default): IEEE 1/a.
+//                  Both keep the operation order the golden trajectories pin.
+//   BAY_PARTNER_ELEMENT 1 (plain and tiled forms): the reference's partner offset
+//                  (uint)(u0 K DIM), an element offset that straddles walkers for
+//                  DIM > 1; elements past the half's end read as 0.  0 (default): the
+//                  partner is walker (uint)(u0 K), clamped to the half.
 
 #ifndef BAY_CTA
 #define BAY_CTA 256
@@ -35,6 +43,12 @@
 #endif
 #ifndef BAY_TILED
 #define BAY_TILED 0
+#endif
+#ifndef BAY_STRETCH_REF
+#define BAY_STRETCH_REF 0
+#endif
+#ifndef BAY_PARTNER_ELEMENT
+#define BAY_PARTNER_ELEMENT 0
 #endif
 #ifndef BAY_GEMM
 #define BAY_GEMM 0
@@ -99,19 +113,45 @@ struct bay_stretch_params {
 };
 
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
-    // z = (a - 2 + 1/a) u1^2 + 2 (1 - 1/a) u1 + 1/a with the first product fused,
-    // each other operation IEEE-rounded (matches the oracle and the golden vectors).
+    // z = (a - 2 + 1/a) u1^2 + 2 (1 - 1/a) u1 + 1/a with the first product fused and
+    // every other operation rounded on its own: the order the reference's golden
+    // trajectories pin (the current compiler contracts the reference's spelling of the
+    // expression, nvidia-gtx-mcmc-stretch.cu:71-72, differently).  1/a is IEEE by default;
+    // BAY_STRETCH_REF takes the reference build's flavour, the compiler's fast division
+    // (this module is compiled with -use_fast_math, as the reference's is).
+#if BAY_STRETCH_REF
+    const float inv_a = 1.0f / a;
+#else
     const float inv_a = __fdiv_rn(1.0f, a);
+#endif
     const float c1 = __fadd_rn(__fsub_rn(a, 2.0f), inv_a);
     const float c2 = __fmul_rn(2.0f, __fsub_rn(1.0f, inv_a));
     return __fadd_rn(__fmaf_rn(__fmul_rn(c1, u1), u1, __fmul_rn(c2, u1)), inv_a);
 }
 
 __device__ __forceinline__ unsigned int bay_partner(float u0, unsigned int K) {
+#if BAY_PARTNER_ELEMENT
+    // the reference's element offset (uint)(u0 * K * DIM), two fp32 products
+    return __float2uint_rz(__fmul_rn(__fmul_rn(u0, (float)K), (float)DIM));
+#else
     // Walker j = (uint)(u0 * K) of the complementary half; u0 < 1 can still round
     // u0*K up to K, so clamp (the reference would read past the half there).
     unsigned int j = __float2uint_rz(__fmul_rn(u0, (float)K));
     return j < K ? j : K - 1;
+#endif
+}
+
+// Coordinate i of the partner j (bay_partner) in the complementary half S of K walkers.
+__device__ __forceinline__ float bay_partner_coord(const float* S, unsigned int K, unsigned int j,
+                                                   unsigned int i) {
+#if BAY_PARTNER_ELEMENT
+    // an element offset: past the half's last element the reference reads out of bounds
+    // (or the moving half, racing with its writes); here those elements read as 0
+    const unsigned long long e = (unsigned long long)j + i;
+    return e < (unsigned long long)K * DIM ? S[e] : 0.0f;
+#else
+    return S[(size_t)j * DIM + i];
+#endif
 }
 
 __device__ __forceinline__ bool bay_accept(float u2, float z, float ly, float lx, float beta) {
@@ -119,10 +159,7 @@ __device__ __forceinline__ bool bay_accept(float u2, float z, float ly, float lx
     const float q = isfinite(ly) ? powf(z, (float)(DIM - 1)) * expf(beta * (ly - lx)) : 0.0f;
     return u2 <= q;
 #else
-    if (!isfinite(ly)) return false;
-    const double lq = (double)(DIM - 1) * (double)__logf(z)
-        + (double)beta * ((double)ly - (double)lx);
-    return (double)__logf(u2) <= lq;
+    return bay_accept_log(u2, z, ly, lx, beta, DIM - 1);
 #endif
 }
 
@@ -1805,7 +1842,7 @@ __device__ __forceinline__ void bay_stretch_plain(const bay_stretch_params& P) {
         const unsigned int j = bay_partner(u0, P.K);
 #pragma unroll
         for (int i = 0; i < DIM; ++i) {
-            const float s = S[(size_t)j * DIM + i];
+            const float s = bay_partner_coord(S, P.K, j, i);
             Y[i] = __fmaf_rn(z, __fsub_rn(X[(size_t)k * DIM + i], s), s);
         }
         const float ly = BAY_LOGFN((unsigned int)P.data_len, P.params_len, P.params, DIM, Y);
@@ -1974,7 +2011,7 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
             float Y[DIM];
 #pragma unroll
             for (int i = 0; i < DIM; ++i) {
-                const float s = S[(size_t)j * DIM + i];
+                const float s = bay_partner_coord(S, P.K, j, i);
                 Y[i] = __fmaf_rn(z, __fsub_rn(X[(size_t)k * DIM + i], s), s);
                 sY[t][i] = Y[i];
             }

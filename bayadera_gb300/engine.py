@@ -92,12 +92,15 @@ class GB300BayaderaFactory:
         return v.value
 
     def mcmc_factory(self, model, form=None, accept_ref=False, walkers_per_cta=0,
-                     cta_threads=0, streaming=False, tensor=False):
+                     cta_threads=0, streaming=False, tensor=False, stretch_ref=False,
+                     partner_element=False):
         """EngineFactory/mcmc-factory: compile the model's fused stretch kernels.  GEMM form:
         streaming=True streams the matrix even when it fits in shared memory; tensor=True
-        streams it through the tensor cores (split bf16, fp32 accumulation)."""
+        streams it through the tensor cores (split bf16, fp32 accumulation).  Reference
+        compatibility: accept_ref (fp32 accept formula), stretch_ref (the stretch factor's
+        fast-math expression), partner_element (the element-offset partner, quirk Q1)."""
         return GB300StretchFactory(self, model, form, accept_ref, walkers_per_cta, cta_threads,
-                                   streaming, tensor)
+                                   streaming, tensor, stretch_ref, partner_element)
 
     def acor(self, data_matrix):
         return self.acor_engine.acor(data_matrix)
@@ -153,7 +156,7 @@ class GB300BayaderaFactory:
 
 
 def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0,
-               streaming=False, tensor=False):
+               streaming=False, tensor=False, stretch_ref=False, partner_element=False):
     """bay_model_desc of a DeviceDistributionModel; form 'plain' | 'tiled' | None (tiled
     when the model has a tiled form)."""
     if form is None:
@@ -172,7 +175,9 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
     d.params_size = model.params_size
     d.flags = ((N.MODEL_ACCEPT_REF if accept_ref else 0) |
                (N.MODEL_GEMM_STREAMING if streaming else 0) |
-               (N.MODEL_GEMM_TENSOR if tensor else 0))
+               (N.MODEL_GEMM_TENSOR if tensor else 0) |
+               (N.MODEL_STRETCH_REF if stretch_ref else 0) |
+               (N.MODEL_PARTNER_ELEMENT if partner_element else 0))
     d.cta_threads = cta_threads
     if form == "tiled":
         t = model.tiled
@@ -281,19 +286,22 @@ class GB300DensityEngine:
         return r.value
 
 
-def check_model(model, form=None, wgs=1024, accept_ref=False, tensor=False):
+def check_model(model, form=None, wgs=1024, accept_ref=False, tensor=False, stretch_ref=False,
+                partner_element=False):
     """Compile-check a model's fused kernels with NVRTC (no device needed)."""
-    d, keep = model_desc(model, form, accept_ref, tensor=tensor)
+    d, keep = model_desc(model, form, accept_ref, tensor=tensor, stretch_ref=stretch_ref,
+                         partner_element=partner_element)
     N.call("bay_model_check", C.byref(d), wgs)
 
 
 class GB300StretchFactory:
     def __init__(self, factory, model, form=None, accept_ref=False, walkers_per_cta=0,
-                 cta_threads=0, streaming=False, tensor=False):
+                 cta_threads=0, streaming=False, tensor=False, stretch_ref=False,
+                 partner_element=False):
         self.factory = factory
         self.model = model
         d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, streaming,
-                             tensor)
+                             tensor, stretch_ref, partner_element)
         h = C.c_void_p()
         N.call("bay_model_compile", factory.ctx, C.byref(d), C.byref(h))
         self.handle = h

@@ -7,12 +7,17 @@ acor and 128-bin histograms).
 
 One step = that whole job on one GPU.  `value` times it with the inputs resident on the
 device; `e2e` times the same job through the C ABI from host buffers (sampler creation
-with the host copy of the precision matrix, results copied back).  The reference arm
-(--impl reference) times the CPU restatement of the reference's stretch kernel on the
-host cores.  Multi-GPU: independent replicas (the path has no exchange step).
+with the host copy of the precision matrix, results copied back).  The default line also
+carries `configs`: the other benchmark workloads (the 2-D Gaussian posterior, logistic
+regression, 512 hierarchical models, robust regression), each its fast form beside the
+plain fp32 form with its log-density error against FP64 on its own data.  The reference
+arm (--impl reference) times the CPU restatement of the reference's stretch kernel, built
+for speed, on the host cores.  Multi-GPU: independent replicas (the path has no exchange
+step).
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -34,6 +39,9 @@ SEED = 0
 BYTES_PER_WALKER_STEP = 12 * DIM + 8      # read self + partner, write on accept, 2 logfn
 FLOP_PER_WALKER_STEP = 2 * DIM * DIM      # dense -x'Px/2
 L2_FLUSH_BYTES = 256 << 20
+LOG_SQRT_2PI = 0.5 * math.log(2.0 * math.pi)
+# the reference arm and cpu_baseline: the whole 50-D job on this many of its walkers
+CPU_WALKERS = 16384
 
 
 def precision_matrix(dim=DIM, seed=SEED):
@@ -104,12 +112,18 @@ class ClockSampler:
 
 
 def measured_peaks():
+    """Roofline denominators: the machine's measured HBM copy bandwidth (GB/s) and cuBLAS bf16
+    rate (TFLOP/s, burst), else the stated fallbacks."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
             j = json.load(f)
-        return j.get("hbm_gbs", 6800.0), "measured"
-    return 6800.0, "fallback"
+        return {"hbm_gbs": float(j.get("hbm_gbs", 6800.0)),
+                "bf16_tflops": float(j.get("bf16_tflops", 1900.0)), "kind": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "kind": "fallback"}
+
+
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12     # nominal: no measured FP32 figure
 
 
 def profile_traffic():
@@ -126,26 +140,129 @@ def profile_traffic():
     return None
 
 
-# ------------------------------------------------------------------ CPU (oracle) timing
-def cpu_sample(steps_budget_s=12.0, walkers=WALKERS):
-    """The CPU restatement of the reference's stretch kernel (OpenMP over walkers, all
-    host cores) on the same workload: bounded to about steps_budget_s of CPU work."""
+# ------------------------------------------------------------------ FP64 error measures
+# Log densities of the configs' models in FP64 (numpy, or torch float64 for the large
+# design matrices), written from the models' formulas; used to report each config's
+# log-density error on its own data.
+def _err(lf, want):
+    lf = np.asarray(lf, np.float64)
+    want = np.asarray(want, np.float64)
+    ok = np.isfinite(want)
+    err = np.abs(lf[ok] - want[ok])
+    rel = err / np.maximum(np.abs(want[ok]), 1e-30)
+    return {"max_abs": float(err.max()), "median_abs": float(np.median(err)),
+            "max_rel": float(rel.max()), "walkers": int(ok.sum())}
+
+
+def fp64_c1(params, pos):
+    """2-D (mu, sigma) posterior: sum_i log N(y_i | mu, sigma) + log N(mu | h0, h1) +
+    log U(sigma | h2, h3); pos (W, 2)."""
+    y = np.asarray(params[:-4], np.float64)
+    h = np.asarray(params[-4:], np.float64)
+    mu, sg = pos[:, 0].astype(np.float64), pos[:, 1].astype(np.float64)
+    ss = np.zeros(mu.size)
+    for c in range(0, y.size, 2000):
+        ss += ((y[None, c:c + 2000] - mu[:, None]) ** 2).sum(axis=1)
+    ll = -ss / (2.0 * sg * sg) - y.size * (np.log(sg) + LOG_SQRT_2PI)
+    pr = -(mu - h[0]) ** 2 / (2.0 * h[1] ** 2) - math.log(h[1]) - LOG_SQRT_2PI
+    pr = pr + np.where((h[2] <= sg) & (sg <= h[3]), -math.log(h[3] - h[2]), -np.inf)
+    return ll + pr
+
+
+def fp64_mvn(P, pos):
+    P64 = P.astype(np.float64)
+    x = pos.astype(np.float64)
+    return -0.5 * np.einsum("wi,ij,wj->w", x, P64, x)
+
+
+def fp64_logistic(rows_dev, F, sd, pos):
+    """sum_n y_n eta_n - softplus(eta_n) - |beta|^2 / (2 sd^2); rows_dev (n, F + 1) on the
+    device, summed in torch float64 by row chunks."""
+    import torch
+    B = torch.from_numpy(pos.astype(np.float64)).cuda()
+    acc = torch.zeros(B.shape[0], dtype=torch.float64, device="cuda")
+    for r0 in range(0, rows_dev.shape[0], 1 << 18):
+        blk = rows_dev[r0:r0 + (1 << 18)].double()
+        eta = blk[:, :F] @ B.T
+        y = blk[:, F:F + 1]
+        acc += (y * eta - (eta.clamp(min=0.0) + torch.log1p(torch.exp(-eta.abs())))).sum(0)
+    acc -= (B * B).sum(1) / (2.0 * sd * sd)
+    return acc.cpu().numpy()
+
+
+def fp64_robust_t(rows_dev, F, h, pos):
+    """sum_n -(nu + 1)/2 log(1 + r_n^2 / nu) - N log sigma - |beta|^2/(2 h1^2)
+    - (log sigma)^2/(2 h2^2), r = (y - x.beta)/sigma; torch float64 by row chunks."""
+    import torch
+    X = torch.from_numpy(pos.astype(np.float64)).cuda()
+    B, ls = X[:, :F], X[:, F]
+    inv_s = torch.exp(-ls)
+    nu = float(h[0])
+    acc = torch.zeros(X.shape[0], dtype=torch.float64, device="cuda")
+    n = rows_dev.shape[0]
+    for r0 in range(0, n, 1 << 19):
+        blk = rows_dev[r0:r0 + (1 << 19)].double()
+        z = (blk[:, F:F + 1] - blk[:, :F] @ B.T) * inv_s[None, :]
+        acc += (-0.5 * (nu + 1.0) * torch.log1p(z * z / nu)).sum(0)
+    acc += -n * ls - (B * B).sum(1) / (2.0 * float(h[1]) ** 2) - ls * ls / (2.0 * float(h[2]) ** 2)
+    return acc.cpu().numpy()
+
+
+def fp64_hrows(params, rows, pos):
+    """Row-encoded hierarchical model: sum_i c_i (y_i - theta_g_i)^2 + sum_j [-(theta_j -
+    mu)^2/(2 tau^2) - log tau] - mu^2/(2 h0^2) - (log tau)^2/(2 h1^2); pos (W, J + 2)."""
+    r = np.asarray(params[:3 * rows], np.float64).reshape(rows, 3)
+    h = np.asarray(params[3 * rows:], np.float64)
+    x = pos.astype(np.float64)
+    J = x.shape[1] - 2
+    g = r[:, 1].astype(np.int64)
+    d = r[None, :, 0] - x[:, g]
+    res = (r[None, :, 2] * d * d).sum(axis=1)
+    mu, lt = x[:, J], x[:, J + 1]
+    res += (-(x[:, :J] - mu[:, None]) ** 2 * 0.5 * np.exp(-2.0 * lt)[:, None]).sum(axis=1)
+    return res - J * lt - mu * mu / (2.0 * h[0] ** 2) - lt * lt / (2.0 * h[1] ** 2)
+
+
+# ------------------------------------------------------------------ CPU port (reference arm)
+def cpu_port(threads, walkers=CPU_WALKERS):
+    """The CPU restatement of the reference's stretch kernel plus the same model, in its
+    speed build (-O3 -ffast-math -funroll-loops, OpenMP over the walkers of a half-step):
+    the reference's own CPU path (OpenCL on pocl) cannot run here."""
     from oracle import oracle as O
+    O.use_speed_build(True)
     P, _ = precision_matrix()
-    threads = os.cpu_count() or 1
     r = O.Stretch("mvn_precision", DIM, walkers, P.reshape(-1), seed=SEED, threads=threads,
                   flags=O.ACCEPT_LOG64)
-    r.init_position_normal(SEED + 1)
-    t0 = time.perf_counter()
-    r.move_bare()
-    t1 = time.perf_counter() - t0
-    n = max(1, int(steps_budget_s / max(t1, 1e-6)))
-    t0 = time.perf_counter()
-    for _ in range(n):
-        r.move_bare()
-    dt = time.perf_counter() - t0
-    return {"value": walkers * n / dt, "unit": "walker-steps/s", "cores": threads, "kind": "port",
-            "sample": "%d ensemble steps of the %d-walker 50-D job (%.1f s)" % (n, walkers, dt)}
+    return O, r
+
+
+def cpu_job(O, r, seed):
+    """The 50-D job on the CPU port: init!, N(0, I) walkers, 2,000 burn-in steps, 4,000
+    accu steps with per-step means, mean, variance, 128-bin histograms, acor."""
+    r.init(seed)
+    r.init_position_normal(seed + 1)
+    r.burn_in(BURN, 2.0)
+    _, means = r.run_sampler(RUN, 2.0)
+    O.mean64(r.xs, DIM)
+    O.variance64(r.xs, DIM)
+    O.histogram([r.xs], DIM, BINS)
+    O.acor64(means)
+
+
+def cpu_sample(budget_s=10.0):
+    """cpu_baseline: whole CPU-port jobs on CPU_WALKERS walkers until budget_s of work."""
+    threads = os.cpu_count() or 1
+    O, r = cpu_port(threads)
+    times = []
+    while not times or sum(times) < budget_s:
+        t0 = time.perf_counter()
+        cpu_job(O, r, SEED + 7 * len(times))
+        times.append(time.perf_counter() - t0)
+    v = CPU_WALKERS * (BURN + RUN) * len(times) / sum(times)
+    return {"value": v, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d whole 50-D jobs (2,000 burn-in + 4,000 run steps, mean, variance, "
+                      "128-bin histograms, acor) on %d of the 65,536 walkers, %.1f s; speed "
+                      "build of the CPU port" % (len(times), CPU_WALKERS, sum(times))}
 
 
 def max_over_ranks(t, dist, device):
@@ -165,22 +282,35 @@ def replica_throughput(jobs, world, t_total):
 
 
 def run_reference(args):
+    """The reference arm: each step is one whole 50-D job on CPU_WALKERS walkers on the
+    host cores (the job's per-walker work does not depend on the walker count; the full
+    65,536-walker job would take about 4 x as long per step)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    budget = max(3.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
-    for _ in range(args.warmup):
-        cpu_sample(budget / 4)
-    vals = [cpu_sample(budget) for _ in range(args.steps)]
-    v = statistics.median(x["value"] for x in vals)
+    threads = os.cpu_count() or 1
+    O, r = cpu_port(threads)
+    for w in range(args.warmup):
+        cpu_job(O, r, 100 + w)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_job(O, r, 1000 + 17 * k)
+        times.append(time.perf_counter() - t0)
+    t_med = statistics.median(times)
+    v = CPU_WALKERS * (BURN + RUN) / t_med
+    sample = ("each step one whole 50-D job (2,000 burn-in + 4,000 run steps, mean, "
+              "variance, 128-bin histograms, acor) on %d of the 65,536 walkers; median of %d "
+              "steps; speed build of the CPU port (-O3 -ffast-math, OpenMP)"
+              % (CPU_WALKERS, args.steps))
     line = {
         "impl": "reference", "metric": "walker-steps/s", "value": v, "unit": "walker-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * WALKERS * (BURN + RUN) / v, "higher_is_better": True,
+        "ms_per_step": 1e3 * t_med, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config(),
-        "cpu_baseline": {"value": v, "unit": "walker-steps/s", "cores": vals[0]["cores"],
-                         "kind": "port", "sample": vals[0]["sample"]},
+        "config": dict(config(), cpu_walkers=CPU_WALKERS),
+        "cpu_baseline": {"value": v, "unit": "walker-steps/s", "cores": threads,
+                         "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "walker-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -198,10 +328,10 @@ def config():
 
 
 # ------------------------------------------------------------------ other workloads
-# (measured with --config; the default line above is the 50-D Gaussian job)
-def _workload(name, rows=0):
-    """(model factory args, params builder, walkers, burn, run, bins, init, algorithmic
-    FLOP and bytes per walker-step, description) of the other benchmark workloads."""
+def _workload(name, rows=0, quick=False):
+    """Model, params, walkers, steps, init, algorithmic work and FP64 error measure of the
+    benchmark workloads other than the 50-D job.  quick: fewer plain-form steps (the
+    configs object of the default line)."""
     import torch
     from bayadera_gb300 import models as M
     if name == "c1":
@@ -211,7 +341,8 @@ def _workload(name, rows=0):
         return dict(model=M.gaussian_posterior_model(), fast="tiled", params=params,
                     walkers=4096, burn=512, run=1024, bins=256,
                     init=lambda s, seed: s.init_position(seed, [2.0, 4.0, 1.0, 3.0]),
-                    flop=3 * 10000, bytes=0,
+                    flop=3 * 10000, bytes=0, bound="fp32",
+                    fp64=lambda pos: fp64_c1(params, pos), check=4096,
                     desc="2-D Gaussian (mu, sigma) posterior, N=10,000 data, prior "
                          "N(0,10^2) x U(0,20)")
     if name == "c3":
@@ -221,16 +352,18 @@ def _workload(name, rows=0):
         beta = rng.normal(0.0, 1.0 / 8.0, F)
         eta = X.astype(np.float64) @ beta
         y = (rng.random(n) < 1.0 / (1.0 + np.exp(-eta))).astype(np.float32)
-        rows = np.empty((n, F + 1), np.float32)
-        rows[:, :F] = X
-        rows[:, F] = y
-        params = torch.from_numpy(np.concatenate([rows.reshape(-1), [5.0]]).astype(np.float32)).cuda()
+        rws = np.empty((n, F + 1), np.float32)
+        rws[:, :F] = X
+        rws[:, F] = y
+        params = torch.from_numpy(np.concatenate([rws.reshape(-1), [5.0]]).astype(np.float32)).cuda()
+        rows_dev = params[: n * (F + 1)].view(n, F + 1)
         return dict(model=M.logistic_model(F), fast="tensor", forms=("tensor", "gemm", "plain"),
                     params=params, walkers=8192,
                     burn=10, run=20, bins=128, plain_burn=1, plain_run=4, rows=n,
-                    row_len=F + 1, hyper_len=1,
+                    row_len=F + 1, hyper_len=1, plain_rows=(1 << 16) if quick else 0,
                     init=lambda s, seed: s.init_position_normal(seed, 0.0, 0.05),
-                    flop=2 * F * n, bytes=4 * (F + 1) * n // (8192 // 2),
+                    flop=2 * F * n, bytes=4 * (F + 1) * n // (8192 // 2), bound="tensor",
+                    fp64=lambda pos: fp64_logistic(rows_dev, F, 5.0, pos), check=256,
                     desc="Bayesian logistic regression, X 1,048,576 x 64 N(0,1), beta* ~ "
                          "N(0,1/64), prior N(0,5^2 I)")
     if name == "c5":
@@ -239,7 +372,7 @@ def _workload(name, rows=0):
         scale = np.exp(rng.uniform(np.log(0.01), np.log(100.0), F)).astype(np.float32)
         beta = (rng.normal(0.0, 1.0, F) / (scale * 16.0)).astype(np.float32)
         params = torch.empty(n * (F + 1) + 3, dtype=torch.float32, device="cuda")
-        rows = params[: n * (F + 1)].view(n, F + 1)
+        rws = params[: n * (F + 1)].view(n, F + 1)
         g = torch.Generator(device="cuda")
         g.manual_seed(0)
         sc = torch.from_numpy(scale).cuda()
@@ -249,31 +382,53 @@ def _workload(name, rows=0):
             x = torch.randn(r1 - r0, F, device="cuda", generator=g) * sc
             z = torch.randn(r1 - r0, 5, device="cuda", generator=g)
             t4 = z[:, 0] / torch.sqrt((z[:, 1:] ** 2).sum(dim=1) / 4.0)
-            rows[r0:r1, :F] = x
-            rows[r0:r1, F] = x @ bt + 0.5 * t4
-        params[n * (F + 1):] = torch.tensor([4.0, 10.0, 1.0], device="cuda")
+            rws[r0:r1, :F] = x
+            rws[r0:r1, F] = x @ bt + 0.5 * t4
+        hyper = np.array([4.0, 10.0, 1.0], np.float32)
+        params[n * (F + 1):] = torch.from_numpy(hyper).cuda()
         torch.cuda.synchronize()
         return dict(model=M.robust_t_model(F), fast="tensor", forms=("tensor", "gemm", "plain"),
                     params=params, walkers=4096,
-                    burn=2, run=10, bins=128, plain_burn=1, plain_run=10, rows=n,
-                    row_len=F + 1, hyper_len=3, plain_rows=1 << 16,
+                    burn=2, run=10, bins=128, plain_burn=1, plain_run=4 if quick else 10,
+                    rows=n, row_len=F + 1, hyper_len=3, plain_rows=1 << 16,
                     init=lambda s, seed: s.init_position_normal(seed, 0.0, 0.01),
-                    flop=2 * F * n, bytes=4 * (F + 1) * n // (4096 // 2),
+                    flop=2 * F * n, bytes=4 * (F + 1) * n // (4096 // 2), bound="tensor",
+                    fp64=lambda pos: fp64_robust_t(rws, F, hyper, pos), check=64,
                     desc="robust regression, Student-t(4) residuals, X 16,777,216 x 256 with "
                          "column scales log-U[0.01,100], D=257")
     raise ValueError(name)
 
 
-def run_config(args):
+def _roofline(bound, flop, bytes_, t_step, W, peaks):
+    """Roofline entry of a config: algorithmic work per ensemble step over its measured
+    time against the bound's peak (measured HBM or bf16; nominal FP32)."""
+    if bound == "fp32":
+        a = W * flop / t_step / 1e12
+        return {"bound": "fp32", "achieved": a, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+                "frac": a / FP32_PEAK_TFLOPS, "peak_kind": "nominal (152 SMs x 128 FMA lanes x "
+                                                            "2.07 GHz)"}
+    if bound == "tensor":
+        a = W * flop / t_step / 1e12
+        return {"bound": "tensor", "achieved": a, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": a / peaks["bf16_tflops"], "peak_kind": peaks["kind"] + " bf16 (burst)",
+                "note": "algorithmic 2 F N per walker-step; the split form issues 3 bf16 "
+                        "products, so the tensor pipe carries 3 x this",
+                "hbm_gbs_algorithmic": W * bytes_ / t_step / 1e9}
+    a = W * bytes_ / t_step / 1e9
+    return {"bound": "hbm", "achieved": a, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": a / peaks["hbm_gbs"], "peak_kind": peaks["kind"]}
+
+
+def measure_config(name, steps, warmup, rows=0, forms=None, quick=False, factory=None):
+    """Times the workload's fast form (and the plain fp32 form, and for the regressions the
+    fp32 SIMT GEMM form unless quick) on whole jobs, the L2 flushed before each; returns
+    the config's record."""
     import torch
-    import __graft_entry__
-    __graft_entry__.build()
     from bayadera_gb300 import _native
     from bayadera_gb300.engine import GB300BayaderaFactory
-    torch.cuda.set_device(0)
-    wl = _workload(args.config, args.rows)
-    if args.rows:
-        wl["desc"] += " [profiling case: %d rows]" % args.rows
+    wl = _workload(name, rows, quick)
+    if rows:
+        wl["desc"] += " [profiling case: %d rows]" % rows
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     f = GB300BayaderaFactory(device=0, wgs=1024, stream=stream.cuda_stream)
@@ -293,33 +448,33 @@ def run_config(args):
     out = {}
     kinds = {"tensor": dict(form="gemm", tensor=True), "gemm": dict(form="gemm"),
              "tiled": dict(form="tiled"), "plain": dict(form="plain")}
-    forms = wl.get("forms", (wl["fast"], "plain"))
-    if args.forms:
-        forms = tuple(args.forms.split(","))
+    forms = forms or wl.get("forms", (wl["fast"], "plain"))
+    if quick:
+        forms = tuple(x for x in forms if x != "gemm")
+    err = None
     for form in forms:
         sf = f.mcmc_factory(wl["model"], **kinds[form])
         params = wl["params"]
         plain_rows = None
         if form == "plain" and wl.get("plain_rows"):
             # One thread per walker loops over every row, so the plain form's cost is
-            # linear in the rows; it is measured on the first plain_rows rows (at full size
-            # a job would take many minutes, and C5's 4.3e9-float data exceeds the uint32
-            # data length of the reference's model ABI) and scaled to the full row count.
+            # linear in the rows; it is measured on the first plain_rows rows and scaled to
+            # the full row count (at full size a job takes minutes, and C5's 4.3e9-float
+            # data exceeds the uint32 data length of the reference's model ABI).
             plain_rows = wl["plain_rows"]
-            F1 = wl["row_len"]
-            nh = wl["hyper_len"]
-            params = torch.cat([params[: plain_rows * F1], params[-nh:]])
+            params = torch.cat([params[: plain_rows * wl["row_len"]], params[-wl["hyper_len"]:]])
         s = sf.create_sampler(11, W, params)
-        steps = args.steps if form == wl["fast"] else 1
-        B = wl["burn"] if form == wl["fast"] else wl.get("plain_burn", wl["burn"])
-        R = wl["run"] if form == wl["fast"] else wl.get("plain_run", wl["run"])
+        fast = form == wl["fast"]
+        n_steps = steps if fast else 1
+        B = wl["burn"] if fast else wl.get("plain_burn", wl["burn"])
+        R = wl["run"] if fast else wl.get("plain_run", wl["run"])
         cur["B"], cur["R"] = B, R
-        for w in range(args.warmup if form == wl["fast"] else 1):
+        for w in range(warmup if fast else 1):
             job(s, 100 + w)
         torch.cuda.synchronize()
         times = []
         l0 = _native.launch_count()
-        for k in range(steps):
+        for k in range(n_steps):
             with torch.cuda.stream(stream):
                 flush.fill_(k & 0xff)
             e0 = torch.cuda.Event(enable_timing=True)
@@ -330,6 +485,11 @@ def run_config(args):
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
         launches = _native.launch_count() - l0
+        if fast:
+            pos = s.positions().T
+            lf = s.logfn()
+            idx = np.linspace(0, W - 1, min(W, wl["check"])).astype(np.int64)
+            err = _err(lf[idx], wl["fp64"](pos[idx]))
         # bare-move probe: average time per ensemble step
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -340,10 +500,9 @@ def run_config(args):
         e1.synchronize()
         t_step = e0.elapsed_time(e1) / 1e3 / nprobe
         scale = (plain_rows / wl["rows"]) if plain_rows else 1.0
-        out[form] = {"value": W * (B + R) * steps / sum(times) * scale,
-                     "ms_per_job": 1e3 * sum(times) / steps,
-                     "launches": launches, "ms_per_ensemble_step": 1e3 * t_step,
-                     "fp32_tflops_per_step": W * wl["flop"] * scale / t_step / 1e12,
+        out[form] = {"value": W * (B + R) * n_steps / sum(times) * scale,
+                     "ms_per_job": 1e3 * sum(times) / n_steps / scale,
+                     "launches": launches, "ms_per_ensemble_step": 1e3 * t_step / scale,
                      "acceptance_rate": res["acceptance_rate"]}
         if plain_rows is not None:
             out[form]["rows_measured"] = plain_rows
@@ -351,25 +510,50 @@ def run_config(args):
         s.release()
         sf.release()
         del params
-    if wl["fast"] not in out or "plain" not in out:
-        print(json.dumps({"config": wl["desc"], "forms": out}))
-        f.release()
-        return 0
-    fast = out[wl["fast"]]
-    B, R = wl["burn"], wl["run"]
-    line = {"metric": "walker-steps/s", "value": fast["value"], "unit": "walker-steps/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": fast["ms_per_job"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": wl["desc"], "walkers": W, "burn_in": B, "run": R,
-                       "form": wl["fast"], "l2": "flushed between timed jobs"},
-            "forms": dict({k: v for k, v in out.items() if k != "plain"},
-                          plain_fp32=out["plain"],
-                          speedup_vs_plain=fast["value"] / out["plain"]["value"]),
-            "algorithmic": {"flop_per_walker_step": wl["flop"],
-                            "bytes_per_walker_step": wl["bytes"]}}
-    print(json.dumps(line))
     f.release()
+    fast = out[wl["fast"]]
+    rec = {"workload": wl["desc"], "walkers": W, "burn_in": wl["burn"], "run": wl["run"],
+           "form": wl["fast"], "value": fast["value"], "unit": "walker-steps/s",
+           "ms_per_job": fast["ms_per_job"], "gpu_launches": fast["launches"],
+           "acceptance_rate": fast["acceptance_rate"],
+           "roofline": _roofline(wl["bound"], wl["flop"], wl["bytes"],
+                                 fast["ms_per_ensemble_step"] / 1e3, W, measured_peaks()),
+           "logfn_err_vs_fp64": err,
+           "forms": {k: v for k, v in out.items()},
+           "algorithmic": {"flop_per_walker_step": wl["flop"],
+                           "bytes_per_walker_step": wl["bytes"]}}
+    if "plain" in out:
+        rec["plain_fp32"] = out["plain"]["value"]
+        rec["speedup_vs_plain"] = fast["value"] / out["plain"]["value"]
+        if "rows_measured" in out["plain"]:
+            rec["plain_fp32_note"] = ("measured on the first %d rows, scaled to the full row "
+                                      "count (cost linear in the rows)"
+                                      % out["plain"]["rows_measured"])
+    return rec
+
+
+def run_config(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    torch.cuda.set_device(0)
+    forms = tuple(args.forms.split(",")) if args.forms else None
+    with ClockSampler(0) as clocks:
+        rec = measure_config(args.config, args.steps, args.warmup, args.rows, forms)
+    line = {"metric": "walker-steps/s", "value": rec["value"], "unit": "walker-steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": rec["ms_per_job"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": rec["workload"], "walkers": rec["walkers"],
+                       "burn_in": rec["burn_in"], "run": rec["run"], "form": rec["form"],
+                       "l2": "flushed between timed jobs"},
+            "gpu_launches": rec["gpu_launches"], "roofline": rec["roofline"],
+            "logfn_err_vs_fp64": rec["logfn_err_vs_fp64"], "forms": rec["forms"],
+            "clocks": clocks.summary()}
+    for k in ("plain_fp32", "speedup_vs_plain", "plain_fp32_note"):
+        if k in rec:
+            line[k] = rec[k]
+    print(json.dumps(line))
     return 0
 
 
@@ -395,14 +579,14 @@ def c4_members(M, n=512, seed=0):
     return out
 
 
-def run_c4(args):
+def measure_c4(steps, warmup):
+    """The 512-model batch: whole jobs (init, 1,000 burn-in and 2,000 accu steps of every
+    member) timed with the L2 flushed before each, the plain single-model form on a sample
+    of the members; returns the config's record."""
     import torch
-    import __graft_entry__
-    __graft_entry__.build()
     from bayadera_gb300 import _native
     from bayadera_gb300 import models as M
     from bayadera_gb300.engine import GB300BayaderaFactory
-    torch.cuda.set_device(0)
     BURN4, RUN4 = 1000, 2000
     mem = c4_members(M)
     W = np.array([m["walkers"] for m in mem], np.float64)
@@ -421,24 +605,34 @@ def run_c4(args):
         b.burn_in(BURN4, 2.0)
         return b.run_sampler(RUN4, 2.0)
 
-    for w in range(args.warmup):
+    for w in range(warmup):
         job(100 + w)
     torch.cuda.synchronize()
     times = []
     l0 = _native.launch_count()
-    with ClockSampler(0) as clocks:
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xff)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            res = job(k)
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xff)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = job(k)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
     launches = _native.launch_count() - l0
-    # one burn-in step alone: time per ensemble step of the whole batch
+    # FP64 error of the members' log densities after the last job (8 members, 64 walkers)
+    errs = []
+    pos_all, lf_all = b.positions(), b.logfn()
+    for i in np.linspace(0, len(mem) - 1, 8).astype(int):
+        m = mem[i]
+        idx = np.linspace(0, m["walkers"] - 1, 64).astype(np.int64)
+        errs.append(_err(lf_all[i][idx], fp64_hrows(m["params"], m["rows"], pos_all[i][idx])))
+    err = {"max_abs": max(e["max_abs"] for e in errs),
+           "median_abs": float(np.median([e["median_abs"] for e in errs])),
+           "max_rel": max(e["max_rel"] for e in errs), "walkers": sum(e["walkers"] for e in errs),
+           "members": 8}
+    # time per ensemble step of the whole batch
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -449,7 +643,7 @@ def run_c4(args):
     info = b.info()
     b.release()
     fam.release()
-    value = float(np.sum(W)) * (BURN4 + RUN4) * args.steps / sum(times)
+    value = float(np.sum(W)) * (BURN4 + RUN4) * steps / sum(times)
 
     # plain single-model form: a uniform random sample of the members, each its own
     # sampler (one plain kernel per half-step, the reference's structure), run in turn;
@@ -481,36 +675,70 @@ def run_c4(args):
     f.release()
     t_plain_full = t_plain * len(mem) / len(sample)
     plain_value = float(np.sum(W)) * (BURN4 + RUN4) / t_plain_full
-    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     achieved = flop_step / t_step / 1e12
     rates = res["acceptance_rates"]
-    line = {"metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)",
-            "config": {"workload": "512 Gaussian hierarchical models, J log-U[2,128], n_j "
-                                   "log-U[10,1000], walkers {256,512,1024,4096}",
-                       "models": len(mem), "walkers_total": int(np.sum(W)),
-                       "rows_total": int(np.sum(N)), "burn_in": BURN4, "run": RUN4,
-                       "form": "batch (3 launches per half-step over balanced work lists, "
-                               "CUDA-graph chunks)",
-                       "rows_items_per_half_step": info["items"],
-                       "l2": "flushed between timed jobs"},
+    return {"workload": "512 Gaussian hierarchical models, J log-U[2,128], n_j log-U[10,1000], "
+                        "walkers {256,512,1024,4096}",
+            "models": len(mem), "walkers_total": int(np.sum(W)), "rows_total": int(np.sum(N)),
+            "burn_in": BURN4, "run": RUN4,
+            "form": "batch (CUDA-graph chunks over balanced work lists)",
+            "rows_items_per_half_step": info["items"],
+            "value": value, "unit": "walker-steps/s", "ms_per_job": 1e3 * sum(times) / steps,
             "gpu_launches": launches,
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                         "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": FP32_PEAK_TFLOPS,
+                         "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS,
                          "peak_kind": "nominal (152 SMs x 128 FMA lanes x 2.07 GHz)",
                          "ms_per_ensemble_step": 1e3 * t_step,
                          "flop_per_ensemble_step": flop_step},
-            "forms": {"batch": value, "plain_fp32": plain_value,
-                      "speedup_vs_plain": value / plain_value,
-                      "plain_sample": "%d of %d members, %d+%d steps each, time scaled to the "
-                                      "full job" % (len(sample), len(mem), PB, PR)},
-            "clocks": clocks.summary(),
-            "result": {"acceptance_rate_min": float(rates.min()),
-                       "acceptance_rate_max": float(rates.max())}}
+            "logfn_err_vs_fp64": err,
+            "plain_fp32": plain_value, "speedup_vs_plain": value / plain_value,
+            "plain_fp32_note": "%d of %d members, %d+%d steps each, time scaled to the full "
+                               "job" % (len(sample), len(mem), PB, PR),
+            "acceptance_rate_min": float(rates.min()), "acceptance_rate_max": float(rates.max())}
+
+
+def run_c4(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    torch.cuda.set_device(0)
+    with ClockSampler(0) as clocks:
+        rec = measure_c4(args.steps, args.warmup)
+    line = {"metric": "walker-steps/s", "value": rec["value"], "unit": "walker-steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": rec["ms_per_job"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {k: rec[k] for k in ("workload", "models", "walkers_total", "rows_total",
+                                           "burn_in", "run", "form",
+                                           "rows_items_per_half_step")},
+            "gpu_launches": rec["gpu_launches"], "roofline": rec["roofline"],
+            "logfn_err_vs_fp64": rec["logfn_err_vs_fp64"],
+            "forms": {"batch": rec["value"], "plain_fp32": rec["plain_fp32"],
+                      "speedup_vs_plain": rec["speedup_vs_plain"],
+                      "plain_sample": rec["plain_fp32_note"]},
+            "clocks": clocks.summary()}
+    line["config"]["l2"] = "flushed between timed jobs"
     print(json.dumps(line))
     return 0
+
+
+def measure_configs():
+    """The configs object of the default line: the other workloads, each its fast form on
+    whole jobs (one warm-up, one or two timed) beside the plain fp32 form, with the
+    log-density error against FP64 on the config's own data."""
+    import torch
+    out = {}
+    for name, steps in (("c1", 2), ("c3", 1), ("c5", 1)):
+        try:
+            out[name] = measure_config(name, steps, 1, quick=True)
+        except Exception as e:          # a failed config is reported, not fatal
+            out[name] = {"error": repr(e)}
+        torch.cuda.empty_cache()
+    try:
+        out["c4"] = measure_c4(1, 1)
+    except Exception as e:
+        out["c4"] = {"error": repr(e)}
+    return out
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -521,9 +749,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="default line without the configs object (the other workloads)")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
-                    help="c2 (default): the 50-D Gaussian job; c1, c3, c5: the other "
-                         "benchmark workloads, measured GEMM/tiled form vs plain form")
+                    help="c2 (default): the 50-D Gaussian job; c1, c3, c4, c5: the other "
+                         "benchmark workloads, their fast form vs the plain form")
     ap.add_argument("--rows", type=int, default=0,
                     help="with --config c3 or c5: data rows instead of the configuration's "
                          "(a smaller case for profiling); the line then names the row count")
@@ -582,11 +812,12 @@ def main():
 
     def timed_jobs(samp, steps, warmup):
         """Warm-up jobs, then `steps` jobs each timed with CUDA events on the library's
-        stream, the L2 flushed by a 256 MiB write before each (outside the events)."""
+        stream, the L2 flushed by a 256 MiB write before each (outside the events).
+        Returns the throughput, the time and every timed job's result."""
         for w in range(warmup):
             job(samp, seed_base + 10 * w)
         torch.cuda.synchronize()
-        times, results = [], None
+        times, results = [], []
         barrier()
         for k in range(steps):
             with torch.cuda.stream(stream):
@@ -594,10 +825,11 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            results = job(samp, seed_base + 7919 * (k + 1))
+            r = job(samp, seed_base + 7919 * (k + 1))
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
+            results.append(r)
         barrier()
         t_total = max_over_ranks(sum(times), dist, "cuda")
         return replica_throughput(steps, world, t_total), t_total, results
@@ -609,6 +841,10 @@ def main():
     with ClockSampler(local) as clocks:
         value, t_total, results = timed_jobs(samp, args.steps, args.warmup)
     launches = _native.launch_count() - launches0
+    # log-density error of the last job's walkers against FP64 (the AR(1) matrix itself)
+    pos = samp.positions().T
+    idx = np.arange(0, WALKERS, 8)
+    err = _err(samp.logfn()[idx], fp64_mvn(P, pos[idx]))
 
     # the fp32 SIMT GEMM form (64-walker tiles, register-blocked x'Px from shared memory)
     samp_gemm = sfs["gemm"].create_sampler(seed_base, WALKERS, dP)
@@ -633,7 +869,7 @@ def main():
     t_launch = e0.elapsed_time(e1) / 1e3 / (2 * n_probe)
     bytes_launch = (WALKERS // 2) * BYTES_PER_WALKER_STEP
     flop_launch = (WALKERS // 2) * FLOP_PER_WALKER_STEP
-    hbm_peak, peak_kind = measured_peaks()
+    peaks = measured_peaks()
     achieved = bytes_launch / t_launch / 1e9
     traffic = profile_traffic()
 
@@ -652,26 +888,43 @@ def main():
                + hist.bin_ranks.nbytes)
     e2e_value = WALKERS * (BURN + RUN) * world / statistics.median(e2e_times)
 
-    # the job's result: posterior means within 3 MC s.e. of the analytic mean 0
-    res, mean, var, hist = results
+    # the jobs' result: posterior means against the analytic mean 0.  Two standard
+    # errors: acor's sigma of each job, and the spread of the run means over the
+    # independent timed jobs (replicas with their own seeds), which needs no estimate of
+    # the autocorrelation time.
+    acs = [r[0]["autocorrelation"] for r in results if r[0]["autocorrelation"] is not None]
+    res = results[-1][0]
     ac = res["autocorrelation"]
-    within = None
-    within_tmax = None
-    err_sd = None
+    result = {"acceptance_rate": res["acceptance_rate"], "dims": DIM, "jobs": len(results)}
     if ac is not None:
-        within = int(np.sum(np.abs(ac.mean) <= 3 * ac.sigma))
-        # the same test with each dimension's standard error taken at the largest tau of the
-        # run (sigma scales with sqrt(tau)): acor's per-dimension tau from n / tau ~ 6
-        # correlation times is itself low for some dimensions
         tau = np.asarray(ac.tau, np.float64)
-        se_tmax = np.asarray(ac.sigma) * np.sqrt(np.max(tau) / np.maximum(tau, 1e-30))
-        within_tmax = int(np.sum(np.abs(ac.mean) <= 3 * se_tmax))
-        # the run mean's distance from the analytic mean 0, in posterior standard deviations
-        err_sd = float(np.max(np.abs(ac.mean) / np.sqrt(np.diag(sigma))))
+        result["tau_max"] = float(np.max(tau))
+        result["means_within_3se_acor"] = int(np.sum(np.abs(ac.mean) <= 3 * ac.sigma))
+        result["max_abs_mean_over_posterior_sd"] = float(
+            np.max(np.abs(ac.mean) / np.sqrt(np.diag(sigma))))
+    if len(acs) >= 3:
+        m = np.array([a.mean for a in acs])                 # jobs x dims
+        sd = m.std(axis=0, ddof=1)                          # s.e. of one job's mean
+        grand = m.mean(axis=0)
+        result["replica_se"] = {
+            "jobs": len(acs),
+            "job_means_within_3se": float(np.mean(np.abs(m) <= 3 * sd[None, :])),
+            "grand_mean_within_3se_dims": int(np.sum(np.abs(grand) <= 3 * sd / np.sqrt(len(acs)))),
+            "acor_sigma_over_replica_sd_median": float(
+                np.median(np.mean([a.sigma for a in acs], axis=0) / sd))}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_sample(12.0)
+        cpu = cpu_sample(10.0)
+
+    configs = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        samp.release()
+        samp = None
+        for x in sfs.values():
+            x.release()
+        sfs = {}
+        configs = measure_configs()
 
     if rank == 0:
         line = {
@@ -684,24 +937,24 @@ def main():
             "e2e": {"value": e2e_value, "unit": "walker-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                         "peak_kind": peak_kind,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                         "peak_kind": peaks["kind"],
                          "kernel": "bay_tcr_bare (GEMM form on the tensor cores, resident matrix)",
                          "launch_us": t_launch * 1e6,
                          "fp32_tflops": flop_launch / t_launch / 1e12},
             "cpu_baseline": cpu,
             "forms": {"tensor": value, "gemm_fp32_simt": gemm_value, "plain_fp32": plain_value,
                       "speedup_vs_plain": value / plain_value},
+            "logfn_err_vs_fp64": err,
             "clocks": clocks.summary(),
-            "result": {"acceptance_rate": res["acceptance_rate"],
-                       "tau_max": float(np.max(ac.tau)) if ac is not None else None,
-                       "means_within_3se": within,
-                       "means_within_3se_at_tau_max": within_tmax, "dims": DIM,
-                       "max_abs_mean_over_posterior_sd": err_sd},
+            "result": result,
         }
+        if configs is not None:
+            line["configs"] = configs
         print(json.dumps(line))
-    samp.release()
+    if samp is not None:
+        samp.release()
     for x in sfs.values():
         x.release()
     f.release()

@@ -127,7 +127,18 @@ enum bay_model_flags {
      * per product term (fp32 SIMT: 2^-24).  The sampler keeps a bf16 hi + lo copy of A
      * (4 bytes per element).  At most 320 features and 2^31 - 256 rows.  No counterpart
      * in the reference (which evaluates every density per walker in fp32). */
-    BAY_MODEL_GEMM_TENSOR = 1u << 2
+    BAY_MODEL_GEMM_TENSOR = 1u << 2,
+    /* the stretch factor z (nvidia-gtx-mcmc-stretch.cu:71-72) with its 1/a by the
+     * compiler's fast division, the flavour of the reference's -use_fast_math build;
+     * default: IEEE 1/a.  Both keep the operation order that the reference's golden
+     * trajectories pin, and agree at a = 2. */
+    BAY_MODEL_STRETCH_REF = 1u << 3,
+    /* plain and tiled forms: the reference's partner offset (uint)(u0 * K * dim)
+     * (nvidia-gtx-mcmc-stretch.cu:75-81, quirk Q1), an element offset that straddles
+     * walkers for dim > 1.  Elements past the half's end, which the reference reads out
+     * of bounds (or racing with the moving half), read as 0.  Default: partner walker
+     * (uint)(u0 * K), clamped to the half (identical at dim = 1). */
+    BAY_MODEL_PARTNER_ELEMENT = 1u << 4
 };
 
 typedef struct bay_model_desc {
@@ -236,7 +247,15 @@ int bay_sd(bay_sampler* s, double* out);
  * nvidia_gtx.clj:500), BAY_HIST_COMPAT_ZERO_LIMITS (reference min/max reduction folds
  * 0.0 into partial blocks, nvidia-gtx-estimate.cu:91-106).  limits 2 x dim, pdf and
  * ranks bins x dim (host or device memory). */
-enum bay_hist_flags { BAY_HIST_COMPAT_START1 = 1u << 0, BAY_HIST_COMPAT_ZERO_LIMITS = 1u << 1 };
+enum bay_hist_flags {
+    BAY_HIST_COMPAT_START1 = 1u << 0,
+    BAY_HIST_COMPAT_ZERO_LIMITS = 1u << 1,
+    /* the bin from the reference's expression (uint)((x - lo) / (hi - lo) * bins)
+     * (nvidia-gtx-estimate.cu:22) compiled with -use_fast_math, i.e. the compiler's fast
+     * division; default: IEEE division.  The two differ only for values within a few ulp
+     * of a bin edge. */
+    BAY_HIST_COMPAT_FASTDIV = 1u << 2
+};
 int bay_histogram(bay_sampler* s, uint32_t cycles, uint32_t bins, uint32_t flags, float* limits,
                   float* pdf, float* ranks);
 
@@ -253,11 +272,13 @@ int bay_acor(bay_ctx* ctx, const float* series, uint32_t dim, uint64_t n, double
  * loop with a fixed memory budget.  The caller passes the series in device memory
  * (dim x n column-major) and the outputs (device or host memory); the work space is a
  * fixed 8 MiB scratch array compiled into the library, so dim * n + 3 * dim must not
- * exceed 1,048,576 doubles (BAY_ERR_ARG otherwise).  Every GPU that loads the library
- * holds that array until the process exits.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.  All calls
- * share the one array: calls whose kernels overlap on the GPU (other contexts, other
- * streams) race and must be serialised by the caller.  Same results as bay_acor. */
+ * exceed 1,048,576 doubles (BAY_ERR_ARG otherwise).  The array becomes resident on a GPU
+ * when the library's module loads there (with CUDA_MODULE_LOADING=LAZY, at first use)
+ * and stays until the process exits; bay_ctx_create looks its device address up, so a
+ * call itself does no set-up.  A series in device memory of a GPU other than the
+ * context's is refused (BAY_ERR_ARG).  All calls share the one array: calls whose
+ * kernels overlap on the GPU (other contexts, other streams) race and must be
+ * serialised by the caller.  Same results as bay_acor. */
 int bay_acor_noalloc(bay_ctx* ctx, const float* d_series, uint32_t dim, uint64_t n,
                      double* tau, double* mean, double* sigma, uint32_t* lag);
 

@@ -277,11 +277,21 @@ static float m_mvn32(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, con
     (void)pl;
     const float* P = p + dl;
     float acc = 0.0f;
+#ifdef BO_SPEED
+    /* speed build (the timed CPU baseline, not a checker): plain sums that -ffast-math
+     * lets the compiler reassociate and vectorise */
+    for (uint32_t i = 0; i < dim; i++) {
+        float t = 0.0f;
+        for (uint32_t j = 0; j < dim; j++) t += P[i * dim + j] * x[j];
+        acc += x[i] * t;
+    }
+#else
     for (uint32_t i = 0; i < dim; i++) {
         float t = 0.0f;
         for (uint32_t j = 0; j < dim; j++) t = fmaf(P[i * dim + j], x[j], t);
         acc = fmaf(x[i], t, acc);
     }
+#endif
     return -0.5f * acc;
 }
 static double m_mvn64(uint32_t dl, uint32_t pl, const float* p, uint32_t dim, const double* x) {
@@ -512,63 +522,97 @@ void bo_logfn_all(const char* name, uint64_t walkers, uint32_t dim, uint32_t dat
  * nvidia-gtx-mcmc-stretch.cu:35-99 (OpenCL twin amd-gcn-mcmc-stretch.cl:31-81).
  * Philox key {seed, 0xdecafbad}, ctr {k, step, stream, 0xbeeff00d};
  * z = (a - 2 + 1/a) u1^2 + 2(1 - 1/a) u1 + 1/a [Christen 2007], first product fused;
- * partner j = (uint)(u0*K) (walker; the reference's element offset (uint)(u0*K*DIM)
- * with BO_PARTNER_ELEMENT), clamped to the half;
+ * partner j = (uint)(u0*K) (walker), clamped to the half; with BO_PARTNER_ELEMENT the
+ * reference's element offset (uint)(u0*K*DIM) (:75), whose elements past the half's end
+ * (read out of bounds, or racing with the moving half, in the reference) read as 0 here
+ * and in the library's compat kernels;
  * Y_i = S_ji + z (X_ki - S_ji) fused; accept if u2 <= z^(D-1) exp(beta (f(Y) - f(X_k)))
  * (fp32, as the reference), or in log space in FP64 with BO_ACCEPT_LOG64. */
-void bo_stretch_half(const bo_stretch_args* A) {
-    const bo_model* m = find_model(A->model);
-    if (!m) return;
+/* Walker k's draws and proposal: z, u2 and Y (D floats). */
+static void stretch_propose_one(const bo_stretch_args* A, uint32_t k, float* Y, float* z_out,
+                                float* u2_out) {
     const uint32_t K = A->K, D = A->dim;
     const float a = A->a;
     const float inv_a = 1.0f / a;
     const float c1 = (a - 2.0f) + inv_a;
     const float c2 = 2.0f * (1.0f - inv_a);
     const float c3 = inv_a;
+    const uint32_t key[2] = {A->seed, 0xdecafbadu};
+    const uint32_t ctr[4] = {k, A->step, A->stream, 0xbeeff00du};
+    float u[4];
+    philox_u01x4(ctr, key, u);
+    const float z = fmaf(c1 * u[1], u[1], c2 * u[1]) + c3;
+    uint64_t j0;
+    if (A->flags & BO_PARTNER_ELEMENT) {
+        j0 = (uint32_t)(u[0] * (float)K * (float)D);
+    } else {
+        uint32_t j = (uint32_t)(u[0] * (float)K);
+        if (j >= K) j = K - 1;
+        j0 = (uint64_t)j * D;
+    }
+    const uint64_t k0 = (uint64_t)k * D;
+    const uint64_t half_len = (uint64_t)K * D;
+    for (uint32_t i = 0; i < D; i++) {
+        const float s = (j0 + i < half_len) ? A->S[j0 + i] : 0.0f;
+        Y[i] = fmaf(z, A->X[k0 + i] - s, s);
+    }
+    *z_out = z;
+    *u2_out = u[2];
+}
+
+/* Walker k's accept test given its proposal's log density ly; on accept Y and ly replace
+ * the walker's position and log density.  Returns the decision. */
+static int stretch_accept_one(const bo_stretch_args* A, uint32_t k, const float* Y, float z,
+                              float u2, float ly) {
+    const uint32_t D = A->dim;
+    int accepted;
+    if (A->flags & BO_ACCEPT_LOG64) {
+        const double lx = A->logfn_X[k];
+        accepted = isfinite(ly)
+            && (log((double)u2)
+                <= (double)(D - 1) * log((double)z) + (double)A->beta * ((double)ly - lx));
+    } else {
+        const float q = isfinite(ly)
+            ? powf(z, (float)(D - 1)) * expf(A->beta * (ly - A->logfn_X[k])) : 0.0f;
+        accepted = u2 <= q;
+    }
+    if (accepted) {
+        const uint64_t k0 = (uint64_t)k * D;
+        for (uint32_t i = 0; i < D; i++) A->X[k0 + i] = Y[i];
+        A->logfn_X[k] = ly;
+    }
+    if (A->accepted) A->accepted[k] = (uint8_t)accepted;
+    return accepted;
+}
+
+void bo_stretch_half(const bo_stretch_args* A) {
+    const bo_model* m = find_model(A->model);
+    if (!m) return;
+    const uint32_t K = A->K, D = A->dim;
 #pragma omp parallel num_threads(A->threads > 0 ? A->threads : 1)
     {
         float* Y = (float*)malloc(sizeof(float) * (D > 0 ? D : 1));
 #pragma omp for schedule(static)
         for (int64_t kk = 0; kk < (int64_t)K; kk++) {
             const uint32_t k = (uint32_t)kk;
-            const uint32_t key[2] = {A->seed, 0xdecafbadu};
-            const uint32_t ctr[4] = {k, A->step, A->stream, 0xbeeff00du};
-            float u[4];
-            philox_u01x4(ctr, key, u);
-            const float z = fmaf(c1 * u[1], u[1], c2 * u[1]) + c3;
-            uint64_t j0;
-            if (A->flags & BO_PARTNER_ELEMENT) {
-                j0 = (uint32_t)(u[0] * (float)K * (float)D);
-            } else {
-                uint32_t j = (uint32_t)(u[0] * (float)K);
-                if (j >= K) j = K - 1;
-                j0 = (uint64_t)j * D;
-            }
-            const uint64_t k0 = (uint64_t)k * D;
-            for (uint32_t i = 0; i < D; i++) {
-                const float s = A->S[j0 + i];
-                Y[i] = fmaf(z, A->X[k0 + i] - s, s);
-            }
+            float z, u2;
+            stretch_propose_one(A, k, Y, &z, &u2);
             const float ly = m->f32(A->data_len, A->params_len, A->params, D, Y);
-            int accepted;
-            if (A->flags & BO_ACCEPT_LOG64) {
-                const double lx = A->logfn_X[k];
-                accepted = isfinite(ly)
-                    && ((double)logf(u[2])
-                        <= (double)(D - 1) * (double)logf(z) + (double)A->beta * ((double)ly - lx));
-            } else {
-                const float q = isfinite(ly)
-                    ? powf(z, (float)(D - 1)) * expf(A->beta * (ly - A->logfn_X[k])) : 0.0f;
-                accepted = u[2] <= q;
-            }
-            if (accepted) {
-                for (uint32_t i = 0; i < D; i++) A->X[k0 + i] = Y[i];
-                A->logfn_X[k] = ly;
-            }
-            if (A->accepted) A->accepted[k] = (uint8_t)accepted;
+            stretch_accept_one(A, k, Y, z, u2, ly);
         }
         free(Y);
     }
+}
+
+void bo_stretch_propose(const bo_stretch_args* A, float* Y, float* zs, float* u2s) {
+    for (uint32_t k = 0; k < A->K; k++)
+        stretch_propose_one(A, k, Y + (uint64_t)k * A->dim, &zs[k], &u2s[k]);
+}
+
+void bo_stretch_accept(const bo_stretch_args* A, const float* Y, const float* zs,
+                       const float* u2s, const float* ly) {
+    for (uint32_t k = 0; k < A->K; k++)
+        stretch_accept_one(A, k, Y + (uint64_t)k * A->dim, zs[k], u2s[k], ly[k]);
 }
 
 /* ======================= reductions ==================================== */
@@ -628,8 +672,13 @@ float bo_launch_reduce_f32(const float* v, uint64_t n, uint32_t wgs) {
 void bo_accu_stats(uint32_t K, uint32_t dim, uint32_t wgs, uint32_t step, const float* X,
                    const uint8_t* accepted, uint32_t* accept_blocks, float* means_blocks) {
     const uint32_t G = (K + wgs - 1) / wgs;
+    /* blocks are independent: any thread count gives the same sums */
+#pragma omp parallel
+    {
     float* blk = (float*)malloc(sizeof(float) * wgs);
-    for (uint32_t b = 0; b < G; b++) {
+#pragma omp for schedule(static)
+    for (int64_t bb = 0; bb < (int64_t)G; bb++) {
+        const uint32_t b = (uint32_t)bb;
         uint32_t cnt = 0;
         for (uint32_t l = 0; l < wgs; l++) {
             const uint32_t g = b * wgs + l;
@@ -645,6 +694,7 @@ void bo_accu_stats(uint32_t K, uint32_t dim, uint32_t wgs, uint32_t step, const 
         }
     }
     free(blk);
+    }
 }
 
 /* sum_means_vertical (nvidia-gtx-mcmc-stretch.cu:250-260) run through launch-reduce!

@@ -97,6 +97,12 @@ typedef struct {
 
 /* One half-step: stretch_move for k in [0, K) (nvidia-gtx-mcmc-stretch.cu:35-99). */
 void bo_stretch_half(const bo_stretch_args* a);
+/* The same half-step in two parts, for checking a kernel whose model density is evaluated
+ * elsewhere: the proposals Y (K x dim), stretch factors z and accept uniforms u2; then the
+ * accept test given the proposals' log densities ly (K), updating X, logfn_X, accepted. */
+void bo_stretch_propose(const bo_stretch_args* a, float* Y, float* zs, float* u2s);
+void bo_stretch_accept(const bo_stretch_args* a, const float* Y, const float* zs,
+                       const float* u2s, const float* ly);
 
 /* Statistics that stretch_move_accu adds after the move
  * (nvidia-gtx-mcmc-stretch.cu:101-134): with G = ceil(K/wgs) blocks,

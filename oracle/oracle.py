@@ -19,6 +19,12 @@ SRC = os.path.join(HERE, "bay_oracle.c")
 LIB = os.path.join(HERE, "libbay_oracle.so")
 
 CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11"]
+# The same source built for speed, for the timed CPU baseline only (never for parity):
+# optimised, vectorised, fast-math arithmetic, OpenMP.  Portable flags only (the library
+# is built on x86-64 here and on the GPU hosts' Arm cores), so no -march=native.
+LIB_FAST = os.path.join(HERE, "libbay_oracle_fast.so")
+CFLAGS_FAST = ["-O3", "-ffast-math", "-funroll-loops", "-fopenmp", "-fPIC", "-shared",
+               "-std=c11", "-DBO_SPEED"]
 
 PARTNER_ELEMENT = 1
 ACCEPT_LOG64 = 2
@@ -26,19 +32,36 @@ HIST_START1 = 1
 HIST_ZERO_LIMITS = 2
 
 
-def build(force=False):
-    """Compile libbay_oracle.so next to its source with gcc."""
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC),
+def _build_one(lib, flags, force):
+    if (not force and os.path.exists(lib)
+            and os.path.getmtime(lib) >= max(os.path.getmtime(SRC),
                                              os.path.getmtime(os.path.join(HERE, "bay_oracle.h")))):
-        return LIB
-    cmd = ["gcc"] + CFLAGS + [SRC, "-o", LIB + ".tmp", "-lm"]
+        return lib
+    cmd = ["gcc"] + flags + [SRC, "-o", lib + ".tmp", "-lm"]
     subprocess.check_call(cmd)
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    os.replace(lib + ".tmp", lib)
+    return lib
+
+
+def build(force=False):
+    """Compile libbay_oracle.so (the exact build, -ffp-contract=off, for parity) and
+    libbay_oracle_fast.so (the speed build, for the timed CPU baseline) next to the
+    source with gcc."""
+    _build_one(LIB_FAST, CFLAGS_FAST, force)
+    return _build_one(LIB, CFLAGS, force)
 
 
 _lib = None
+_speed = False
+
+
+def use_speed_build(enabled=True):
+    """Route this module's calls to the speed build (for timing the CPU baseline; its
+    fast-math arithmetic is not the oracle's).  Call before the first use."""
+    global _speed, _lib
+    if _lib is not None and _speed != enabled:
+        raise RuntimeError("the oracle library is already loaded")
+    _speed = enabled
 
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -59,7 +82,7 @@ def lib():
     global _lib
     if _lib is None:
         build()
-        L = C.CDLL(LIB)
+        L = C.CDLL(LIB_FAST if _speed else LIB)
         L.bo_philox4x32_10.argtypes = [u32p, u32p, u32p]
         L.bo_u01_oo_32_24.argtypes = [C.c_uint32]
         L.bo_u01_oo_32_24.restype = C.c_float
@@ -79,6 +102,8 @@ def lib():
         L.bo_logfn_all.argtypes = [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                    f32p, f32p, f32p, C.c_int]
         L.bo_stretch_half.argtypes = [C.POINTER(StretchArgs)]
+        L.bo_stretch_propose.argtypes = [C.POINTER(StretchArgs), f32p, f32p, f32p]
+        L.bo_stretch_accept.argtypes = [C.POINTER(StretchArgs), f32p, f32p, f32p, f32p]
         L.bo_accu_stats.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, f32p, u8p,
                                     u32p, f32p]
         L.bo_tree_sum_f32.argtypes = [f32p, C.c_uint32]
@@ -201,18 +226,43 @@ class Stretch:
         self.xs[:] = _f32(xs).ravel()
         self.logfn_all()
 
-    def half(self, which, seed, stream, step, a, beta, accepted=None):
+    def _args(self, which, seed, stream, step, a, beta, accepted=None):
         D, K = self.dim, self.K
         X = self.xs[which * K * D:(which + 1) * K * D]
         S = self.xs[(1 - which) * K * D:(2 - which) * K * D]
         lf = self.logfn[which * K:(which + 1) * K]
         assert X.base is self.xs or X.ctypes.data >= self.xs.ctypes.data
-        args = StretchArgs(K, D, seed & 0xffffffff, stream, step & 0xffffffff, a, beta,
+        return StretchArgs(K, D, seed & 0xffffffff, stream, step & 0xffffffff, a, beta,
                            self.data_len, len(self.params) - self.data_len,
                            self.params.ctypes.data, self.model.encode(), S.ctypes.data,
                            X.ctypes.data, lf.ctypes.data, self.flags,
                            accepted.ctypes.data if accepted is not None else None, self.threads)
-        lib().bo_stretch_half(C.byref(args))
+
+    def half(self, which, seed, stream, step, a, beta, accepted=None):
+        lib().bo_stretch_half(C.byref(self._args(which, seed, stream, step, a, beta, accepted)))
+
+    def half_with_density(self, which, seed, stream, step, a, beta, density):
+        """One half-step whose proposals' log densities come from density(Y) (Y: K x dim
+        float32 -> K float32), e.g. the model compiled for the device, instead of the
+        oracle's own restatement of the model; Philox draws, partner, proposal and the
+        accept test are the oracle's."""
+        D, K = self.dim, self.K
+        args = self._args(which, seed, stream, step, a, beta)
+        Y = np.zeros(K * D, np.float32)
+        zs = np.zeros(K, np.float32)
+        u2 = np.zeros(K, np.float32)
+        lib().bo_stretch_propose(C.byref(args), Y, zs, u2)
+        ly = np.ascontiguousarray(density(Y.reshape(K, D)), np.float32).ravel()
+        assert ly.size == K
+        lib().bo_stretch_accept(C.byref(args), Y, zs, u2, ly)
+
+    def move_bare_with_density(self, density, a=None, beta=None):
+        """move-bare! with the proposals' log densities from density (half_with_density)."""
+        a = self.a if a is None else a
+        beta = self.beta if beta is None else beta
+        self.half_with_density(0, self.seed, 3333, self.bare_counter, a, beta, density)
+        self.half_with_density(1, self.seed + 1, 4444, self.bare_counter, a, beta, density)
+        self.bare_counter += 1
 
     # move-bare! (nvidia_gtx.clj:358-364): odd half (s0) then even half (s1)
     def move_bare(self, a=None, beta=None):

@@ -182,8 +182,9 @@ def extract(ref_root):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    g, series = extract(ref)
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the uncomplicate/bayadera source tree>")
+    g, series = extract(sys.argv[1])
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(g, f, indent=1)
     np.savez_compressed(os.path.join(HERE, "acor_series.npz"), **series)

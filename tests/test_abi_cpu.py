@@ -86,6 +86,22 @@ def test_model_check_benchmark_models(native):
     _check(M.hierarchical_model(4))
 
 
+def test_model_check_reference_compat_flags(native):
+    """The reference-compatibility modules compile: the stretch factor's fast-math
+    expression (every form), the element-offset partner (plain and tiled forms); the
+    element partner is an argument error for the GEMM forms."""
+    from bayadera_gb300 import models as M
+    uni = M.distribution_models()["uniform"]
+    _check(uni, stretch_ref=True)
+    _check(uni, partner_element=True)
+    _check(uni, stretch_ref=True, partner_element=True, accept_ref=True)
+    _check(M.gaussian_posterior_model(), "tiled", partner_element=True, stretch_ref=True)
+    _check(M.mvn_precision_model(50), "gemm", tensor=True, stretch_ref=True)
+    _check(M.hierarchical_rows_batch_model(16), "batch", stretch_ref=True)
+    with pytest.raises(native.IllegalArgument, match="plain and tiled"):
+        _check(M.mvn_precision_model(8), "gemm", partner_element=True)
+
+
 def test_model_check_batch_form(native):
     """The batched engine's kernels (runtime dimension) compile for the hierarchical family;
     a model without a batch form is an argument error."""

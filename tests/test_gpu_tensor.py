@@ -346,6 +346,40 @@ def test_tcr_mvn_logfn_and_moves(factory, M, oracle):
     assert differ <= W // 25, differ
 
 
+def test_tcr_c2_matrix_logfn_error(factory, M, oracle):
+    """The 50-D benchmark's own target: the AR(1) rho = 0.9 precision matrix with scales
+    log-uniform in [0.1, 10] (entries from 0.1 to 929, strong cancellation in x'Px), 4,096
+    walkers after 300 burn-in steps (near the posterior).  The resident tensor-core form's
+    log densities against the oracle's FP64 density: every walker within the split-bf16
+    bound (2^-15 + 4 D 2^-24) sum_r |x_r| sum_c |P_rc x_c| / 2; the measured error, and the
+    fp32 SIMT form's beside it, are printed."""
+    import bench
+    D, W = 50, 4096
+    P, _ = bench.precision_matrix()
+    P64 = P.astype(np.float64)
+    for tensor in (True, False):
+        sf = factory.mcmc_factory(M.mvn_precision_model(D), form="gemm", tensor=tensor)
+        s = sf.create_sampler(13, W, P.reshape(-1))
+        s.init_position_normal(3, 0.0, 1.0)
+        s.burn_in(300, 2.0)
+        pos = s.positions().T.astype(np.float64)
+        lf = s.logfn().astype(np.float64)
+        want = -0.5 * np.einsum("wi,ij,wj->w", pos, P64, pos)
+        mag = 0.5 * np.einsum("wi,ij,wj->w", np.abs(pos), np.abs(P64), np.abs(pos))
+        err = np.abs(lf - want)
+        print("%s form: |logfn - FP64| max %.3g, median %.3g; relative max %.3g; "
+              "bound median %.3g" % ("tensor-core" if tensor else "fp32 SIMT", err.max(),
+                                     np.median(err), (err / np.abs(want)).max(),
+                                     np.median((2.0 ** -15 + 4 * D * 2.0 ** -24) * mag)))
+        if tensor:
+            tol = (2.0 ** -15 + 4 * D * 2.0 ** -24) * mag + 1e-6 * np.abs(want) + 1e-6
+        else:
+            tol = 4 * D * 2.0 ** -24 * mag + 1e-6 * np.abs(want) + 1e-6
+        assert np.all(err <= tol), (err / tol).max()
+        s.release()
+        sf.release()
+
+
 @pytest.mark.parametrize("D", [10, 63, 64, 80])
 def test_tcr_run_sampler_matches_simt(factory, M, D):
     """Resident tensor-core accu path: acceptance rate within 3 binomial s.e. of the SIMT

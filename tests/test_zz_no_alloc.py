@@ -70,3 +70,38 @@ def test_acor_noalloc_rejects_oversize_and_host_input(setup):
     host = np.zeros(2 * 1000, np.float32)
     with pytest.raises(N.IllegalArgument):
         _acor(N, f.ctx, "bay_acor_noalloc", C.c_void_p(host.ctypes.data), 2, 1000)
+
+
+def test_acor_noalloc_first_call_on_a_fresh_context(setup, acor_series):
+    """bay_acor_noalloc as the very first computation of a new context (the scratch
+    array's address was looked up when the context was created), then bay_acor."""
+    N, f, torch = setup
+    from bayadera_gb300.engine import GB300BayaderaFactory
+    m = _series(acor_series)[1]
+    D, n = m.shape
+    host = np.ascontiguousarray(m.T)
+    dev = torch.from_numpy(host.copy()).cuda()
+    torch.cuda.synchronize()
+    g = GB300BayaderaFactory(device=0, wgs=256)
+    try:
+        got = _acor(N, g.ctx, "bay_acor_noalloc", C.c_void_p(dev.data_ptr()), D, n)
+        want = _acor(N, g.ctx, "bay_acor", C.c_void_p(host.ctypes.data), D, n)
+        for a, b in zip(got[:3], want[:3]):
+            np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-15)
+        assert got[3] == want[3]
+    finally:
+        g.release()
+
+
+def test_acor_noalloc_refuses_another_gpus_memory(setup):
+    """A series in device memory of a GPU other than the context's is refused before any
+    launch (the kernel would read another GPU's memory)."""
+    N, f, torch = setup
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs a second GPU")
+    other = torch.zeros(2 * 1000, device="cuda:1")
+    torch.cuda.synchronize(1)
+    with pytest.raises(N.IllegalArgument):
+        _acor(N, f.ctx, "bay_acor_noalloc", C.c_void_p(other.data_ptr()), 2, 1000)
+    with pytest.raises(N.IllegalArgument):
+        _acor(N, f.ctx, "bay_acor", C.c_void_p(other.data_ptr()), 2, 1000)
