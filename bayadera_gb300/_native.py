@@ -64,7 +64,9 @@ class ModelDesc(C.Structure):
                 ("gemm_features", C.c_uint32), ("gemm_coef", C.c_uint32),
                 ("gemm_block", C.c_uint32), ("gemm_ld", C.c_uint32),
                 ("gemm_offset", C.c_uint64), ("gemm_rows", C.c_uint64),
-                ("gemm_aux_col", C.c_uint32), ("gemm_aux_len", C.c_uint32)]
+                ("gemm_aux_col", C.c_uint32), ("gemm_aux_len", C.c_uint32),
+                ("tc_subtiles", C.c_uint32), ("tc_stages", C.c_uint32),
+                ("tc_groups", C.c_uint32)]
 
 
 class SamplerInfo(C.Structure):
@@ -75,6 +77,28 @@ class SamplerInfo(C.Structure):
 class BatchMember(C.Structure):
     _fields_ = [("dim", C.c_uint32), ("seed", C.c_uint32), ("walkers", C.c_uint64),
                 ("params", C.c_void_p), ("n_params", C.c_uint64), ("rows", C.c_uint64)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("walkers_per_cta", C.c_uint32), ("cta_threads", C.c_uint32),
+                ("tc_subtiles", C.c_uint32), ("tc_stages", C.c_uint32),
+                ("tc_groups", C.c_uint32),
+                ("candidates", C.c_uint32), ("from_cache", C.c_uint32),
+                ("us_per_step", C.c_double), ("default_us_per_step", C.c_double)]
+
+
+class BatchShape(C.Structure):
+    _fields_ = [("rows_per_thread", C.c_uint32), ("walkers_per_item", C.c_uint32),
+                ("chunk_floats", C.c_uint32)]
+
+
+class BatchTuneResult(C.Structure):
+    _fields_ = [("shape", BatchShape), ("candidates", C.c_uint32), ("from_cache", C.c_uint32),
+                ("us_per_step", C.c_double), ("default_us_per_step", C.c_double)]
+
+
+class AdaptResult(C.Structure):
+    _fields_ = [("a", C.c_double), ("acc_rate", C.c_double), ("probes", C.c_uint32)]
 
 
 class RunResult(C.Structure):
@@ -110,6 +134,8 @@ _SIGNATURES = {
     "bay_burn_in": (C.c_int, [P, C.c_uint64, C.c_float]),
     "bay_anneal": (C.c_int, [P, P, C.c_uint64, C.c_float]),
     "bay_acc_rate": (C.c_int, [P, C.c_float, C.POINTER(C.c_double)]),
+    "bay_adapt_a": (C.c_int, [P, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                              C.POINTER(AdaptResult)]),
     "bay_run_sampler": (C.c_int, [P, C.c_uint64, C.c_float, C.POINTER(RunResult), P, P, P, P]),
     "bay_sample": (C.c_int, [P, C.c_uint64, P]),
     "bay_mean": (C.c_int, [P, P]),
@@ -133,6 +159,12 @@ _SIGNATURES = {
     "bay_data_histogram": (C.c_int, [P, P, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, P, P,
                                      P]),
     "bay_batch_create": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32, C.POINTER(P)]),
+    "bay_batch_create_shaped": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32,
+                                          C.POINTER(BatchShape), C.POINTER(P)]),
+    "bay_autotune": (C.c_int, [P, C.POINTER(ModelDesc), C.c_uint64, P, C.c_uint64, P,
+                               C.POINTER(TuneResult)]),
+    "bay_batch_autotune": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32,
+                                     C.POINTER(BatchTuneResult)]),
     "bay_batch_release": (C.c_int, [P]),
     "bay_batch_init_position_normal": (C.c_int, [P, P, C.c_float, C.c_float]),
     "bay_batch_init_position_host": (C.c_int, [P, P]),

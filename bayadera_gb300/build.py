@@ -24,7 +24,7 @@ EMBED = [("bay_embedded_rng", "device/bay_rng.cuh"),
          ("bay_embedded_direct", "device/bay_direct.cuh"),
          ("bay_embedded_hist_fastdiv", "device/bay_hist_fastdiv.cuh")]
 SOURCES = ["bay_api.cpp", "bay_kernels.cu"]
-HEADERS = ["bay_kernels.cuh", "bay_batch_api.inc", "bay_engines_api.inc",
+HEADERS = ["bay_kernels.cuh", "bay_batch_api.inc", "bay_engines_api.inc", "bay_tune_api.inc",
            os.path.join("..", "..", "include", "bayadera_gb300.h")]
 
 

@@ -12,6 +12,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <array>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -225,6 +226,7 @@ struct bay_model {
     CUkernel k_tr[6] = {};   // bare, accu, logfn, persistent bare, persistent accu, statistics
     uint32_t tc_g = 0, tc_stages = 0;
     size_t tc_smem = 0;
+    uint32_t tr_g = 1;   // resident tensor-core form: tile groups per CTA of the move kernels
     // batch form: propose / accept in k_gp / k_ga, rows in k_gr, per-step means here
     CUkernel k_bmeans = nullptr;
     uint32_t row_len = 0;
@@ -246,6 +248,17 @@ size_t gemm_smem_bytes(const bay_model* m, uint64_t rows) {
                             kGemmWalkers * dpad + np * auxs);
 }
 
+// Tiled form: the data rows are staged in chunks of kTileChunk floats (BAY_TILE_CHUNK of
+// the kernel), rounded down to whole rows, a multiple of 4; two chunk buffers when the
+// data span more than one chunk, else one buffer of the data's size.
+constexpr uint32_t kTileChunk = 12288;
+size_t tile_smem_bytes(uint32_t row_len, uint64_t data_len) {
+    const uint64_t chunk_rows = (kTileChunk / row_len) & ~3ull;
+    const uint64_t n_rows = data_len / row_len;
+    if (n_rows > chunk_rows) return 2ull * kTileChunk * sizeof(float);
+    return ((n_rows * row_len * sizeof(float)) + 15) & ~15ull;
+}
+
 // Tensor-core rows kernel (bay_gemm_rows_tc_impl): G sub-tiles of 128 walkers per CTA
 // with their bf16 hi + lo coefficient operand resident (G x ceil(F/64) x 32 KB), a ring
 // of S stages of one 128-row x 64-feature hi + lo chunk (32 KB each), two aux buffers,
@@ -254,12 +267,20 @@ size_t gemm_smem_bytes(const bay_model* m, uint64_t rows) {
 constexpr size_t kTcSmemMax = 232448;  // opt-in dynamic shared memory per CTA, sm_100 family
 constexpr uint32_t kTrWalkers = 64;
 constexpr uint32_t kTrGroups = 4;   // tile groups (256 threads each) per persistent CTA      // walkers per CTA of the resident tensor-core form
-bool tc_plan(uint32_t features, uint32_t aux_len, uint32_t* G, uint32_t* S, size_t* smem) {
+// want_g / want_s (0 = free) ask for a shape; false when no shape fits (or the asked one
+// does not).
+bool tc_plan(uint32_t features, uint32_t aux_len, uint32_t* G, uint32_t* S, size_t* smem,
+             uint32_t want_g = 0, uint32_t want_s = 0) {
     const size_t kc = (features + 63) / 64, auxs = aux_len ? aux_len : 1;
     for (uint32_t g = 2; g >= 1; --g) {
+        if (want_g && g != want_g) continue;
         const size_t fixed = (size_t)g * kc * 32768 + 2 * 128 * auxs * sizeof(float) + 1024 + 256;
         if (fixed + 2 * 32768 > kTcSmemMax) continue;
-        const size_t st = std::min<size_t>(6, (kTcSmemMax - fixed) / 32768);
+        size_t st = std::min<size_t>(6, (kTcSmemMax - fixed) / 32768);
+        if (want_s) {
+            if (want_s < 2 || want_s > st) return false;
+            st = want_s;
+        }
         *G = g;
         *S = (uint32_t)st;
         *smem = fixed + st * 32768;
@@ -382,6 +403,7 @@ struct bay_sampler {
     bool graphs = true;
     cudaGraphExec_t g_bare = nullptr, g_accu = nullptr;
     uint64_t g_accu_cap = 0;
+    bay_mix_state* mix = nullptr;   // bay_adapt_a's device state, allocated on first use
 
     uint64_t gemm_base = 0, gemm_rows = 0;  // GEMM form: A's row 0 and row count in params
     uint32_t gemm_np = 0;                   // rows padded to a multiple of 64
@@ -420,6 +442,8 @@ struct bay_sampler {
     bool tc = false;
     bool tcr = false;   // tensor cores, matrix resident (one launch per half-step, or
                         // one persistent cooperative launch per chunk of steps)
+    uint32_t tr_g = 1;          // tcr: tile groups per CTA of the per-launch move kernels
+    size_t smem_move = 0;       // tcr: their dynamic shared memory
     bool persistent = false;    // tcr: the persistent form (when tr_smem != 0); measured
                                 // slower than programmatic dependent launches, so opt-in
     uint32_t tr_grid = 0;       // tcr: CTAs of the persistent form (all co-resident)
@@ -506,7 +530,9 @@ struct bay_sampler {
         return p;
     }
 
-    void launch_half(bool accu, uint32_t half, uint32_t step_off, cudaStream_t st) {
+    // pdl = false launches the resident tensor-core kernels without programmatic
+    // dependent launch (the body of a conditional graph node)
+    void launch_half(bool accu, uint32_t half, uint32_t step_off, cudaStream_t st, bool pdl = true) {
         if (streaming) {
             launch_streaming(accu ? 1 : 0, half, step_off, st);
             return;
@@ -522,16 +548,16 @@ struct bay_sampler {
             at[0].id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
             at[0].value.programmaticStreamSerializationAllowed = 1;
             CUlaunchConfig cfg{};
-            cfg.gridDimX = grid();
+            cfg.gridDimX = (grid() + tr_g - 1) / tr_g;
             cfg.gridDimY = 1;
             cfg.gridDimZ = 1;
-            cfg.blockDimX = 256;
+            cfg.blockDimX = 256 * tr_g;
             cfg.blockDimY = 1;
             cfg.blockDimZ = 1;
-            cfg.sharedMemBytes = (unsigned)smem;
+            cfg.sharedMemBytes = (unsigned)smem_move;
             cfg.hStream = (CUstream)st;
             cfg.attrs = at;
-            cfg.numAttrs = 1;
+            cfg.numAttrs = pdl ? 1 : 0;
             cu_check(g_cu.LaunchKernelEx(&cfg, (CUfunction)model->k_tr[accu ? 1 : 0], args, nullptr),
                      "cuLaunchKernelEx(stretch, tensor cores)");
             return;
@@ -821,6 +847,7 @@ struct Codegen {
     uint32_t cta = 256, wpc = 1;
     uint32_t tc_g = 0, tc_stages = 0;
     size_t tc_smem = 0;
+    uint32_t tr_g = 1;
 };
 
 // Source and NVRTC options of a model's fused kernels (the reference's stretch-options,
@@ -860,7 +887,8 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
         const uint32_t pl = d->prep_len ? d->prep_len : 1u;
         if (pl > 64) fail(BAY_ERR_ARG, "prep_len must be <= 64");
         wpc = d->walkers_per_cta ? d->walkers_per_cta : 8u;
-        if (wpc > 32 || wpc > cta) fail(BAY_ERR_ARG, "walkers_per_cta must be <= 32 and <= cta_threads");
+        if (wpc > 32 || wpc > cta || (wpc & (wpc - 1)))
+            fail(BAY_ERR_ARG, "walkers_per_cta must be a power of two, <= 32 and <= cta_threads");
         opts.push_back("-DBAY_TILED=1");
         opts.push_back("-DBAY_ROW_LEN=" + std::to_string(d->row_len));
         opts.push_back("-DBAY_PREP_LEN=" + std::to_string(pl));
@@ -891,6 +919,14 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
         if (d->flags & BAY_MODEL_GEMM_TENSOR) {
             if (!tc_plan(d->gemm_features, d->gemm_aux_len, &g.tc_g, &g.tc_stages, &g.tc_smem))
                 fail(BAY_ERR_ARG, "tensor-core GEMM form: at most 320 features");
+            if ((d->tc_subtiles || d->tc_stages) &&
+                !tc_plan(d->gemm_features, d->gemm_aux_len, &g.tc_g, &g.tc_stages, &g.tc_smem,
+                         d->tc_subtiles, d->tc_stages))
+                fail(BAY_ERR_ARG, "tensor-core GEMM form: the asked sub-tiles / stages do not fit "
+                                  "in shared memory");
+            if (d->tc_groups > 2) fail(BAY_ERR_ARG, "tc_groups must be 0, 1 or 2");
+            g.tr_g = d->tc_groups ? d->tc_groups : 1u;
+            opts.push_back("-DBAY_TR_G=" + std::to_string(g.tr_g) + "u");
             opts.push_back("-DBAY_GEMM_TC=1");
             opts.push_back("-DBAY_TC_G=" + std::to_string(g.tc_g));
             opts.push_back("-DBAY_TC_STAGES=" + std::to_string(g.tc_stages));
@@ -956,6 +992,7 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
         m->cta = g.cta;
         m->wpc = g.wpc;
         m->flags = d->flags;
+        if (d->form == BAY_FORM_TILED) m->row_len = d->row_len;
         if (d->form == BAY_FORM_GEMM) {
             m->prep_len = d->prep_len ? d->prep_len : 1u;
             m->gemm_features = d->gemm_features;
@@ -968,6 +1005,7 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
             m->tc_g = g.tc_g;
             m->tc_stages = g.tc_stages;
             m->tc_smem = g.tc_smem;
+            m->tr_g = g.tr_g;
         }
         try {
             cu_check(g_cu.LibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr,
@@ -997,6 +1035,13 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                     cu_check(g_cu.LibraryGetKernel(&m->k_evidence, m->lib, "bay_points_evidence"),
                              "GetKernel(evidence)");
                 }
+            }
+            if (d->form == BAY_FORM_TILED) {
+                CUdevice dev = (CUdevice)c->device;
+                for (CUkernel k : {m->k_bare, m->k_accu, m->k_logfn})
+                    cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                     (int)(2 * kTileChunk * sizeof(float)), k, dev),
+                             "cuKernelSetAttribute(smem)");
             }
             if (d->form == BAY_FORM_GEMM) {
                 const char* gp[3] = {"bay_gemm_propose_bare", "bay_gemm_propose_accu",
@@ -1079,6 +1124,7 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
         s->D = m->dim;
         s->n_params = n_params;
         s->data_len = n_params - m->params_size;
+        if (m->form == BAY_FORM_TILED) s->smem = tile_smem_bytes(m->row_len, s->data_len);
         if (m->form == BAY_FORM_GEMM) {
             const uint64_t block = m->gemm_block ? s->data_len : 0;
             const uint64_t block_len = m->gemm_block ? m->params_size : s->data_len;
@@ -1118,6 +1164,8 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                     s->tc = false;
                     s->tcr = true;
                     s->smem = (size_t)(base + greg);
+                    s->tr_g = (base + m->tr_g * greg <= kGemmMaxSmem) ? m->tr_g : 1u;
+                    s->smem_move = (size_t)(base + s->tr_g * greg);
                     s->gemm_np = (uint32_t)np;
                     // persistent form: kTrGroups groups per CTA, their accumulators within
                     // the SM's 512 TMEM columns
@@ -1314,6 +1362,7 @@ int bay_sampler_release(bay_sampler* s) {
         c->release(s->stage);
         c->release(s->hist);
         c->release(s->counts);
+        c->release(s->mix);
         c->release(s->gemm_lay);
         for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
         for (unsigned short* q : {s->tc_xh, s->tc_xl, s->s_bh, s->s_bl}) c->release(q);
@@ -1631,6 +1680,91 @@ int bay_acc_rate(bay_sampler* s, float a, double* rate) {
     });
 }
 
+int bay_adapt_a(bay_sampler* s, uint32_t step, double a, double min_acc, double max_acc,
+                bay_adapt_result* out) {
+    NvtxRange trace_("bay_adapt_a");
+    return guarded([&] {
+        if (!s || !out) fail(BAY_ERR_ARG, "NULL argument");
+        if (!((float)a > 1.0f)) fail(BAY_ERR_ARG, "the stretch parameter a must be > 1");
+        if (!(0.0 <= min_acc && min_acc < max_acc && max_acc <= 1.0))
+            fail(BAY_ERR_ARG, "the acceptance window must satisfy 0 <= min < max <= 1");
+        std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+        bay_ctx* c = s->ctx;
+        c->use();
+        s->require_positions();
+        if (!s->mix) s->mix = (bay_mix_state*)c->alloc(sizeof(bay_mix_state));
+        bay_mix_state h0{};
+        h0.a = a;
+        cuda_check(cudaMemcpyAsync(s->mix, &h0, sizeof(h0), cudaMemcpyHostToDevice, c->stream),
+                   "cudaMemcpy(mix state)");
+        // one graph: a WHILE node whose body is one probe (init-move!, the accu step's two
+        // half-step launches, the loop's rule); mix_end sets the condition, so the loop runs
+        // on the device with no host readback per probe
+        const uint64_t cap = s->means_cap;
+        s->means_cap = 0;  // acc-rate! probes record no per-step means
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ex = nullptr;
+        auto cleanup = [&] {
+            s->means_cap = cap;
+            if (ex) cudaGraphExecDestroy(ex);
+            if (g) cudaGraphDestroy(g);
+        };
+        try {
+            cuda_check(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+            cudaGraphConditionalHandle cond;
+            cuda_check(cudaGraphConditionalHandleCreate(&cond, g, 1u, cudaGraphCondAssignDefault),
+                       "cudaGraphConditionalHandleCreate");
+            cudaGraphNodeParams np{};
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = cond;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t node;
+            cuda_check(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np), "cudaGraphAddNode(while)");
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            cudaStream_t cs = c->capture;
+            cuda_check(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                                     cudaStreamCaptureModeThreadLocal),
+                       "cudaStreamBeginCaptureToGraph");
+            try {
+                cuda_check(bay::launch_mix_begin(s->ctl, s->mix, cs), "mix_begin");
+                s->launch_half(true, 0, 0, cs, false);
+                s->launch_half(true, 1, 0, cs, false);
+                cuda_check(bay::launch_mix_end(s->ctl, s->mix, s->W, step, min_acc, max_acc, cond, cs),
+                           "mix_end");
+            } catch (...) {
+                cudaGraph_t tmp = nullptr;
+                cudaStreamEndCapture(cs, &tmp);
+                throw;
+            }
+            cuda_check(cudaStreamEndCapture(cs, &body), "cudaStreamEndCapture");
+            cuda_check(cudaGraphInstantiate(&ex, g, 0), "cudaGraphInstantiate(adapt)");
+            cuda_check(cudaGraphLaunch(ex, c->stream), "cudaGraphLaunch(adapt)");
+            bay_mix_state h{};
+            cuda_check(cudaMemcpyAsync(&h, s->mix, sizeof(h), cudaMemcpyDeviceToHost, c->stream),
+                       "cudaMemcpy(mix state)");
+            cuda_check(cudaStreamSynchronize(c->stream), "sync");
+            s->check_status();
+            // the host mirror of what the probes did: init-move! per probe, one accu step
+            s->seed_accu += 2u * h.probes;
+            s->step_accu = 1;
+            s->a = (float)h.a;
+            s->iteration_counter += h.probes;
+            bay::count_launches((uint64_t)h.probes * (2u + (s->streaming ? 6u : 2u)));
+            if (h.bad)
+                fail(BAY_ERR_ARG, "the stretch parameter a must be > 1 (the adaptation took a "
+                                  "to " + std::to_string(h.a) + ")");
+            out->a = h.a;
+            out->acc_rate = h.rate;
+            out->probes = h.probes;
+        } catch (...) {
+            cleanup();
+            throw;
+        }
+        cleanup();
+    });
+}
+
 int bay_run_sampler(bay_sampler* s, uint64_t n, float a, bay_run_result* res, double* tau,
                     double* mean, double* sigma, float* means_out) {
     NvtxRange trace_("bay_run_sampler");
@@ -1927,3 +2061,4 @@ int bay_logfn_values(bay_sampler* s, float* out) {
 
 #include "bay_batch_api.inc"
 #include "bay_engines_api.inc"
+#include "bay_tune_api.inc"

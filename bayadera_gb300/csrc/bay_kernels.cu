@@ -47,6 +47,45 @@ __global__ void ctl_apply(bay_ctl* c, bay_ctl_op op) {
     }
 }
 
+// mix!'s a-adaptation probes (mcmc.clj:84-91): init-move! before the probe's accu step,
+// the loop's rule after it.  The rule runs in FP64 with explicit IEEE operations (no fused
+// multiply-add), so a follows the same sequence as the host loop.
+__global__ void mix_begin(bay_ctl* c, const bay_mix_state* st) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    c->seed[1] += 2u;
+    c->step[1] = 0u;
+    c->a = (float)st->a;
+    c->accepted = 0ull;
+    c->ticket[0] = 0u;
+    c->ticket[1] = 0u;
+}
+
+__global__ void mix_end(bay_ctl* c, bay_mix_state* st, unsigned long long W, unsigned int step,
+                        double min_acc, double max_acc, cudaGraphConditionalHandle cont) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    c->step[1] += 1u;                                   // the probe's one accu step
+    const double r = __ddiv_rn((double)c->accepted, (double)W);
+    const double target = __ddiv_rn(__dadd_rn(max_acc, min_acc), 2.0);
+    st->rate = r;
+    st->probes += 1u;
+    unsigned int go = 0u;
+    if (!(step < st->i)) {
+        if (r < min_acc) {
+            st->a = __dadd_rn(1.0, __dmul_rn(__dsub_rn(st->a, 1.0), __ddiv_rn(r, target)));
+            go = 1u;
+        } else if (max_acc < r) {
+            st->a = __dmul_rn(st->a, __ddiv_rn(r, target));
+            go = 1u;
+        }
+        if (go) st->i += 1u;
+        if (go && !((float)st->a > 1.0f)) {
+            st->bad = 1u;
+            go = 0u;
+        }
+    }
+    cudaGraphSetConditional(cont, go);
+}
+
 // init_walkers (nvidia-gtx-mcmc-stretch.cu:158-195): element e = w*D + d (the
 // reference's AoS index) takes word e%4 of Philox(ctr {e/4, 0xf00dcafe, 0xdeadbeef,
 // 0xbeeff00d}, key {seed, 0xdecafaaa}); x = u*hi + (1-u)*lo, first product fused.
@@ -445,6 +484,18 @@ void count_launches(unsigned long long n) { g_launches += n; }
 cudaError_t launch_ctl_apply(bay_ctl* ctl, const bay_ctl_op& op, cudaStream_t s) {
     ctl_apply<<<1, 1, 0, s>>>(ctl, op);
     g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mix_begin(bay_ctl* ctl, bay_mix_state* st, cudaStream_t s) {
+    mix_begin<<<1, 32, 0, s>>>(ctl, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mix_end(bay_ctl* ctl, bay_mix_state* st, unsigned long long W, unsigned int step,
+                           double min_acc, double max_acc, cudaGraphConditionalHandle cont,
+                           cudaStream_t s) {
+    mix_end<<<1, 32, 0, s>>>(ctl, st, W, step, min_acc, max_acc, cont);
     return cudaGetLastError();
 }
 

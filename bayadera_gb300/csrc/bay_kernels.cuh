@@ -77,6 +77,19 @@ struct bay_ctl_op {
     float beta;
 };
 
+// Device state of mix!'s a-adaptation loop (bay_adapt_a): the current a (FP64, as the
+// host loop keeps it), the last acceptance rate, the loop index i of mcmc.clj's loop, the
+// number of acc-rate! probes run, and bad = 1 when the rule took a to 1 or below (the next
+// probe would be refused, as bay_acc_rate refuses it).
+struct bay_mix_state {
+    double a;
+    double rate;
+    unsigned int i;
+    unsigned int probes;
+    unsigned int bad;
+    unsigned int pad;
+};
+
 namespace bay {
 
 cudaError_t launch_ctl_apply(bay_ctl* ctl, const bay_ctl_op& op, cudaStream_t s);
@@ -132,6 +145,14 @@ cudaError_t launch_acor(const float* series, uint32_t D, uint32_t n, uint32_t wg
 // Device address of that scratch on the current device (cudaGetSymbolAddress; loads the
 // library's module on that device if it is not loaded yet).  Allocates nothing.
 cudaError_t acor_noalloc_scratch(double** ptr);
+// One probe of mix!'s loop on the device: mix_begin is init-move! (accu seed + 2, accu
+// step 0, a = (float) st->a, acceptance count 0); after the probe's accu step, mix_end
+// counts the step, computes the rate and applies the loop's rule (mcmc.clj:84-91) in FP64
+// without contraction, then sets the graph's WHILE condition (cont) to go on or stop.
+cudaError_t launch_mix_begin(bay_ctl* ctl, bay_mix_state* st, cudaStream_t s);
+cudaError_t launch_mix_end(bay_ctl* ctl, bay_mix_state* st, unsigned long long W, unsigned int step,
+                           double min_acc, double max_acc, cudaGraphConditionalHandle cont,
+                           cudaStream_t s);
 // Kernels enqueued through this library in this process (graph nodes counted at replay).
 unsigned long long launch_count();
 void count_launches(unsigned long long n);

@@ -1202,6 +1202,26 @@ __device__ __forceinline__ void bay_tmem_ld8(unsigned int ta, float (&v)[8]) {
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// n8 (1..4, warp-uniform) loads of 8 TMEM columns each from ta, ta + 8, ..., then one wait:
+// the loads' latencies overlap.  v[8 q + i] = column ta + 8 q + i of the thread's lane.
+__device__ __forceinline__ void bay_tmem_ld32(unsigned int ta, unsigned int n8, float (&v)[32]) {
+    unsigned int r[32];
+#pragma unroll
+    for (unsigned int q = 0; q < 4u; ++q) {
+        if (q < n8)
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                         : "=r"(r[8 * q]), "=r"(r[8 * q + 1]), "=r"(r[8 * q + 2]), "=r"(r[8 * q + 3]),
+                           "=r"(r[8 * q + 4]), "=r"(r[8 * q + 5]), "=r"(r[8 * q + 6]), "=r"(r[8 * q + 7])
+                         : "r"(ta + 8u * q));
+        else
+#pragma unroll
+            for (int i = 0; i < 8; ++i) r[8 * q + i] = 0u;
+    }
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void bay_mma_n(unsigned int d, unsigned long long a, unsigned long long b,
                                           unsigned int idesc, unsigned int acc) {
     asm volatile(
@@ -1444,18 +1464,21 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     __syncthreads();
     bay_tc_fence_after();
     const unsigned int tmem = sTmem + g * ncols;
-    if (!PERSIST) {
-        // nothing above reads device memory: with a programmatic dependent launch this CTA
-        // may have started before the previous kernel of the stream finished; wait for it
-        // (and its memory) here, then let the next launch start its own set-up
-        asm volatile("griddepcontrol.wait;" ::: "memory");
-        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    }
+    // the matrix image is written once, when the sampler is created, so its copy may start
+    // before this launch's dependency on the previous kernel resolves
     if (threadIdx.x == 0) {
         bay_expect_tx(bar_img, img_bytes);
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
             ::"r"(s_img), "l"(P.gemm_lay), "r"(img_bytes), "r"(bar_img) : "memory");
+    }
+    if (!PERSIST) {
+        // nothing above reads memory another kernel writes: with a programmatic dependent
+        // launch this CTA may have started before the previous kernel of the stream
+        // finished; wait for it (and its memory) here, then let the next launch start its
+        // own set-up
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     }
     unsigned int mma_par = 0u;                  // phase parity of bar_mma's next completion
     const unsigned int nsteps = PERSIST ? m : 1u;
@@ -1638,22 +1661,32 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
         const unsigned int ta = tmem + ((32u * (warp & 3u)) << 16) + c0;
         const float* xw = &Yw[wl * BAY_TR_DPAD];
         float sum = 0.0f, cmp = 0.0f;
-        for (unsigned int j0 = 0; j0 < half_rows; j0 += 8u) {
-            float v[8];
-            bay_tmem_ld8(ta + j0, v);
+        // up to 32 columns per batch of loads (one wait), then per 8 columns: the row terms,
+        // a pairwise sum, a Kahan step (the same order as one 8-column load at a time)
+        for (unsigned int j1 = 0; j1 < half_rows; j1 += 32u) {
+            const unsigned int n8 = (half_rows - j1) >= 32u ? 4u : (half_rows - j1) >> 3;
+            float v32[32];
+            bay_tmem_ld32(ta + j1, n8, v32);
 #pragma unroll
-            for (unsigned int i = 0; i < 8u; ++i) {
-                const unsigned int r = c0 + j0 + i;
-                v[i] = r < rows ? BAY_GEMM_TERM(v[i], &Aux[r * BAY_AUXS], (uint64_t)r, xw, sPrep[g][wl]) : 0.0f;
+            for (unsigned int q = 0; q < 4u; ++q) {
+                if (q >= n8) break;
+                float v[8];
+#pragma unroll
+                for (unsigned int i = 0; i < 8u; ++i) {
+                    const unsigned int r = c0 + j1 + 8u * q + i;
+                    v[i] = r < rows ? BAY_GEMM_TERM(v32[8u * q + i], &Aux[r * BAY_AUXS], (uint64_t)r, xw,
+                                                    sPrep[g][wl])
+                                    : 0.0f;
+                }
+#pragma unroll
+                for (unsigned int s2 = 4u; s2 >= 1u; s2 >>= 1)
+#pragma unroll
+                    for (unsigned int i = 0; i < s2; ++i) v[i] = __fadd_rn(v[i], v[i + s2]);
+                const float yk = __fsub_rn(v[0], cmp);
+                const float t = __fadd_rn(sum, yk);
+                cmp = __fsub_rn(__fsub_rn(t, sum), yk);
+                sum = t;
             }
-#pragma unroll
-            for (unsigned int s2 = 4u; s2 >= 1u; s2 >>= 1)
-#pragma unroll
-                for (unsigned int i = 0; i < s2; ++i) v[i] = __fadd_rn(v[i], v[i + s2]);
-            const float yk = __fsub_rn(v[0], cmp);
-            const float t = __fadd_rn(sum, yk);
-            cmp = __fsub_rn(__fsub_rn(t, sum), yk);
-            sum = t;
         }
         if (h) {                                        // second half of the rows
             sHalf[g][wl][0] = sum;
@@ -1782,11 +1815,17 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     }
 }
 
-extern "C" __global__ void __launch_bounds__(256) bay_tcr_bare(bay_stretch_params P) {
-    bay_stretch_tcr<false, false, false, 1u>(P, 1u);
+// The per-launch move kernels hold BAY_TR_G tile groups per CTA (1 or 2): one matrix-image
+// copy and one TMEM allocation serve BAY_TR_G tiles; group g takes tile g * gridDim.x +
+// blockIdx.x.  Same results for either.
+#ifndef BAY_TR_G
+#define BAY_TR_G 1u
+#endif
+extern "C" __global__ void __launch_bounds__(256 * BAY_TR_G) bay_tcr_bare(bay_stretch_params P) {
+    bay_stretch_tcr<false, false, false, BAY_TR_G>(P, 1u);
 }
-extern "C" __global__ void __launch_bounds__(256) bay_tcr_accu(bay_stretch_params P) {
-    bay_stretch_tcr<true, false, false, 1u>(P, 1u);
+extern "C" __global__ void __launch_bounds__(256 * BAY_TR_G) bay_tcr_accu(bay_stretch_params P) {
+    bay_stretch_tcr<true, false, false, BAY_TR_G>(P, 1u);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_tcr_logfn(bay_stretch_params P) {
     bay_stretch_tcr<false, true, false, 1u>(P, 1u);
@@ -1923,57 +1962,159 @@ bay_points_evidence(unsigned long long n, unsigned int data_len, unsigned int pa
 
 #else
 // ---------------------------------------------------------------- tiled form
-// A CTA owns BAY_WPC walkers; all its threads sweep the data rows, each row read
-// once per CTA and applied to every walker of the tile, with per-thread Kahan sums
-// and a fixed-order (deterministic) CTA reduction.
+// A CTA owns BAY_WPC walkers (a power of two, at most 32) and BAY_CTA threads.  The data
+// rows reach shared memory by TMA bulk copies (cp.async.bulk, completion counted on an
+// mbarrier; the wait is bounded) in chunks of at most BAY_TILE_CHUNK floats, two chunk
+// buffers in flight when the data span more than one.  Thread t works for walker
+// t % BAY_WPC on row group t / BAY_WPC: walkers are fastest across lanes, so the lanes of
+// one row group read the same row (a shared-memory broadcast), and each thread sums its rows
+// in batches of 8 (pairwise) added with a Kahan carry.  The lanes and warps of a walker
+// then combine as compensated pairs in a fixed order (deterministic for a given shape).
 #ifndef BAY_WPC
 #define BAY_WPC 8
 #endif
+#ifndef BAY_TILE_CHUNK
+#define BAY_TILE_CHUNK 12288u                     // floats per staged chunk (48 KB)
+#endif
+#define BAY_TILE_CHUNK_ROWS ((BAY_TILE_CHUNK / BAY_ROW_LEN) & ~3u)   // 16-byte chunk starts
+#define BAY_TILE_WAIT_NS 2000000000ull
 
-__device__ __forceinline__ void bay_tiled_logfn_rows(const bay_stretch_params& P,
-                                                    const float (*prep)[BAY_PREP_LEN],
-                                                    bay_cf (*red)[BAY_WPC], bay_cf* out) {
-    const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
-    float acc[BAY_WPC], cmp[BAY_WPC], pv[BAY_WPC][BAY_PREP_LEN];
-#pragma unroll
-    for (int w = 0; w < BAY_WPC; ++w) {
-        acc[w] = 0.0f;
-        cmp[w] = 0.0f;
-#pragma unroll
-        for (int i = 0; i < BAY_PREP_LEN; ++i) pv[w][i] = prep[w][i];
-    }
-    for (unsigned long long r = threadIdx.x; r < n_rows; r += blockDim.x) {
-        const float* row = P.params + r * BAY_ROW_LEN;
-        float rv[BAY_ROW_LEN];
-#pragma unroll
-        for (int c = 0; c < BAY_ROW_LEN; ++c) rv[c] = __ldg(row + c);
-#pragma unroll
-        for (int w = 0; w < BAY_WPC; ++w) {
-            const float t = BAY_TILE_TERM(rv, pv[w]);
-            // Kahan step (nvcc does not reassociate, so the compensation survives)
-            const float y = __fsub_rn(t, cmp[w]);
-            const float s = __fadd_rn(acc[w], y);
-            cmp[w] = __fsub_rn(__fsub_rn(s, acc[w]), y);
-            acc[w] = s;
+__device__ __forceinline__ unsigned long long bay_tile_timer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for phase `par` of the mbarrier at shared address `bar`: gives up after
+// BAY_TILE_WAIT_NS and sets status bit 1 (the host reports the shared-memory copy).
+__device__ __forceinline__ bool bay_tile_wait(unsigned int bar, unsigned int par,
+                                              unsigned int* status) {
+    unsigned long long t0 = 0;
+    for (unsigned int it = 0;; ++it) {
+        unsigned int ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok) : "r"(bar), "r"(par) : "memory");
+        if (ok) return true;
+        if ((it & 15u) == 0u) {
+            const unsigned long long t = bay_tile_timer();
+            if (it == 0u) {
+                t0 = t;
+            } else if (t - t0 > BAY_TILE_WAIT_NS) {
+                atomicOr(status, 1u);
+                return false;
+            }
         }
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int w = 0; w < BAY_WPC; ++w) {
-        bay_cf v;
-        v.hi = acc[w];
-        v.lo = -cmp[w];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = bay_cadd(v, bay_cf_shfl_xor(v, o));
-        if (lane == 0) red[warp][w] = v;
+}
+
+// Chunk c of the rows -> buffer `buf` (floats): the 16-byte-aligned prefix by one bulk
+// copy completing on `bar`, issued by the calling thread.  Returns the chunk's floats.
+__device__ __forceinline__ unsigned int bay_tile_issue(const bay_stretch_params& P, unsigned long long c,
+                                                       float* buf, unsigned int bar) {
+    const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
+    const unsigned long long r0 = c * BAY_TILE_CHUNK_ROWS;
+    const unsigned long long nr = n_rows - r0 < BAY_TILE_CHUNK_ROWS ? n_rows - r0 : BAY_TILE_CHUNK_ROWS;
+    const unsigned int nf = (unsigned int)(nr * BAY_ROW_LEN);
+    const unsigned int bytes = (nf * 4u) & ~15u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    if (bytes)
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+            ::"r"((unsigned int)__cvta_generic_to_shared(buf)), "l"(P.params + r0 * BAY_ROW_LEN),
+            "r"(bytes), "r"(bar) : "memory");
+    return nf;
+}
+
+// Sum over all data rows of BAY_TILE_TERM(row, prep of walker w) for the CTA's walkers
+// w < BAY_WPC (prep: [BAY_WPC][BAY_PREP_LEN] in shared memory) -> out[w] (compensated
+// pairs).  Every thread of the CTA calls it.  Returns false (and sets the status) when a
+// bounded wait for a copy gave up; out is then incomplete.
+__device__ __forceinline__ bool bay_tiled_logfn_rows(const bay_stretch_params& P,
+                                                    const float (*prep)[BAY_PREP_LEN],
+                                                    bay_cf (*red)[BAY_WPC], bay_cf* out) {
+    extern __shared__ __align__(128) float bay_tsm[];
+    __shared__ __align__(8) unsigned long long sBar[2];
+    __shared__ unsigned int sOk;
+    constexpr unsigned int L = BAY_CTA / BAY_WPC;       // row groups
+    const unsigned int tid = threadIdx.x, w = tid % BAY_WPC, l = tid / BAY_WPC;
+    const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
+    const unsigned long long nch = (n_rows + BAY_TILE_CHUNK_ROWS - 1) / BAY_TILE_CHUNK_ROWS;
+    float* buf[2] = {bay_tsm, bay_tsm + BAY_TILE_CHUNK};
+    const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(&sBar[0]);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sOk = 1u;
     }
     __syncthreads();
-    if (threadIdx.x < BAY_WPC) {
-        bay_cf s = red[0][threadIdx.x];
-        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) s = bay_cadd(s, red[i][threadIdx.x]);
-        out[threadIdx.x] = s;
+    if (tid == 0) {
+        for (unsigned long long c = 0; c < 2 && c < nch; ++c)
+            bay_tile_issue(P, c, buf[c], bar0 + 8u * (unsigned int)c);
+    }
+    float pv[BAY_PREP_LEN];
+#pragma unroll
+    for (int i = 0; i < BAY_PREP_LEN; ++i) pv[i] = prep[w][i];
+    float sum = 0.0f, cmp = 0.0f;
+    for (unsigned long long c = 0; c < nch; ++c) {
+        const unsigned int b = (unsigned int)(c & 1ull);
+        float* R = buf[b];
+        const unsigned long long r0 = c * BAY_TILE_CHUNK_ROWS;
+        const unsigned int nr = (unsigned int)(n_rows - r0 < BAY_TILE_CHUNK_ROWS ? n_rows - r0
+                                                                              : BAY_TILE_CHUNK_ROWS);
+        const unsigned int nf = nr * BAY_ROW_LEN, nb = ((nf * 4u) & ~15u) / 4u;
+        const bool done = bay_tile_wait(bar0 + 8u * b, (unsigned int)((c >> 1) & 1ull), &P.ctl->status);
+        if (!done) sOk = 0u;
+        if (nb < nf) {   // the chunk's last floats past its 16-byte-aligned prefix
+            for (unsigned int e = nb + tid; e < nf; e += BAY_CTA) R[e] = P.params[r0 * BAY_ROW_LEN + e];
+        }
+        __syncthreads();
+        if (sOk == 0u) break;
+        unsigned int r = l;
+        for (; r + 7u * L < nr; r += 8u * L) {
+            float t[8];
+#pragma unroll
+            for (unsigned int i = 0; i < 8u; ++i) t[i] = BAY_TILE_TERM(R + (r + i * L) * BAY_ROW_LEN, pv);
+#pragma unroll
+            for (unsigned int h = 4u; h >= 1u; h >>= 1)
+#pragma unroll
+                for (unsigned int i = 0; i < h; ++i) t[i] = __fadd_rn(t[i], t[i + h]);
+            const float y = __fsub_rn(t[0], cmp);
+            const float s2 = __fadd_rn(sum, y);
+            cmp = __fsub_rn(__fsub_rn(s2, sum), y);
+            sum = s2;
+        }
+        for (; r < nr; r += L) {
+            const float y = __fsub_rn(BAY_TILE_TERM(R + r * BAY_ROW_LEN, pv), cmp);
+            const float s2 = __fadd_rn(sum, y);
+            cmp = __fsub_rn(__fsub_rn(s2, sum), y);
+            sum = s2;
+        }
+        __syncthreads();                                // buffer b is free again
+        if (tid == 0 && c + 2 < nch) bay_tile_issue(P, c + 2, R, bar0 + 8u * b);
+    }
+    const bool ok = sOk != 0u;
+    // the lanes of a walker (lane bits above the walker bits) by an xor butterfly, then
+    // the warps in order
+    bay_cf v;
+    v.hi = sum;
+    v.lo = -cmp;
+#pragma unroll
+    for (unsigned int o = 16u; o >= BAY_WPC && o >= 1u; o >>= 1) v = bay_cadd(v, bay_cf_shfl_xor(v, o));
+    const unsigned int lane = tid & 31u, warp = tid >> 5;
+    if (lane < BAY_WPC) red[warp][lane] = v;
+    __syncthreads();
+    if (tid < BAY_WPC) {
+        bay_cf s = red[0][tid];
+        for (unsigned int i = 1; i < BAY_CTA / 32u; ++i) s = bay_cadd(s, red[i][tid]);
+        out[tid] = s;
     }
     __syncthreads();
+    return ok;
 }
 
 template <bool ACCU>
@@ -2029,19 +2170,21 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
         }
     }
     __syncthreads();
-    bay_tiled_logfn_rows(P, sPrep, sRed, sSum);
+    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum);
     bool accepted = false;
     const unsigned int t = threadIdx.x, k = k0 + t;
     const bool valid = t < BAY_WPC && k < P.K;
     float mine[DIM];
     if (valid) {
-        const float ly = bay_cf_total(sW[t], sSum[t]);
-        const float lx = P.logfn[(size_t)P.half * P.K + k];
-        accepted = bay_accept(sU2[t], sZ[t], ly, lx, beta);
-        if (accepted) {
+        if (ok) {
+            const float ly = bay_cf_total(sW[t], sSum[t]);
+            const float lx = P.logfn[(size_t)P.half * P.K + k];
+            accepted = bay_accept(sU2[t], sZ[t], ly, lx, beta);
+            if (accepted) {
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) X[(size_t)k * DIM + i] = sY[t][i];
-            P.logfn[(size_t)P.half * P.K + k] = ly;
+                for (int i = 0; i < DIM; ++i) X[(size_t)k * DIM + i] = sY[t][i];
+                P.logfn[(size_t)P.half * P.K + k] = ly;
+            }
         }
         if (ACCU) {
 #pragma unroll
@@ -2085,8 +2228,8 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
         }
     }
     __syncthreads();
-    bay_tiled_logfn_rows(P, sPrep, sRed, sSum);
+    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum);
     const unsigned int t = threadIdx.x, k = k0 + t;
-    if (t < BAY_WPC && k < P.W) P.logfn[k] = bay_cf_total(sW[t], sSum[t]);
+    if (ok && t < BAY_WPC && k < P.W) P.logfn[k] = bay_cf_total(sW[t], sSum[t]);
 }
 #endif

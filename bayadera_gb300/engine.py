@@ -91,16 +91,46 @@ class GB300BayaderaFactory:
         N.call("bay_ctx_allocated", self.ctx, C.byref(v))
         return v.value
 
+    def autotune(self, model, walkers, params, form=None, tensor=False, positions=None):
+        """bay_autotune: the fastest kernel shape of the model's form on this workload (the
+        tiled form's walkers per CTA and CTA threads, the streamed tensor-core form's
+        sub-tiles and stages), timed on the device; pass the result's shape keys to
+        mcmc_factory."""
+        d, keep = model_desc(model, form, tensor=tensor)
+        r = N.TuneResult()
+        dp = _dev_ptr(params)
+        if dp is not None:
+            pp, n = dp, int(params.numel())
+        else:
+            p = np.ascontiguousarray(params, np.float32).reshape(-1)
+            keep.append(p)
+            pp, n = _ptr(p), p.size
+        pos = None
+        if positions is not None:
+            pos = np.ascontiguousarray(positions, np.float32)
+        N.call("bay_autotune", self.ctx, C.byref(d), int(walkers), pp, n,
+               _ptr(pos) if pos is not None else None, C.byref(r))
+        shape = {}
+        if r.walkers_per_cta:
+            shape.update(walkers_per_cta=r.walkers_per_cta, cta_threads=r.cta_threads)
+        if r.tc_subtiles:
+            shape.update(tc_subtiles=r.tc_subtiles, tc_stages=r.tc_stages)
+        if r.tc_groups:
+            shape.update(tc_groups=r.tc_groups)
+        return {"shape": shape, "candidates": r.candidates, "from_cache": bool(r.from_cache),
+                "us_per_step": r.us_per_step, "default_us_per_step": r.default_us_per_step}
+
     def mcmc_factory(self, model, form=None, accept_ref=False, walkers_per_cta=0,
                      cta_threads=0, streaming=False, tensor=False, stretch_ref=False,
-                     partner_element=False):
+                     partner_element=False, tc_subtiles=0, tc_stages=0, tc_groups=0):
         """EngineFactory/mcmc-factory: compile the model's fused stretch kernels.  GEMM form:
         streaming=True streams the matrix even when it fits in shared memory; tensor=True
         streams it through the tensor cores (split bf16, fp32 accumulation).  Reference
         compatibility: accept_ref (fp32 accept formula), stretch_ref (the stretch factor's
         fast-math expression), partner_element (the element-offset partner, quirk Q1)."""
         return GB300StretchFactory(self, model, form, accept_ref, walkers_per_cta, cta_threads,
-                                   streaming, tensor, stretch_ref, partner_element)
+                                   streaming, tensor, stretch_ref, partner_element, tc_subtiles,
+                                   tc_stages, tc_groups)
 
     def acor(self, data_matrix):
         return self.acor_engine.acor(data_matrix)
@@ -156,7 +186,8 @@ class GB300BayaderaFactory:
 
 
 def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0,
-               streaming=False, tensor=False, stretch_ref=False, partner_element=False):
+               streaming=False, tensor=False, stretch_ref=False, partner_element=False,
+               tc_subtiles=0, tc_stages=0, tc_groups=0):
     """bay_model_desc of a DeviceDistributionModel; form 'plain' | 'tiled' | None (tiled
     when the model has a tiled form)."""
     if form is None:
@@ -179,6 +210,9 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
                (N.MODEL_STRETCH_REF if stretch_ref else 0) |
                (N.MODEL_PARTNER_ELEMENT if partner_element else 0))
     d.cta_threads = cta_threads
+    d.tc_subtiles = tc_subtiles
+    d.tc_stages = tc_stages
+    d.tc_groups = tc_groups
     if form == "tiled":
         t = model.tiled
         if not t:
@@ -287,21 +321,24 @@ class GB300DensityEngine:
 
 
 def check_model(model, form=None, wgs=1024, accept_ref=False, tensor=False, stretch_ref=False,
-                partner_element=False):
+                partner_element=False, walkers_per_cta=0, cta_threads=0, tc_subtiles=0,
+                tc_stages=0, tc_groups=0):
     """Compile-check a model's fused kernels with NVRTC (no device needed)."""
-    d, keep = model_desc(model, form, accept_ref, tensor=tensor, stretch_ref=stretch_ref,
-                         partner_element=partner_element)
+    d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, tensor=tensor,
+                         stretch_ref=stretch_ref, partner_element=partner_element,
+                         tc_subtiles=tc_subtiles, tc_stages=tc_stages, tc_groups=tc_groups)
     N.call("bay_model_check", C.byref(d), wgs)
 
 
 class GB300StretchFactory:
     def __init__(self, factory, model, form=None, accept_ref=False, walkers_per_cta=0,
                  cta_threads=0, streaming=False, tensor=False, stretch_ref=False,
-                 partner_element=False):
+                 partner_element=False, tc_subtiles=0, tc_stages=0, tc_groups=0):
         self.factory = factory
         self.model = model
         d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, streaming,
-                             tensor, stretch_ref, partner_element)
+                             tensor, stretch_ref, partner_element, tc_subtiles, tc_stages,
+                             tc_groups)
         h = C.c_void_p()
         N.call("bay_model_compile", factory.ctx, C.byref(d), C.byref(h))
         self.handle = h
@@ -316,34 +353,58 @@ class GB300StretchFactory:
         CUDA tensor that stays resident and must outlive the sampler)."""
         return GB300Stretch(self, seed, walkers, params)
 
-    def create_batch(self, members):
+    def create_batch(self, members, shape=None):
         """A batch of independent models of this (batch-form) family; members is a list of
-        dicts {dim, seed, walkers, params (numpy float32: rows || hyperparameters), rows}."""
-        return GB300Batch(self, members)
+        dicts {dim, seed, walkers, params (numpy float32: rows || hyperparameters), rows};
+        shape: the work lists' {rows_per_thread, walkers_per_item, chunk_floats} (e.g. from
+        autotune_batch), None = the library's."""
+        return GB300Batch(self, members, shape)
+
+    def autotune_batch(self, members):
+        """bay_batch_autotune: the fastest work-list shape for these members."""
+        arr, keep = _batch_members(members)
+        r = N.BatchTuneResult()
+        N.call("bay_batch_autotune", self.handle, arr, len(members), C.byref(r))
+        return {"shape": {"rows_per_thread": r.shape.rows_per_thread,
+                          "walkers_per_item": r.shape.walkers_per_item,
+                          "chunk_floats": r.shape.chunk_floats},
+                "candidates": r.candidates, "from_cache": bool(r.from_cache),
+                "us_per_step": r.us_per_step, "default_us_per_step": r.default_us_per_step}
+
+
+def _batch_members(members):
+    arr = (N.BatchMember * len(members))()
+    keep = []
+    for i, m in enumerate(members):
+        p = np.ascontiguousarray(m["params"], np.float32)
+        keep.append(p)
+        arr[i].dim = int(m["dim"])
+        arr[i].seed = int(m["seed"]) & 0xffffffff
+        arr[i].walkers = int(m["walkers"])
+        arr[i].params = p.ctypes.data
+        arr[i].n_params = p.size
+        arr[i].rows = int(m["rows"])
+    return arr, keep
 
 
 class GB300Batch:
     """Many independent models of one family advanced together (bay_batch_*): member m
     behaves as GB300Stretch(seed_m, walkers_m, params_m) of dimension dim_m."""
 
-    def __init__(self, sfactory, members):
+    def __init__(self, sfactory, members, shape=None):
         self.sfactory = sfactory
         self.members = [dict(m) for m in members]
-        arr = (N.BatchMember * len(members))()
-        self._keep = []
-        for i, m in enumerate(self.members):
-            p = np.ascontiguousarray(m["params"], np.float32)
-            self._keep.append(p)
-            arr[i].dim = int(m["dim"])
-            arr[i].seed = int(m["seed"]) & 0xffffffff
-            arr[i].walkers = int(m["walkers"])
-            arr[i].params = p.ctypes.data
-            arr[i].n_params = p.size
-            arr[i].rows = int(m["rows"])
+        arr, keep = _batch_members(self.members)
         h = C.c_void_p()
-        N.call("bay_batch_create", sfactory.handle, arr, len(members), C.byref(h))
+        if shape:
+            sh = N.BatchShape(int(shape.get("rows_per_thread", 0)),
+                              int(shape.get("walkers_per_item", 0)),
+                              int(shape.get("chunk_floats", 0)))
+            N.call("bay_batch_create_shaped", sfactory.handle, arr, len(members), C.byref(sh),
+                   C.byref(h))
+        else:
+            N.call("bay_batch_create", sfactory.handle, arr, len(members), C.byref(h))
         self.handle = h
-        self._keep = None
         self.dims = np.array([m["dim"] for m in self.members], np.int64)
         self.walkers = np.array([m["walkers"] for m in self.members], np.int64)
 
@@ -507,6 +568,14 @@ class GB300Stretch:
         r = C.c_double()
         N.call("bay_acc_rate", self.handle, float(a), C.byref(r))
         return r.value
+
+    def adapt_a(self, step, a, min_acc, max_acc):
+        """mix!'s a-adaptation loop (mcmc.clj:84-91) on the device (bay_adapt_a): returns
+        {a, acc_rate (the last probe's), probes}."""
+        r = N.AdaptResult()
+        N.call("bay_adapt_a", self.handle, int(step), float(a), float(min_acc), float(max_acc),
+               C.byref(r))
+        return {"a": r.a, "acc_rate": r.acc_rate, "probes": r.probes}
 
     def run_sampler(self, n, a, return_means=False):
         res = N.RunResult()

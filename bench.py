@@ -41,7 +41,7 @@ FLOP_PER_WALKER_STEP = 2 * DIM * DIM      # dense -x'Px/2
 L2_FLUSH_BYTES = 256 << 20
 LOG_SQRT_2PI = 0.5 * math.log(2.0 * math.pi)
 # the reference arm and cpu_baseline: the whole 50-D job on this many of its walkers
-CPU_WALKERS = 16384
+CPU_WALKERS = 8192
 
 
 def precision_matrix(dim=DIM, seed=SEED):
@@ -284,7 +284,7 @@ def replica_throughput(jobs, world, t_total):
 def run_reference(args):
     """The reference arm: each step is one whole 50-D job on CPU_WALKERS walkers on the
     host cores (the job's per-walker work does not depend on the walker count; the full
-    65,536-walker job would take about 4 x as long per step)."""
+    65,536-walker job would take about 8 x as long per step)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -452,8 +452,11 @@ def measure_config(name, steps, warmup, rows=0, forms=None, quick=False, factory
     if quick:
         forms = tuple(x for x in forms if x != "gemm")
     err = None
+    # the fast form's kernel shape, chosen by the library's autotuner on this workload
+    tune = f.autotune(wl["model"], W, wl["params"], **kinds[wl["fast"]])
     for form in forms:
-        sf = f.mcmc_factory(wl["model"], **kinds[form])
+        shape = tune["shape"] if form == wl["fast"] else {}
+        sf = f.mcmc_factory(wl["model"], **kinds[form], **shape)
         params = wl["params"]
         plain_rows = None
         if form == "plain" and wl.get("plain_rows"):
@@ -519,6 +522,7 @@ def measure_config(name, steps, warmup, rows=0, forms=None, quick=False, factory
            "roofline": _roofline(wl["bound"], wl["flop"], wl["bytes"],
                                  fast["ms_per_ensemble_step"] / 1e3, W, measured_peaks()),
            "logfn_err_vs_fp64": err,
+           "autotune": tune,
            "forms": {k: v for k, v in out.items()},
            "algorithmic": {"flop_per_walker_step": wl["flop"],
                            "bytes_per_walker_step": wl["bytes"]}}
@@ -549,7 +553,7 @@ def run_config(args):
                        "l2": "flushed between timed jobs"},
             "gpu_launches": rec["gpu_launches"], "roofline": rec["roofline"],
             "logfn_err_vs_fp64": rec["logfn_err_vs_fp64"], "forms": rec["forms"],
-            "clocks": clocks.summary()}
+            "autotune": rec["autotune"], "clocks": clocks.summary()}
     for k in ("plain_fp32", "speedup_vs_plain", "plain_fp32_note"):
         if k in rec:
             line[k] = rec[k]
@@ -597,7 +601,8 @@ def measure_c4(steps, warmup):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     f = GB300BayaderaFactory(device=0, wgs=1024, stream=stream.cuda_stream)
     fam = f.mcmc_factory(M.hierarchical_rows_batch_model(128), form="batch")
-    b = fam.create_batch(mem)
+    tune = fam.autotune_batch(mem)          # the work lists' shape, by timing (untimed here)
+    b = fam.create_batch(mem, tune["shape"])
     seeds = [7 + i for i in range(len(mem))]
 
     def job(k):
@@ -690,7 +695,7 @@ def measure_c4(steps, warmup):
                          "peak_kind": "nominal (152 SMs x 128 FMA lanes x 2.07 GHz)",
                          "ms_per_ensemble_step": 1e3 * t_step,
                          "flop_per_ensemble_step": flop_step},
-            "logfn_err_vs_fp64": err,
+            "logfn_err_vs_fp64": err, "autotune": tune,
             "plain_fp32": plain_value, "speedup_vs_plain": value / plain_value,
             "plain_fp32_note": "%d of %d members, %d+%d steps each, time scaled to the full "
                                "job" % (len(sample), len(mem), PB, PR),
@@ -712,7 +717,7 @@ def run_c4(args):
                                            "burn_in", "run", "form",
                                            "rows_items_per_half_step")},
             "gpu_launches": rec["gpu_launches"], "roofline": rec["roofline"],
-            "logfn_err_vs_fp64": rec["logfn_err_vs_fp64"],
+            "logfn_err_vs_fp64": rec["logfn_err_vs_fp64"], "autotune": rec["autotune"],
             "forms": {"batch": rec["value"], "plain_fp32": rec["plain_fp32"],
                       "speedup_vs_plain": rec["speedup_vs_plain"],
                       "plain_sample": rec["plain_fp32_note"]},
@@ -790,7 +795,10 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     f = GB300BayaderaFactory(device=local, wgs=1024, stream=stream.cuda_stream)
     model = M.mvn_precision_model(DIM)
-    sfs = {"tensor": f.mcmc_factory(model, form="gemm", tensor=True),
+    # the resident tensor-core kernels' shape (tile groups per CTA), chosen by the library's
+    # autotuner on this workload before anything is timed
+    tune = f.autotune(model, WALKERS, dP, form="gemm", tensor=True)
+    sfs = {"tensor": f.mcmc_factory(model, form="gemm", tensor=True, **tune["shape"]),
            "gemm": f.mcmc_factory(model, form="gemm"),
            "plain": f.mcmc_factory(model, form="plain")}
     seed_base = 1000 * (rank + 1)
@@ -911,7 +919,7 @@ def main():
             "job_means_within_3se": float(np.mean(np.abs(m) <= 3 * sd[None, :])),
             "grand_mean_within_3se_dims": int(np.sum(np.abs(grand) <= 3 * sd / np.sqrt(len(acs)))),
             "acor_sigma_over_replica_sd_median": float(
-                np.median(np.mean([a.sigma for a in acs], axis=0) / sd))}
+                np.nanmedian(np.nanmean([a.sigma for a in acs], axis=0) / sd))}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -947,6 +955,7 @@ def main():
             "forms": {"tensor": value, "gemm_fp32_simt": gemm_value, "plain_fp32": plain_value,
                       "speedup_vs_plain": value / plain_value},
             "logfn_err_vs_fp64": err,
+            "autotune": tune,
             "clocks": clocks.summary(),
             "result": result,
         }

@@ -164,6 +164,14 @@ typedef struct bay_model_desc {
     uint64_t gemm_rows;       /* rows of A; 0 = (block length - offset) / ld */
     uint32_t gemm_aux_col;    /* column of the row's auxiliary values */
     uint32_t gemm_aux_len;    /* auxiliary values per row (0..8) */
+    /* BAY_MODEL_GEMM_TENSOR, streamed: 128-walker sub-tiles per CTA (1 or 2) and shared-
+     * memory ring stages (2..6); 0 = library choice (bay_autotune picks them). */
+    uint32_t tc_subtiles;
+    uint32_t tc_stages;
+    /* BAY_MODEL_GEMM_TENSOR with the matrix resident: 64-walker tile groups per CTA of the
+     * move kernels (1 or 2: one matrix copy and one tensor-memory allocation per group or
+     * per pair); 0 = library choice (bay_autotune picks it). */
+    uint32_t tc_groups;
 } bay_model_desc;
 
 int bay_model_compile(bay_ctx* ctx, const bay_model_desc* desc, bay_model** out);
@@ -213,6 +221,23 @@ int bay_burn_in(bay_sampler* s, uint64_t steps, float a);
 int bay_anneal(bay_sampler* s, const float* temperatures, uint64_t steps, float a);
 /* MCMC/acc-rate! (nvidia_gtx.clj:466-478): one accu step; accepted / walkers. */
 int bay_acc_rate(bay_sampler* s, float a, double* rate);
+
+/* The a-adaptation loop of mix! (mcmc.clj:84-91) on the device.  Starting from a, each
+ * probe is acc-rate! (init-move! and one accu step, as bay_acc_rate); after probe i the
+ * loop stops if step < i, else moves a toward the acceptance window -- below min_acc
+ * a = 1 + (a - 1) r / t, above max_acc a = a r / t, t = (min_acc + max_acc) / 2, in FP64 --
+ * and stops once r lies inside it.  The whole loop is one CUDA graph whose conditional
+ * WHILE node runs the probes, the rule deciding on the device: no host readback per probe.
+ * Results: the final a, the last probe's acceptance rate and the number of probes (at most
+ * step + 2); the sampler is left as the same sequence of bay_acc_rate calls leaves it.
+ * No reference counterpart as an engine call (the reference runs this loop on the host). */
+typedef struct bay_adapt_result {
+    double a;
+    double acc_rate;
+    uint32_t probes;
+} bay_adapt_result;
+int bay_adapt_a(bay_sampler* s, uint32_t step, double a, double min_acc, double max_acc,
+                bay_adapt_result* out);
 
 /* MCMC/run-sampler! (nvidia_gtx.clj:441-465): n accu steps with fresh accu seeds
  * (+2 per call), then acor of the per-step ensemble means.  Results:
@@ -364,6 +389,19 @@ typedef struct bay_batch_member {
 
 int bay_batch_create(bay_model* model, const bay_batch_member* members, uint32_t n,
                      bay_batch** out);
+/* The same with the shape of the row-term work lists (0 in a field = library choice):
+ * rows_per_thread sets a work item's row chunk (about 256 x rows_per_thread / walkers
+ * rows), walkers_per_item caps the walkers of one item (a power of two <= 64; fewer when a
+ * member's dimension or walker count asks for it), chunk_floats caps the staged floats of
+ * a chunk (64..4096).  Results agree with any shape up to the order of the row sums.
+ * bay_batch_autotune picks a shape by timing. */
+typedef struct bay_batch_shape {
+    uint32_t rows_per_thread;   /* default 128 */
+    uint32_t walkers_per_item;  /* default 64 */
+    uint32_t chunk_floats;      /* default 4096 */
+} bay_batch_shape;
+int bay_batch_create_shaped(bay_model* model, const bay_batch_member* members, uint32_t n,
+                            const bay_batch_shape* shape, bay_batch** out);
 int bay_batch_release(bay_batch* b);
 /* Walkers of member m ~ N(mean, sd^2) i.i.d. with seeds[m] (bay_init_position_normal). */
 int bay_batch_init_position_normal(bay_batch* b, const uint32_t* seeds, float mean, float sd);
@@ -380,6 +418,45 @@ int bay_batch_state_export(bay_batch* b, float* positions, float* logfn);
 /* total walkers, total positions (floats), rows work items of a move half-step */
 int bay_batch_info(bay_batch* b, uint64_t* walkers, uint64_t* floats, uint64_t* items);
 int bay_batch_set_graphs(bay_batch* b, int enabled);
+
+/* ---------------------------------------------------------------- autotuner
+ * Kernel shapes chosen by timing (no reference counterpart: the reference fixes its work-
+ * group size at max-block-dim-x, nvidia_gtx.clj:803-807).  bay_autotune times the
+ * candidate shapes of a model description on a workload -- walkers, params (host or
+ * device) and optional starting positions (dim x walkers; NULL = N(0, I)) -- over bare
+ * steps with CUDA events, and returns the fastest: for BAY_FORM_TILED walkers_per_cta and
+ * cta_threads, for the BAY_MODEL_GEMM_TENSOR form tc_subtiles and tc_stages (streamed) or
+ * tc_groups (matrix resident) -- set them in the bay_model_desc to compile the chosen
+ * shape.  Other forms have nothing to
+ * tune (the defaults come back, candidates 0).  Results are cached per (model, walkers,
+ * params size, device) for the life of the process (from_cache 1).  Shapes change only the
+ * order of the log-density sums. */
+typedef struct bay_tune_result {
+    uint32_t walkers_per_cta;     /* BAY_FORM_TILED */
+    uint32_t cta_threads;         /* BAY_FORM_TILED */
+    uint32_t tc_subtiles;         /* streamed tensor-core GEMM form */
+    uint32_t tc_stages;           /* streamed tensor-core GEMM form */
+    uint32_t tc_groups;           /* tensor-core GEMM form, matrix resident */
+    uint32_t candidates;          /* shapes timed */
+    uint32_t from_cache;
+    double us_per_step;           /* the chosen shape: microseconds per ensemble step */
+    double default_us_per_step;   /* the library's default shape */
+} bay_tune_result;
+int bay_autotune(bay_ctx* ctx, const bay_model_desc* desc, uint64_t walkers, const float* params,
+                 uint64_t n_params, const float* positions, bay_tune_result* out);
+
+/* The batched engine's work-list shape (bay_batch_shape) by timing whole-batch bare steps
+ * of the members (walkers N(0, I) with the members' seeds); cached per (model, members'
+ * sizes, device). */
+typedef struct bay_batch_tune_result {
+    bay_batch_shape shape;
+    uint32_t candidates;
+    uint32_t from_cache;
+    double us_per_step;
+    double default_us_per_step;
+} bay_batch_tune_result;
+int bay_batch_autotune(bay_model* model, const bay_batch_member* members, uint32_t n,
+                       bay_batch_tune_result* out);
 
 #ifdef __cplusplus
 }

@@ -151,3 +151,26 @@ def test_model_check_rejects_bad_names(native):
                                     logpdf="gaussian_logpdf; int x")
     with pytest.raises(native.IllegalArgument):
         _check(m)
+
+
+def test_model_check_autotuner_shapes(native):
+    """Every shape the autotuner times compiles: the tiled form's (walkers per CTA, CTA
+    threads) pairs, the streamed tensor-core form's sub-tiles and stages, the resident
+    form's tile groups; shapes outside the kernels' limits are argument errors."""
+    from bayadera_gb300 import models as M
+    post = M.gaussian_posterior_model()
+    for wpc, cta in ((8, 256), (4, 128), (8, 128), (16, 256), (32, 256), (8, 512), (16, 512),
+                     (32, 512), (32, 1024)):
+        _check(post, "tiled", walkers_per_cta=wpc, cta_threads=cta)
+    for bad in ((3, 256), (64, 256), (32, 16)):
+        with pytest.raises(native.IllegalArgument):
+            _check(post, "tiled", walkers_per_cta=bad[0], cta_threads=bad[1])
+    lg = M.logistic_model(64)
+    for g, st in ((2, 2), (2, 3), (2, 4), (1, 2), (1, 6)):
+        _check(lg, "gemm", tensor=True, tc_subtiles=g, tc_stages=st)
+    with pytest.raises(native.IllegalArgument, match="do not fit"):
+        _check(M.logistic_model(320), "gemm", tensor=True, tc_subtiles=2, tc_stages=6)
+    for g in (1, 2):
+        _check(M.mvn_precision_model(50), "gemm", tensor=True, tc_groups=g)
+    with pytest.raises(native.IllegalArgument, match="tc_groups"):
+        _check(M.mvn_precision_model(50), "gemm", tensor=True, tc_groups=3)
