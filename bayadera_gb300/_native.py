@@ -89,7 +89,7 @@ class TuneResult(C.Structure):
 
 class BatchShape(C.Structure):
     _fields_ = [("rows_per_thread", C.c_uint32), ("walkers_per_item", C.c_uint32),
-                ("chunk_floats", C.c_uint32)]
+                ("chunk_floats", C.c_uint32), ("walkers_per_thread", C.c_uint32)]
 
 
 class BatchTuneResult(C.Structure):

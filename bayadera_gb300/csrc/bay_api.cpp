@@ -218,6 +218,7 @@ struct bay_model {
     // GEMM form, streaming kernels: propose / accept [bare, accu, logfn], rows [move, logfn]
     CUkernel k_gp[3] = {nullptr, nullptr, nullptr};
     CUkernel k_gr[2] = {nullptr, nullptr};
+    CUkernel k_gr_wpt[3][2] = {};   // batch form rows kernels with 1, 2, 4 walkers per thread
     CUkernel k_ga[3] = {nullptr, nullptr, nullptr};
     // GEMM form on the tensor cores: rows kernels [move, logfn], walker sub-tiles per CTA,
     // shared-memory stages, dynamic shared memory
@@ -540,26 +541,28 @@ struct bay_sampler {
         if (st == ctx->stream) bay::count_launches(1);
         bay_stretch_params p = make_params(half, step_off);
         void* args[] = {&p};
-        if (tcr) {
-            // programmatic dependent launch: the kernel sets up its barriers and tensor memory,
-            // then waits (griddepcontrol.wait) for the previous kernel of the stream to
-            // complete before it reads anything, so its set-up overlaps that kernel's tail
+        if (tcr || model->form == BAY_FORM_TILED) {
+            // programmatic dependent launch: the kernel sets up its barriers (tensor memory,
+            // data copies) and reads what the previous kernel of the stream does not write,
+            // then waits (griddepcontrol.wait) for that kernel to complete, so all this
+            // overlaps its tail
             CUlaunchAttribute at[1];
             at[0].id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
             at[0].value.programmaticStreamSerializationAllowed = 1;
             CUlaunchConfig cfg{};
-            cfg.gridDimX = (grid() + tr_g - 1) / tr_g;
+            cfg.gridDimX = tcr ? (grid() + tr_g - 1) / tr_g : grid();
             cfg.gridDimY = 1;
             cfg.gridDimZ = 1;
-            cfg.blockDimX = 256 * tr_g;
+            cfg.blockDimX = tcr ? 256 * tr_g : model->cta;
             cfg.blockDimY = 1;
             cfg.blockDimZ = 1;
-            cfg.sharedMemBytes = (unsigned)smem_move;
+            cfg.sharedMemBytes = (unsigned)(tcr ? smem_move : smem);
             cfg.hStream = (CUstream)st;
             cfg.attrs = at;
             cfg.numAttrs = pdl ? 1 : 0;
-            cu_check(g_cu.LaunchKernelEx(&cfg, (CUfunction)model->k_tr[accu ? 1 : 0], args, nullptr),
-                     "cuLaunchKernelEx(stretch, tensor cores)");
+            CUkernel k = tcr ? model->k_tr[accu ? 1 : 0] : (accu ? model->k_accu : model->k_bare);
+            cu_check(g_cu.LaunchKernelEx(&cfg, (CUfunction)k, args, nullptr),
+                     tcr ? "cuLaunchKernelEx(stretch, tensor cores)" : "cuLaunchKernelEx(stretch, tiled)");
             return;
         }
         CUkernel k = accu ? model->k_accu : model->k_bare;
@@ -1022,6 +1025,13 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                 }
                 cu_check(g_cu.LibraryGetKernel(&m->k_gr[0], m->lib, "bay_batch_rows_move"), "GetKernel(rows)");
                 cu_check(g_cu.LibraryGetKernel(&m->k_gr[1], m->lib, "bay_batch_rows_logfn"), "GetKernel(rows)");
+                const char* rw[3][2] = {{"bay_batch_rows_move", "bay_batch_rows_logfn"},
+                                        {"bay_batch_rows_move2", "bay_batch_rows_logfn2"},
+                                        {"bay_batch_rows_move4", "bay_batch_rows_logfn4"}};
+                for (int q = 0; q < 3; ++q)
+                    for (int i = 0; i < 2; ++i)
+                        cu_check(g_cu.LibraryGetKernel(&m->k_gr_wpt[q][i], m->lib, rw[q][i]),
+                                 "GetKernel(rows)");
                 cu_check(g_cu.LibraryGetKernel(&m->k_bmeans, m->lib, "bay_batch_means"), "GetKernel(means)");
                 m->row_len = d->row_len;
                 m->prep_len = d->prep_len ? d->prep_len : 1u;

@@ -188,7 +188,14 @@ __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P
     }
 }
 
-template <int MODE>  // 0: move (K walkers), 2: log density of all W
+// WPT walkers per thread (1, 2 or 4): thread t serves walkers tw, tw + TPR, ..., tw + (WPT -
+// 1) TPR of the item (TPR = wpc / WPT threads per row group, tw = t % TPR) on row group
+// t / TPR, so one staged row -- one broadcast load, and whatever the model derives from the
+// row alone -- serves WPT walkers.  Each walker's sum has the same structure for any WPT
+// (its rows split over L = 256 / TPR row groups, batches of 8 pairwise with a Kahan carry,
+// the row groups combined in xor-butterfly then warp order), so results depend on WPT only
+// through L.
+template <int MODE, unsigned int WPT>  // MODE 0: move (K walkers), 2: log density of all W
 __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
     extern __shared__ __align__(16) float bay_bsm[];
     const bay_bitem I = P.items[blockIdx.x];
@@ -201,7 +208,7 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
     float* Ys = bay_bsm;                                              // [wpc][dpad]
     float* Pr = Ys + ((wpc * dpad + 3u) & ~3u);                        // [wpc][BAY_PREP_LEN]
     float* Rs = Pr + ((wpc * BAY_PREP_LEN + 3u) & ~3u);                // [nr][BAY_ROW_STRIDE]
-    float* red = Rs + M.chunk_rows * BAY_ROW_STRIDE;                   // [256][2]
+    float* red = Rs + M.chunk_rows * BAY_ROW_STRIDE;                   // [256][WPT][2]
     const unsigned int nv = nk - I.k0 < wpc ? nk - I.k0 : wpc;   // walkers of the item
     // stage the item's walkers, their prep values and its chunk of rows (coalesced,
     // every load issued before any is used)
@@ -221,17 +228,24 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
     }
     __syncthreads();
     // walkers fastest: a warp's lanes are up to 32 walkers on the same row (a broadcast)
-    const unsigned int L = blockDim.x / wpc, w = tid % wpc, l = tid / wpc;
-    float sum = 0.0f, cmp = 0.0f;
-    if (w < nv) {
-        const float* xw = Ys + w * dpad;
-        const float* pw = Pr + w * BAY_PREP_LEN;
+    const unsigned int TPR = wpc / WPT;                 // threads per row group
+    const unsigned int L = blockDim.x / TPR, tw = tid % TPR, l = tid / TPR;
+    float sum[WPT], cmp[WPT];
+    const float* xw[WPT];
+    const float* pw[WPT];
+#pragma unroll
+    for (unsigned int j = 0; j < WPT; ++j) {
+        sum[j] = 0.0f;
+        cmp[j] = 0.0f;
+        xw[j] = Ys + (tw + j * TPR) * dpad;
+        pw[j] = Pr + (tw + j * TPR) * BAY_PREP_LEN;
+    }
+    if (tw < nv) {      // walkers past nv are zero rows in Ys/Pr: their sums are dropped
         unsigned int r = l;
-        // batches of 8 rows summed pairwise, each batch added with Kahan compensation;
-        // a row comes to registers as BAY_ROW_STRIDE / 4 vector loads (a warp's lanes load
-        // the same row: a broadcast)
+        // batches of 8 rows summed pairwise per walker, each batch added with Kahan
+        // compensation; a row comes to registers as BAY_ROW_STRIDE / 4 vector loads
         for (; r + 7u * L < nr; r += 8u * L) {
-            float t[8];
+            float t[WPT][8];
 #pragma unroll
             for (unsigned int i = 0; i < 8u; ++i) {
                 float rv[BAY_ROW_STRIDE];
@@ -244,53 +258,64 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
                     rv[4 * q + 2] = v4.z;
                     rv[4 * q + 3] = v4.w;
                 }
-                t[i] = BAY_TILE_TERM(rv, xw, pw);
+#pragma unroll
+                for (unsigned int j = 0; j < WPT; ++j) t[j][i] = BAY_TILE_TERM(rv, xw[j], pw[j]);
             }
 #pragma unroll
-            for (unsigned int h = 4u; h >= 1u; h >>= 1)
+            for (unsigned int j = 0; j < WPT; ++j) {
 #pragma unroll
-                for (unsigned int i = 0; i < h; ++i) t[i] = __fadd_rn(t[i], t[i + h]);
-            const float yk = __fsub_rn(t[0], cmp);
-            const float s2 = __fadd_rn(sum, yk);
-            cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
-            sum = s2;
+                for (unsigned int h = 4u; h >= 1u; h >>= 1)
+#pragma unroll
+                    for (unsigned int i = 0; i < h; ++i) t[j][i] = __fadd_rn(t[j][i], t[j][i + h]);
+                const float yk = __fsub_rn(t[j][0], cmp[j]);
+                const float s2 = __fadd_rn(sum[j], yk);
+                cmp[j] = __fsub_rn(__fsub_rn(s2, sum[j]), yk);
+                sum[j] = s2;
+            }
         }
         for (; r < nr; r += L) {
-            const float yk = __fsub_rn(BAY_TILE_TERM(Rs + r * BAY_ROW_STRIDE, xw, pw), cmp);
-            const float s2 = __fadd_rn(sum, yk);
-            cmp = __fsub_rn(__fsub_rn(s2, sum), yk);
-            sum = s2;
+#pragma unroll
+            for (unsigned int j = 0; j < WPT; ++j) {
+                const float yk = __fsub_rn(BAY_TILE_TERM(Rs + r * BAY_ROW_STRIDE, xw[j], pw[j]), cmp[j]);
+                const float s2 = __fadd_rn(sum[j], yk);
+                cmp[j] = __fsub_rn(__fsub_rn(s2, sum[j]), yk);
+                sum[j] = s2;
+            }
         }
     }
     // combine the lanes of each walker: inside a warp by an xor butterfly over the lane
     // bits above the walker bits (bay_bcadd is symmetric, so every lane of a walker ends
     // with the same bits), then across warps in warp order
-    bay_bcf v;
-    v.hi = sum;
-    v.lo = -cmp;
-    for (unsigned int o = 16u; o >= wpc && o >= 1u; o >>= 1) {
-        bay_bcf u;
-        u.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
-        u.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
-        v = bay_bcadd(v, u);
-    }
     const unsigned int lane = tid & 31u, warp = tid >> 5;
-    const unsigned int wpw = wpc < 32u ? wpc : 32u;   // walkers per warp
-    if (lane < wpw) {
-        red[2 * (warp * 32u + lane)] = v.hi;
-        red[2 * (warp * 32u + lane) + 1] = v.lo;
+    const unsigned int tpw = TPR < 32u ? TPR : 32u;   // walker slots per warp
+#pragma unroll
+    for (unsigned int j = 0; j < WPT; ++j) {
+        bay_bcf v;
+        v.hi = sum[j];
+        v.lo = -cmp[j];
+        for (unsigned int o = 16u; o >= TPR && o >= 1u; o >>= 1) {
+            bay_bcf u;
+            u.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+            u.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+            v = bay_bcadd(v, u);
+        }
+        if (lane < tpw) {
+            red[2 * ((warp * 32u + lane) * WPT + j)] = v.hi;
+            red[2 * ((warp * 32u + lane) * WPT + j) + 1] = v.lo;
+        }
     }
     __syncthreads();
     if (tid < nv) {
-        // walker tid's partials: warps holding it, each at lane tid % 32
-        const unsigned int stride = wpc < 32u ? 1u : wpc / 32u;   // warps between its copies
+        // walker tid = tw' + j' TPR: its partials sit at lane tw' % 32 of the warps holding tw'
+        const unsigned int twp = tid % TPR, jp = tid / TPR;
+        const unsigned int stride = TPR < 32u ? 1u : TPR / 32u;   // warps between its copies
         bay_bcf a;
         a.hi = 0.0f;
         a.lo = 0.0f;
-        for (unsigned int wq = tid / 32u; wq < blockDim.x / 32u; wq += stride) {
+        for (unsigned int wq = twp / 32u; wq < blockDim.x / 32u; wq += stride) {
             bay_bcf b;
-            b.hi = red[2 * (wq * 32u + (tid & 31u))];
-            b.lo = red[2 * (wq * 32u + (tid & 31u)) + 1];
+            b.hi = red[2 * ((wq * 32u + (twp & 31u)) * WPT + jp)];
+            b.lo = red[2 * ((wq * 32u + (twp & 31u)) * WPT + jp) + 1];
             a = bay_bcadd(a, b);
         }
         float* out = P.part + M.part + 2 * ((size_t)(I.k0 + tid) * M.chunks + I.c);
@@ -385,10 +410,22 @@ extern "C" __global__ void __launch_bounds__(256) bay_batch_propose_logfn(bay_ba
     bay_batch_propose_impl<2>(P);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_move(bay_batch_params P) {
-    bay_batch_rows_impl<0>(P);
+    bay_batch_rows_impl<0, 1u>(P);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_logfn(bay_batch_params P) {
-    bay_batch_rows_impl<2>(P);
+    bay_batch_rows_impl<2, 1u>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_move2(bay_batch_params P) {
+    bay_batch_rows_impl<0, 2u>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_logfn2(bay_batch_params P) {
+    bay_batch_rows_impl<2, 2u>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_move4(bay_batch_params P) {
+    bay_batch_rows_impl<0, 4u>(P);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_logfn4(bay_batch_params P) {
+    bay_batch_rows_impl<2, 4u>(P);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_accept_bare(bay_batch_params P) {
     bay_batch_accept_impl<0>(P);

@@ -1472,25 +1472,65 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
             ::"r"(s_img), "l"(P.gemm_lay), "r"(img_bytes), "r"(bar_img) : "memory");
     }
-    if (!PERSIST) {
-        // nothing above reads memory another kernel writes: with a programmatic dependent
-        // launch this CTA may have started before the previous kernel of the stream
-        // finished; wait for it (and its memory) here, then let the next launch start its
-        // own set-up
-        asm volatile("griddepcontrol.wait;" ::: "memory");
-        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    }
     unsigned int mma_par = 0u;                  // phase parity of bar_mma's next completion
     const unsigned int nsteps = PERSIST ? m : 1u;
     const unsigned int h_lo = (PERSIST && !LOGFN_ONLY) ? 0u : P.half;
     const unsigned int h_hi = (PERSIST && !LOGFN_ONLY) ? 2u : P.half + 1u;
-    // control words, constant during a launch
+    // control words, constant during a launch: separate kernels between chunks write them,
+    // and a launch after one of those starts only once it completed
     const unsigned int step0 = P.ctl->step[kind], seed0 = P.ctl->seed[kind];
     const float a_str = P.ctl->a, beta = ACCU ? 1.0f : P.ctl->beta;
     // tiles g * gridDim.x + blockIdx.x, + G * gridDim.x, ...: consecutive tiles on
     // different SMs, every SM busy when the tiles outnumber the CTAs
     const unsigned int tile0 = g * gridDim.x + blockIdx.x;
     const unsigned int tstride = PERSIST ? gridDim.x * G : ntiles;
+    constexpr unsigned int NU = (DIM + 7u) / 8u;               // 8-dim units of a row
+    constexpr unsigned int NQ = BAY_TR_W * NU;                  // (walker, unit) items
+    constexpr unsigned int IB = 2u;                             // items in flight per thread
+    // 2. proposals (Philox, z, partner) and the current log densities of a tile's walkers
+    auto proposals = [&](unsigned int tile, unsigned int half, unsigned int step) {
+        const unsigned int k0 = tile * BAY_TR_W;
+        const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
+        if (tid < nt) {
+            const unsigned int k = k0 + tid;
+            const unsigned int stream = ACCU ? (half ? 2222u : 1111u) : (half ? 4444u : 3333u);
+            bay_u4 c;
+            c.x = k;
+            c.y = step;
+            c.z = stream;
+            c.w = 0xbeeff00du;
+            const bay_u4 r = bay_philox4x32_10(c, seed0 + half, 0xdecafbadu);
+            sZ[g][tid] = bay_stretch_z(a_str, bay_u01(r.y));
+            sJ[g][tid] = bay_partner(bay_u01(r.x), P.K);
+            sU2[g][tid] = bay_u01(r.z);
+            sLx[g][tid] = P.logfn[(size_t)half * P.K + k];
+        }
+    };
+    // the first gather pass's own rows (the tile's walkers), kept in registers
+    float xpre[IB][8];
+    auto own_rows = [&](const float* Xt, unsigned int nt) {
+#pragma unroll
+        for (unsigned int b = 0; b < IB; ++b) {
+            const unsigned int q = b * 256u + tid;
+            const unsigned int w = q / NU, u = q - w * NU;
+            bay_tr_ld8(Xt + (size_t)w * DIM, u, q < NQ && w < nt, xpre[b]);
+        }
+    };
+    if (!PERSIST) {
+        // One launch per half-step: this half's walkers last moved two launches back, so
+        // their rows and log densities, like the draws, are final once the previous launch
+        // began its work -- which it did only after waiting for its own predecessor, before
+        // it let this launch start.  Load them now; only the partner rows (the half the
+        // previous launch moves) wait for that launch and its memory.
+        if (tile0 < ntiles) {
+            const unsigned int k0 = tile0 * BAY_TR_W;
+            const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
+            if (!LOGFN_ONLY) proposals(tile0, P.half, step0 + P.step_off);
+            own_rows(P.xs + (LOGFN_ONLY ? 0 : (size_t)P.half * P.K * DIM) + (size_t)k0 * DIM, nt);
+        }
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    }
     bool go = true;
     for (unsigned int si = 0; si < nsteps && go; ++si) {
     for (unsigned int half = h_lo; half < h_hi && go; ++half) {
@@ -1504,20 +1544,10 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     for (unsigned int tile = tile0; tile < ntiles; tile += tstride) {
     const unsigned int k0 = tile * BAY_TR_W;
     const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
-    // 2. proposals (Philox, z, partner) of the tile
-    if (!LOGFN_ONLY && tid < nt) {
-        const unsigned int k = k0 + tid;
-        const unsigned int stream = ACCU ? (half ? 2222u : 1111u) : (half ? 4444u : 3333u);
-        bay_u4 c;
-        c.x = k;
-        c.y = step;
-        c.z = stream;
-        c.w = 0xbeeff00du;
-        const bay_u4 r = bay_philox4x32_10(c, seed0 + half, 0xdecafbadu);
-        sZ[g][tid] = bay_stretch_z(a_str, bay_u01(r.y));
-        sJ[g][tid] = bay_partner(bay_u01(r.x), P.K);
-        sU2[g][tid] = bay_u01(r.z);
-        sLx[g][tid] = P.logfn[(size_t)half * P.K + k];
+    float* const Xt = X + (size_t)k0 * DIM;
+    if (PERSIST) {
+        if (!LOGFN_ONLY) proposals(tile, half, step);
+        own_rows(Xt, nt);
     }
     bay_gsync(g);
     // 3. Y of the tile (walker-major rows of odd stride) from (walker, 8-dim unit) items:
@@ -1525,10 +1555,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     //    contiguous block, a partner's row is 4 * DIM contiguous bytes), IB items' loads in
     //    flight per thread; with the coefficients at dim 0 the same thread splits its unit
     //    into bf16 hi + lo and writes it to the A operand
-    constexpr unsigned int NU = (DIM + 7u) / 8u;               // 8-dim units of a row
-    constexpr unsigned int NQ = BAY_TR_W * NU;                  // (walker, unit) items
-    constexpr unsigned int IB = 2u;                             // items in flight per thread
-    float* const Xt = X + (size_t)k0 * DIM;
     for (unsigned int q0 = 0; q0 < NQ; q0 += IB * 256u) {
         float xv[IB][8], sv[IB][8];
 #pragma unroll
@@ -1536,7 +1562,12 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
             const unsigned int q = q0 + b * 256u + tid;
             const unsigned int w = q / NU, u = q - w * NU;
             const bool ok = q < NQ && w < nt;
-            bay_tr_ld8(Xt + (size_t)w * DIM, u, ok, xv[b]);
+            if (q0 == 0u) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) xv[b][i] = xpre[b][i];
+            } else {
+                bay_tr_ld8(Xt + (size_t)w * DIM, u, ok, xv[b]);
+            }
             if (!LOGFN_ONLY) bay_tr_ld8(S + (size_t)sJ[g][ok ? w : 0u] * DIM, u, ok, sv[b]);
         }
 #pragma unroll
@@ -2029,40 +2060,52 @@ __device__ __forceinline__ unsigned int bay_tile_issue(const bay_stretch_params&
     return nf;
 }
 
+// The chunk buffers' barriers and the CTA's verdict on its copies.
+struct bay_tile_sync {
+    unsigned long long bar[2];
+    unsigned int ok;
+};
+
+// Thread 0: the chunk barriers and the first two chunks' copies.  The data never change
+// while a sampler runs, so this may run before the launch waits for its predecessor.  The
+// CTA's threads wait on the barriers only after a __syncthreads that follows this.
+__device__ __forceinline__ void bay_tile_begin(const bay_stretch_params& P, bay_tile_sync* sy) {
+    extern __shared__ __align__(128) float bay_tsm[];
+    if (threadIdx.x != 0) return;
+    const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
+    const unsigned long long nch = (n_rows + BAY_TILE_CHUNK_ROWS - 1) / BAY_TILE_CHUNK_ROWS;
+    const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(&sy->bar[0]);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    sy->ok = 1u;
+    for (unsigned long long c = 0; c < 2 && c < nch; ++c)
+        bay_tile_issue(P, c, bay_tsm + (unsigned int)c * BAY_TILE_CHUNK, bar0 + 8u * (unsigned int)c);
+}
+
 // Sum over all data rows of BAY_TILE_TERM(row, prep of walker w) for the CTA's walkers
 // w < BAY_WPC (prep: [BAY_WPC][BAY_PREP_LEN] in shared memory) -> out[w] (compensated
-// pairs).  Every thread of the CTA calls it.  Returns false (and sets the status) when a
-// bounded wait for a copy gave up; out is then incomplete.
+// pairs), the copies begun by bay_tile_begin.  Every thread of the CTA calls it.  Returns
+// false (and sets the status) when a bounded wait for a copy gave up; out is then
+// incomplete.
 __device__ __forceinline__ bool bay_tiled_logfn_rows(const bay_stretch_params& P,
                                                     const float (*prep)[BAY_PREP_LEN],
-                                                    bay_cf (*red)[BAY_WPC], bay_cf* out) {
+                                                    bay_cf (*red)[BAY_WPC], bay_cf* out,
+                                                    bay_tile_sync* sy) {
     extern __shared__ __align__(128) float bay_tsm[];
-    __shared__ __align__(8) unsigned long long sBar[2];
-    __shared__ unsigned int sOk;
+    unsigned int& sOk = sy->ok;
     constexpr unsigned int L = BAY_CTA / BAY_WPC;       // row groups
     const unsigned int tid = threadIdx.x, w = tid % BAY_WPC, l = tid / BAY_WPC;
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     const unsigned long long nch = (n_rows + BAY_TILE_CHUNK_ROWS - 1) / BAY_TILE_CHUNK_ROWS;
-    float* buf[2] = {bay_tsm, bay_tsm + BAY_TILE_CHUNK};
-    const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(&sBar[0]);
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        sOk = 1u;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        for (unsigned long long c = 0; c < 2 && c < nch; ++c)
-            bay_tile_issue(P, c, buf[c], bar0 + 8u * (unsigned int)c);
-    }
+    const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(&sy->bar[0]);
     float pv[BAY_PREP_LEN];
 #pragma unroll
     for (int i = 0; i < BAY_PREP_LEN; ++i) pv[i] = prep[w][i];
     float sum = 0.0f, cmp = 0.0f;
     for (unsigned long long c = 0; c < nch; ++c) {
         const unsigned int b = (unsigned int)(c & 1ull);
-        float* R = buf[b];
+        float* R = bay_tsm + b * BAY_TILE_CHUNK;
         const unsigned long long r0 = c * BAY_TILE_CHUNK_ROWS;
         const unsigned int nr = (unsigned int)(n_rows - r0 < BAY_TILE_CHUNK_ROWS ? n_rows - r0
                                                                               : BAY_TILE_CHUNK_ROWS);
@@ -2136,24 +2179,40 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
     const float* hyper = P.params + P.data_len;
     const unsigned int k0 = blockIdx.x * BAY_WPC;
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
+    __shared__ bay_tile_sync sSync;
+    bay_tile_begin(P, &sSync);
+    // Launched with programmatic dependent launch: the draws, the walker's own row and log
+    // density (this half last moved two launches back, final once the previous launch began
+    // its work, which it did only after waiting for its own predecessor) come before the
+    // wait for the previous launch; the partner row, from the half that launch moves, after.
+    const unsigned int t0 = threadIdx.x, kk = k0 + t0;
+    const bool mine_ok = t0 < BAY_WPC && kk < P.K;
+    float xr[DIM], z = 0.0f, u2 = 0.0f;
+    unsigned int j = 0;
+    if (mine_ok) {
+        bay_u4 c;
+        c.x = kk;
+        c.y = step;
+        c.z = stream;
+        c.w = 0xbeeff00du;
+        const bay_u4 r = bay_philox4x32_10(c, seed, 0xdecafbadu);
+        z = bay_stretch_z(a, bay_u01(r.y));
+        j = bay_partner(bay_u01(r.x), P.K);
+        u2 = bay_u01(r.z);
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) xr[i] = X[(size_t)kk * DIM + i];
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     if (threadIdx.x < BAY_WPC) {
         const unsigned int t = threadIdx.x, k = k0 + t;
         if (k < P.K) {
-            bay_u4 c;
-            c.x = k;
-            c.y = step;
-            c.z = stream;
-            c.w = 0xbeeff00du;
-            const bay_u4 r = bay_philox4x32_10(c, seed, 0xdecafbadu);
-            const float u0 = bay_u01(r.x), u1 = bay_u01(r.y);
-            const float z = bay_stretch_z(a, u1);
-            const unsigned int j = bay_partner(u0, P.K);
             float Y[DIM];
 #pragma unroll
             for (int i = 0; i < DIM; ++i) {
                 const float s = bay_partner_coord(S, P.K, j, i);
-                Y[i] = __fmaf_rn(z, __fsub_rn(X[(size_t)k * DIM + i], s), s);
+                Y[i] = __fmaf_rn(z, __fsub_rn(xr[i], s), s);
                 sY[t][i] = Y[i];
             }
             float pr[BAY_PREP_LEN];
@@ -2162,7 +2221,7 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
             for (int i = 0; i < BAY_PREP_LEN; ++i) sPrep[t][i] = pr[i];
             sW[t] = BAY_TILE_WALKER(n_rows, hyper, P.params_len, DIM, Y);
             sZ[t] = z;
-            sU2[t] = bay_u01(r.z);
+            sU2[t] = u2;
         } else {
 #pragma unroll
             for (int i = 0; i < BAY_PREP_LEN; ++i) sPrep[t][i] = 0.0f;
@@ -2170,7 +2229,7 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
         }
     }
     __syncthreads();
-    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum);
+    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum, &sSync);
     bool accepted = false;
     const unsigned int t = threadIdx.x, k = k0 + t;
     const bool valid = t < BAY_WPC && k < P.K;
@@ -2210,6 +2269,8 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
     const float* hyper = P.params + P.data_len;
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     const unsigned int k0 = blockIdx.x * BAY_WPC;
+    __shared__ bay_tile_sync sSync;
+    bay_tile_begin(P, &sSync);
     if (threadIdx.x < BAY_WPC) {
         const unsigned int t = threadIdx.x, k = k0 + t;
         if (k < P.W) {
@@ -2228,7 +2289,7 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
         }
     }
     __syncthreads();
-    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum);
+    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum, &sSync);
     const unsigned int t = threadIdx.x, k = k0 + t;
     if (ok && t < BAY_WPC && k < P.W) P.logfn[k] = bay_cf_total(sW[t], sSum[t]);
 }

@@ -367,7 +367,8 @@ class GB300StretchFactory:
         N.call("bay_batch_autotune", self.handle, arr, len(members), C.byref(r))
         return {"shape": {"rows_per_thread": r.shape.rows_per_thread,
                           "walkers_per_item": r.shape.walkers_per_item,
-                          "chunk_floats": r.shape.chunk_floats},
+                          "chunk_floats": r.shape.chunk_floats,
+                          "walkers_per_thread": r.shape.walkers_per_thread},
                 "candidates": r.candidates, "from_cache": bool(r.from_cache),
                 "us_per_step": r.us_per_step, "default_us_per_step": r.default_us_per_step}
 
@@ -399,7 +400,8 @@ class GB300Batch:
         if shape:
             sh = N.BatchShape(int(shape.get("rows_per_thread", 0)),
                               int(shape.get("walkers_per_item", 0)),
-                              int(shape.get("chunk_floats", 0)))
+                              int(shape.get("chunk_floats", 0)),
+                              int(shape.get("walkers_per_thread", 0)))
             N.call("bay_batch_create_shaped", sfactory.handle, arr, len(members), C.byref(sh),
                    C.byref(h))
         else:

@@ -159,8 +159,8 @@ def test_model_check_autotuner_shapes(native):
     form's tile groups; shapes outside the kernels' limits are argument errors."""
     from bayadera_gb300 import models as M
     post = M.gaussian_posterior_model()
-    for wpc, cta in ((8, 256), (4, 128), (8, 128), (16, 256), (32, 256), (8, 512), (16, 512),
-                     (32, 512), (32, 1024)):
+    for wpc, cta in ((8, 256), (2, 256), (4, 256), (4, 512), (4, 128), (8, 128), (16, 256),
+                     (32, 256), (8, 512), (16, 512), (32, 512), (32, 1024)):
         _check(post, "tiled", walkers_per_cta=wpc, cta_threads=cta)
     for bad in ((3, 256), (64, 256), (32, 16)):
         with pytest.raises(native.IllegalArgument):

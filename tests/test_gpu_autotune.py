@@ -49,7 +49,7 @@ def test_tiled_shapes_match_fp64(factory, M, n):
     initial and moved walkers within 2e-6 relative of FP64."""
     params = _c1_params(n)
     W = 1024
-    for wpc, cta in ((8, 256), (4, 128), (16, 256), (32, 256), (8, 512), (32, 1024)):
+    for wpc, cta in ((8, 256), (2, 256), (4, 512), (16, 256), (32, 256), (32, 1024)):
         sf = factory.mcmc_factory(M.gaussian_posterior_model(), form="tiled", walkers_per_cta=wpc,
                                   cta_threads=cta)
         s = sf.create_sampler(5, W, params)
@@ -131,8 +131,8 @@ def test_autotune_tiled_and_cache(factory, M):
     assert r["candidates"] >= 2 and not r["from_cache"]
     assert r["us_per_step"] <= r["default_us_per_step"]
     assert (r["shape"]["walkers_per_cta"], r["shape"]["cta_threads"]) in (
-        (8, 256), (4, 128), (8, 128), (16, 256), (32, 256), (8, 512), (16, 512), (32, 512),
-        (32, 1024))
+        (8, 256), (2, 256), (4, 256), (4, 512), (4, 128), (8, 128), (16, 256), (32, 256),
+        (8, 512), (16, 512), (32, 512), (32, 1024))
     r2 = factory.autotune(model, 4096, params, form="tiled")
     assert r2["from_cache"] and r2["shape"] == r["shape"]
     sf = factory.mcmc_factory(model, form="tiled", **r["shape"])
@@ -185,3 +185,32 @@ def test_batch_shapes_and_autotune(factory, M, oracle):
     assert r["us_per_step"] <= r["default_us_per_step"]
     assert fam.autotune_batch(members)["from_cache"]
     fam.release()
+
+
+def test_batch_walkers_per_thread_bit_identical(factory, M):
+    """The row-term kernel with 4 walkers per thread shares each staged row between them;
+    with the same row groups per walker (16 walkers per item at 1 per thread, 64 at 4 per
+    thread: 16 row groups each) and the same row chunks (chunk_floats caps them at 256
+    rows), every walker's sum has the same order: identical positions and log densities."""
+    rng = np.random.default_rng(5)
+    fam = factory.mcmc_factory(M.hierarchical_rows_batch_model(16), form="batch")
+    members = []
+    for i, J in enumerate((2, 7, 16)):
+        ys = [rng.normal(j, 1.0, 100 + 29 * j) for j in range(J)]
+        p, rows = M.hierarchical_rows_params(ys, np.ones(J))
+        members.append({"dim": J + 2, "seed": 20 + i, "walkers": 256, "params": p, "rows": rows})
+    out = []
+    for shape in ({"rows_per_thread": 512, "walkers_per_item": 16, "chunk_floats": 1024,
+                   "walkers_per_thread": 1},
+                  {"rows_per_thread": 512, "walkers_per_item": 64, "chunk_floats": 1024,
+                   "walkers_per_thread": 4}):
+        b = fam.create_batch(members, shape)
+        b.init_position_normal([5, 6, 7], 0.0, 1.0)
+        b.burn_in(6, 2.0)
+        out.append(([p.copy() for p in b.positions()], [l.copy() for l in b.logfn()]))
+        b.release()
+    fam.release()
+    for pa, pb in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(pa, pb)
+    for la, lb in zip(out[0][1], out[1][1]):
+        np.testing.assert_array_equal(la, lb)
