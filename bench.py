@@ -583,7 +583,7 @@ def c4_members(M, n=512, seed=0):
     return out
 
 
-def measure_c4(steps, warmup):
+def measure_c4(steps, warmup, members=512):
     """The 512-model batch: whole jobs (init, 1,000 burn-in and 2,000 accu steps of every
     member) timed with the L2 flushed before each, the plain single-model form on a sample
     of the members; returns the config's record."""
@@ -592,7 +592,7 @@ def measure_c4(steps, warmup):
     from bayadera_gb300 import models as M
     from bayadera_gb300.engine import GB300BayaderaFactory
     BURN4, RUN4 = 1000, 2000
-    mem = c4_members(M)
+    mem = c4_members(M, members)
     W = np.array([m["walkers"] for m in mem], np.float64)
     N = np.array([m["rows"] for m in mem], np.float64)
     J = np.array([m["dim"] - 2 for m in mem], np.float64)
@@ -682,8 +682,10 @@ def measure_c4(steps, warmup):
     plain_value = float(np.sum(W)) * (BURN4 + RUN4) / t_plain_full
     achieved = flop_step / t_step / 1e12
     rates = res["acceptance_rates"]
-    return {"workload": "512 Gaussian hierarchical models, J log-U[2,128], n_j log-U[10,1000], "
-                        "walkers {256,512,1024,4096}",
+    return {"workload": "%d Gaussian hierarchical models, J log-U[2,128], n_j log-U[10,1000], "
+                        "walkers {256,512,1024,4096}%s"
+                        % (len(mem), "" if members == 512 else " [profiling case: the first %d of 512]"
+                           % members),
             "models": len(mem), "walkers_total": int(np.sum(W)), "rows_total": int(np.sum(N)),
             "burn_in": BURN4, "run": RUN4,
             "form": "batch (CUDA-graph chunks over balanced work lists)",
@@ -708,7 +710,7 @@ def run_c4(args):
     __graft_entry__.build()
     torch.cuda.set_device(0)
     with ClockSampler(0) as clocks:
-        rec = measure_c4(args.steps, args.warmup)
+        rec = measure_c4(args.steps, args.warmup, args.members)
     line = {"metric": "walker-steps/s", "value": rec["value"], "unit": "walker-steps/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": rec["ms_per_job"], "higher_is_better": True, "scaling": "weak",
@@ -762,6 +764,9 @@ def main():
     ap.add_argument("--rows", type=int, default=0,
                     help="with --config c3 or c5: data rows instead of the configuration's "
                          "(a smaller case for profiling); the line then names the row count")
+    ap.add_argument("--members", type=int, default=512,
+                    help="with --config c4: the first N of the 512 models (a smaller case for "
+                         "profiling); the line then names the count")
     ap.add_argument("--forms", default="",
                     help="with --config: comma-separated subset of the forms to run "
                          "(tensor, gemm, tiled, plain), e.g. for a profile of one form")
