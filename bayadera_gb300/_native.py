@@ -159,6 +159,8 @@ _SIGNATURES = {
     "bay_data_histogram": (C.c_int, [P, P, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, P, P,
                                      P]),
     "bay_batch_create": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32, C.POINTER(P)]),
+    "bay_batch_set_persistent": (C.c_int, [P, C.c_int]),
+    "bay_batch_test_barrier_timeout": (C.c_int, [P, C.c_int]),
     "bay_batch_create_shaped": (C.c_int, [P, C.POINTER(BatchMember), C.c_uint32,
                                           C.POINTER(BatchShape), C.POINTER(P)]),
     "bay_autotune": (C.c_int, [P, C.POINTER(ModelDesc), C.c_uint64, P, C.c_uint64, P,

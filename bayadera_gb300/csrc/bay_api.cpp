@@ -219,6 +219,7 @@ struct bay_model {
     CUkernel k_gp[3] = {nullptr, nullptr, nullptr};
     CUkernel k_gr[2] = {nullptr, nullptr};
     CUkernel k_gr_wpt[3][2] = {};   // batch form rows kernels with 1, 2, 4 walkers per thread
+    CUkernel k_brun[2][3] = {};     // batch form persistent launches [bare, accu][walkers per thread]
     CUkernel k_ga[3] = {nullptr, nullptr, nullptr};
     // GEMM form on the tensor cores: rows kernels [move, logfn], walker sub-tiles per CTA,
     // shared-memory stages, dynamic shared memory
@@ -1032,6 +1033,12 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                     for (int i = 0; i < 2; ++i)
                         cu_check(g_cu.LibraryGetKernel(&m->k_gr_wpt[q][i], m->lib, rw[q][i]),
                                  "GetKernel(rows)");
+                const char* br[2][3] = {{"bay_batch_run_bare", "bay_batch_run_bare2", "bay_batch_run_bare4"},
+                                        {"bay_batch_run_accu", "bay_batch_run_accu2", "bay_batch_run_accu4"}};
+                for (int i = 0; i < 2; ++i)
+                    for (int q = 0; q < 3; ++q)
+                        cu_check(g_cu.LibraryGetKernel(&m->k_brun[i][q], m->lib, br[i][q]),
+                                 "GetKernel(batch run)");
                 cu_check(g_cu.LibraryGetKernel(&m->k_bmeans, m->lib, "bay_batch_means"), "GetKernel(means)");
                 m->row_len = d->row_len;
                 m->prep_len = d->prep_len ? d->prep_len : 1u;

@@ -89,6 +89,10 @@ struct bay_batch_params {
     bay_ctl* ctl;
     unsigned long long dsum_stride;
     unsigned int half, step_off, means_cap, n_members;
+    unsigned int n_tiles, n_items;  // move tiles and rows work items (the persistent launch)
+    unsigned int gbar_extra;        // persistent launch: extra arrivals its barriers wait for
+                                    // (0; 1 makes them run out, for tests)
+    unsigned int pad;
 };
 
 // log u <= (dim - 1) log z + beta (ly - lx), decided as in FP64 (bay_accept_log); a
@@ -134,10 +138,10 @@ __device__ __forceinline__ unsigned int bay_partner(float u0, unsigned int K) {
 }
 
 template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions (all W)
-__device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P) {
+__device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P, unsigned int idx) {
     __shared__ float sZ[256];
     __shared__ unsigned int sJ[256];
-    const bay_btile T = P.tiles[blockIdx.x];
+    const bay_btile T = P.tiles[idx];
     const bay_bmember& M = P.mem[T.m];
     const unsigned int nk = MODE == 2 ? M.W : M.K;
     const unsigned int dim = M.dim;
@@ -196,9 +200,9 @@ __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P
 // the row groups combined in xor-butterfly then warp order), so results depend on WPT only
 // through L.
 template <int MODE, unsigned int WPT>  // MODE 0: move (K walkers), 2: log density of all W
-__device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
+__device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, unsigned int idx) {
     extern __shared__ __align__(16) float bay_bsm[];
-    const bay_bitem I = P.items[blockIdx.x];
+    const bay_bitem I = P.items[idx];
     const bay_bmember& M = P.mem[I.m];
     const unsigned int nk = MODE == 2 ? M.W : M.K;
     const unsigned int dim = M.dim, wpc = I.wpc, tid = threadIdx.x;
@@ -325,8 +329,8 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P) {
 }
 
 template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions
-__device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P) {
-    const bay_btile T = P.tiles[blockIdx.x];
+__device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P, unsigned int idx) {
+    const bay_btile T = P.tiles[idx];
     const bay_bmember& M = P.mem[T.m];
     const unsigned int nk = MODE == 2 ? M.W : M.K;
     const unsigned int dim = M.dim, tid = threadIdx.x;
@@ -368,7 +372,7 @@ __device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P)
     const unsigned int nt = nk - T.k0 < blockDim.x ? nk - T.k0 : blockDim.x;
     const float* Xc = P.xs + M.xs + ((size_t)P.half * M.K + T.k0) * dim;
     float* out = P.dsum + ((size_t)P.step_off * 2 + P.half) * P.dsum_stride + M.dsum
-        + (size_t)(blockIdx.x - M.tile0) * dim;
+        + (size_t)(idx - M.tile0) * dim;
     for (unsigned int d = tid; d < dim; d += blockDim.x) {
         bay_bcf s;
         s.hi = 0.0f;
@@ -401,41 +405,93 @@ __device__ __forceinline__ void bay_batch_means_impl(const bay_batch_params& P) 
 }
 
 extern "C" __global__ void __launch_bounds__(256) bay_batch_propose_bare(bay_batch_params P) {
-    bay_batch_propose_impl<0>(P);
+    bay_batch_propose_impl<0>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_propose_accu(bay_batch_params P) {
-    bay_batch_propose_impl<1>(P);
+    bay_batch_propose_impl<1>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_propose_logfn(bay_batch_params P) {
-    bay_batch_propose_impl<2>(P);
+    bay_batch_propose_impl<2>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_move(bay_batch_params P) {
-    bay_batch_rows_impl<0, 1u>(P);
+    bay_batch_rows_impl<0, 1u>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_logfn(bay_batch_params P) {
-    bay_batch_rows_impl<2, 1u>(P);
+    bay_batch_rows_impl<2, 1u>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_move2(bay_batch_params P) {
-    bay_batch_rows_impl<0, 2u>(P);
+    bay_batch_rows_impl<0, 2u>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_logfn2(bay_batch_params P) {
-    bay_batch_rows_impl<2, 2u>(P);
+    bay_batch_rows_impl<2, 2u>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_move4(bay_batch_params P) {
-    bay_batch_rows_impl<0, 4u>(P);
+    bay_batch_rows_impl<0, 4u>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_rows_logfn4(bay_batch_params P) {
-    bay_batch_rows_impl<2, 4u>(P);
+    bay_batch_rows_impl<2, 4u>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_accept_bare(bay_batch_params P) {
-    bay_batch_accept_impl<0>(P);
+    bay_batch_accept_impl<0>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_accept_accu(bay_batch_params P) {
-    bay_batch_accept_impl<1>(P);
+    bay_batch_accept_impl<1>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(256) bay_batch_accept_logfn(bay_batch_params P) {
-    bay_batch_accept_impl<2>(P);
+    bay_batch_accept_impl<2>(P, blockIdx.x);
 }
 extern "C" __global__ void __launch_bounds__(128) bay_batch_means(bay_batch_params P) {
     bay_batch_means_impl(P);
+}
+
+// One persistent cooperative launch of m steps (both halves each) of every member.  Each
+// half-step's three phases -- proposals over the move tiles, row terms over the work items,
+// accept over the tiles -- run with a bounded grid barrier between them; CTA b takes work
+// b, b + gridDim.x, ... of every phase.  The same functions on the same work as the three
+// launches per half-step, so the results are identical.  A barrier that runs out (status
+// bit 4) ends the launch.
+template <int MODE, unsigned int WPT>
+__device__ __forceinline__ void bay_batch_run_impl(bay_batch_params P, unsigned int m) {
+    unsigned int k = 0;   // grid barriers passed
+    for (unsigned int si = 0; si < m; ++si) {
+        for (unsigned int half = 0; half < 2u; ++half) {
+            P.half = half;
+            P.step_off = si;
+            if ((si | half) != 0u &&
+                !bay_grid_sync(&P.ctl->gbar_count, &P.ctl->abort, &P.ctl->status, gridDim.x, ++k,
+                               P.gbar_extra))
+                return;
+            for (unsigned int t = blockIdx.x; t < P.n_tiles; t += gridDim.x)
+                bay_batch_propose_impl<MODE>(P, t);
+            if (!bay_grid_sync(&P.ctl->gbar_count, &P.ctl->abort, &P.ctl->status, gridDim.x, ++k,
+                               P.gbar_extra))
+                return;
+            for (unsigned int i = blockIdx.x; i < P.n_items; i += gridDim.x)
+                bay_batch_rows_impl<0, WPT>(P, i);
+            if (!bay_grid_sync(&P.ctl->gbar_count, &P.ctl->abort, &P.ctl->status, gridDim.x, ++k,
+                               P.gbar_extra))
+                return;
+            for (unsigned int t = blockIdx.x; t < P.n_tiles; t += gridDim.x)
+                bay_batch_accept_impl<MODE>(P, t);
+        }
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) bay_batch_run_bare(bay_batch_params P, unsigned int m) {
+    bay_batch_run_impl<0, 1u>(P, m);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_run_accu(bay_batch_params P, unsigned int m) {
+    bay_batch_run_impl<1, 1u>(P, m);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_run_bare2(bay_batch_params P, unsigned int m) {
+    bay_batch_run_impl<0, 2u>(P, m);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_run_accu2(bay_batch_params P, unsigned int m) {
+    bay_batch_run_impl<1, 2u>(P, m);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_run_bare4(bay_batch_params P, unsigned int m) {
+    bay_batch_run_impl<0, 4u>(P, m);
+}
+extern "C" __global__ void __launch_bounds__(256) bay_batch_run_accu4(bay_batch_params P, unsigned int m) {
+    bay_batch_run_impl<1, 4u>(P, m);
 }

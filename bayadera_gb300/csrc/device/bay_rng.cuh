@@ -9,6 +9,7 @@
 // (0.5 + (i >> 9)) * 2^-23, an exactly representable value in (0, 1).
 //
 // bay_accept_log: the stretch move's accept test, shared by every kernel form.
+// bay_grid_sync: a bounded grid barrier for persistent cooperative launches.
 //
 // This header is compiled both by nvcc (into libbayadera_gb300.so) and by NVRTC
 // (prepended to every fused stretch kernel), so it uses no host headers.
@@ -71,6 +72,55 @@ __device__ __forceinline__ bool bay_accept_log(float u2, float z, float ly, floa
     if (lhs > rhs + tol) return false;
     const double dl64 = (double)beta * ((double)ly - (double)lx);
     return log((double)u2) <= (double)dm1 * log((double)z) + dl64;
+}
+
+// Grid barrier k (k = 1, 2, ... within a launch) of a cooperative launch (every CTA
+// resident): each CTA adds 1 to *count (a release reduction) and waits until it reaches
+// k * nblocks + extra; the count only grows during a launch and is cleared before it.
+// Bounded: a CTA that waits longer than 2 s raises *abort and status bit 4, and a raised
+// abort ends every wait at once.  Returns false when the launch is being abandoned.
+// `extra` arrivals beyond the grid (nonzero only in tests) make every barrier run out.
+__device__ __forceinline__ bool bay_grid_sync(unsigned int* count, unsigned int* abort_flag,
+                                              unsigned int* status, unsigned int nblocks,
+                                              unsigned int k, unsigned int extra) {
+    __shared__ unsigned int s_go;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int go = 1u;
+        volatile unsigned int* ab = abort_flag;
+        if (*ab) {
+            go = 0u;
+        } else {
+            const unsigned int target = k * nblocks + extra;
+            __threadfence();
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+            unsigned long long t0;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+            for (unsigned int it = 0;; ++it) {
+                unsigned int c;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(count) : "memory");
+                if (c >= target) break;
+                if ((it & 63u) == 63u) {
+                    if (*ab) {
+                        go = 0u;
+                        break;
+                    }
+                    unsigned long long t;
+                    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+                    if (t - t0 > 2000000000ull) {
+                        *ab = 1u;
+                        atomicOr(status, 4u);
+                        go = 0u;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+        }
+        s_go = go;
+    }
+    __syncthreads();
+    return s_go != 0u;
 }
 
 #endif

@@ -429,6 +429,16 @@ class GB300Batch:
     def set_graphs(self, enabled):
         N.call("bay_batch_set_graphs", self.handle, 1 if enabled else 0)
 
+    def set_persistent(self, enabled):
+        """One persistent cooperative launch per chunk of steps for every member, or three
+        launches per half-step (default); both give the same results."""
+        N.call("bay_batch_set_persistent", self.handle, 1 if enabled else 0)
+
+    def arm_barrier_timeout(self, enabled):
+        """Testing the device failure path: the persistent launch's grid barriers wait for
+        one CTA more than the launch has and run out after their bounded wait."""
+        N.call("bay_batch_test_barrier_timeout", self.handle, 1 if enabled else 0)
+
     def init_position_normal(self, seeds, mean=0.0, sd=1.0):
         sd_ = np.ascontiguousarray(seeds, np.uint32)
         if sd_.size != len(self.members):

@@ -610,22 +610,33 @@ def measure_c4(steps, warmup, members=512):
         b.burn_in(BURN4, 2.0)
         return b.run_sampler(RUN4, 2.0)
 
-    for w in range(warmup):
-        job(100 + w)
-    torch.cuda.synchronize()
-    times = []
-    l0 = _native.launch_count()
-    for k in range(steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(k & 0xff)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        res = job(k)
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1) / 1e3)
-    launches = _native.launch_count() - l0
+    def timed(persistent):
+        """warm-up and timed jobs in one launch mode: three launches per half-step, or one
+        persistent launch per chunk of steps"""
+        b.set_persistent(persistent)
+        for w in range(warmup):
+            job(100 + w)
+        torch.cuda.synchronize()
+        ts = []
+        l0 = _native.launch_count()
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = job(k)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return ts, _native.launch_count() - l0, r
+
+    t_launch, l_launch, res_launch = timed(False)
+    t_persist, l_persist, res_persist = timed(True)
+    persistent = sum(t_persist) < sum(t_launch)
+    times, launches, res = ((t_persist, l_persist, res_persist) if persistent
+                            else (t_launch, l_launch, res_launch))
+    b.set_persistent(persistent)
     # FP64 error of the members' log densities after the last job (8 members, 64 walkers)
     errs = []
     pos_all, lf_all = b.positions(), b.logfn()
@@ -688,7 +699,11 @@ def measure_c4(steps, warmup, members=512):
                            % members),
             "models": len(mem), "walkers_total": int(np.sum(W)), "rows_total": int(np.sum(N)),
             "burn_in": BURN4, "run": RUN4,
-            "form": "batch (CUDA-graph chunks over balanced work lists)",
+            "form": "batch (CUDA-graph chunks over balanced work lists; %s)"
+                    % ("one persistent launch per chunk" if persistent
+                       else "three launches per half-step"),
+            "launch_modes_ms_per_job": {"three_launches_per_half_step": 1e3 * sum(t_launch) / steps,
+                                        "persistent_per_chunk": 1e3 * sum(t_persist) / steps},
             "rows_items_per_half_step": info["items"],
             "value": value, "unit": "walker-steps/s", "ms_per_job": 1e3 * sum(times) / steps,
             "gpu_launches": launches,
@@ -717,7 +732,7 @@ def run_c4(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {k: rec[k] for k in ("workload", "models", "walkers_total", "rows_total",
                                            "burn_in", "run", "form",
-                                           "rows_items_per_half_step")},
+                                           "rows_items_per_half_step", "launch_modes_ms_per_job")},
             "gpu_launches": rec["gpu_launches"], "roofline": rec["roofline"],
             "logfn_err_vs_fp64": rec["logfn_err_vs_fp64"], "autotune": rec["autotune"],
             "forms": {"batch": rec["value"], "plain_fp32": rec["plain_fp32"],

@@ -372,7 +372,8 @@ int bay_data_histogram(bay_ctx* ctx, const float* x, uint32_t dim, uint64_t n, u
 /* ---------------------------------------------------------------- batched models
  * Many independent models of one BAY_FORM_BATCH family -- each with its own dimension,
  * walkers, data and seed -- advanced together: every half-step of every member is three
- * launches over balanced work lists (propose, row terms, accept), and the step loops
+ * phases over balanced work lists (propose, row terms, accept), as three launches or within
+ * one persistent launch per chunk of steps (bay_batch_set_persistent), and the step loops
  * replay as CUDA graphs.  Member m behaves as a sampler created with its seed (same
  * Philox counters and keys, same init!/init-move! seed rules), so the per-member
  * semantics are those of the functions above.  No counterpart in the reference, which
@@ -420,6 +421,17 @@ int bay_batch_state_export(bay_batch* b, float* positions, float* logfn);
 /* total walkers, total positions (floats), rows work items of a move half-step */
 int bay_batch_info(bay_batch* b, uint64_t* walkers, uint64_t* floats, uint64_t* items);
 int bay_batch_set_graphs(bay_batch* b, int enabled);
+/* One persistent cooperative launch per chunk of steps for every member (the proposals,
+ * row terms and accept phases of each half-step separated by bounded grid barriers), or
+ * three launches per half-step (default).  Both give the same results.  No reference
+ * counterpart (the reference runs one model per sampler). */
+int bay_batch_set_persistent(bay_batch* b, int enabled);
+/* Testing the device failure path (no reference counterpart): with enabled != 0 the
+ * persistent launch's grid barriers wait for one more CTA than the launch has, so every CTA
+ * gives up after its bounded wait (2 s), raises the abort flag and the status word, and the
+ * launch ends; the next status check returns BAY_ERR_DEVICE.  No fault, trap or unbounded
+ * wait is involved. */
+int bay_batch_test_barrier_timeout(bay_batch* b, int enabled);
 
 /* ---------------------------------------------------------------- autotuner
  * Kernel shapes chosen by timing (no reference counterpart: the reference fixes its work-

@@ -167,3 +167,58 @@ def test_batch_rejects_bad_members(family, M):
         family.create_batch([m, bad])
     with pytest.raises(BayaderaError, match="walkers"):
         family.create_batch([dict(m, walkers=7)])
+
+
+@pytest.mark.parametrize("shape", [None, {"rows_per_thread": 64, "walkers_per_item": 32,
+                                          "walkers_per_thread": 4}])
+def test_batch_persistent_matches_per_launch(family, M, shape):
+    """One persistent cooperative launch per chunk of steps (every member's proposals, row
+    terms and accept phases separated by bounded grid barriers) against three launches per
+    half-step: identical positions, log densities, acceptance rates and per-step means (a
+    40-step burn-in: a whole chunk and a partial one; a 37-step run)."""
+    mem = _members(M, 4)
+    out = {}
+    for persist in (False, True):
+        b = family.create_batch(mem, shape)
+        b.set_persistent(persist)
+        b.init_position_normal([31 + i for i in range(len(mem))], 0.0, 1.0)
+        b.burn_in(40, 2.0)
+        r = b.run_sampler(37, 2.0, return_means=True)
+        out[persist] = ([p.copy() for p in b.positions()], [l.copy() for l in b.logfn()],
+                        np.array(r["acceptance_rates"]), [m.copy() for m in r["means"]])
+        b.release()
+    a, c = out[False], out[True]
+    for x, y in zip(a[0], c[0]):
+        np.testing.assert_array_equal(x, y)
+    for x, y in zip(a[1], c[1]):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_array_equal(a[2], c[2])
+    for x, y in zip(a[3], c[3]):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_batch_grid_barrier_runs_out_and_context_recovers(family, M):
+    """Device failure path without a fault: armed, the persistent launch's grid barriers
+    wait for one CTA more than the launch has; every CTA gives up after its bounded wait
+    (2 s), raises the abort flag and the status word, and the launch ends.  The host reads
+    the status (BAY_ERR_DEVICE, naming the grid barrier); a new batch on the same context
+    then runs normally."""
+    import time
+    from bayadera_gb300._native import BayaderaError, BAY_ERR_DEVICE
+    mem = _members(M, 5)
+    b = family.create_batch(mem)
+    b.set_persistent(True)
+    b.init_position_normal([1 + i for i in range(len(mem))], 0.0, 1.0)
+    b.arm_barrier_timeout(True)
+    t0 = time.perf_counter()
+    with pytest.raises(BayaderaError, match="grid barrier") as e:
+        b.run_sampler(8, 2.0)
+    assert e.value.code == BAY_ERR_DEVICE
+    assert time.perf_counter() - t0 < 60.0
+    b.release()
+    b = family.create_batch(mem)
+    b.set_persistent(True)
+    b.init_position_normal([1 + i for i in range(len(mem))], 0.0, 1.0)
+    r = b.run_sampler(16, 2.0)
+    assert np.all((np.array(r["acceptance_rates"]) > 0.05) & (np.array(r["acceptance_rates"]) < 0.95))
+    b.release()
