@@ -874,15 +874,19 @@ def main():
     idx = np.arange(0, WALKERS, 8)
     err = _err(samp.logfn()[idx], fp64_mvn(P, pos[idx]))
 
-    # the fp32 SIMT GEMM form (64-walker tiles, register-blocked x'Px from shared memory)
-    samp_gemm = sfs["gemm"].create_sampler(seed_base, WALKERS, dP)
-    gemm_value, _, _ = timed_jobs(samp_gemm, max(1, min(args.steps, 2)), 1)
-    samp_gemm.release()
-
-    # the plain FP32 form (one thread per walker, the reference's kernel structure)
-    samp_plain = sfs["plain"].create_sampler(seed_base, WALKERS, dP)
-    plain_value, _, _ = timed_jobs(samp_plain, max(1, min(args.steps, 2)), 1)
-    samp_plain.release()
+    # the comparison forms (--forms tensor skips them: a shorter run for profiling)
+    gemm_value = plain_value = None
+    only = set(args.forms.split(",")) if args.forms else {"tensor", "gemm", "plain"}
+    if "gemm" in only:
+        # the fp32 SIMT GEMM form (64-walker tiles, register-blocked x'Px from shared memory)
+        samp_gemm = sfs["gemm"].create_sampler(seed_base, WALKERS, dP)
+        gemm_value, _, _ = timed_jobs(samp_gemm, max(1, min(args.steps, 2)), 1)
+        samp_gemm.release()
+    if "plain" in only:
+        # the plain FP32 form (one thread per walker, the reference's kernel structure)
+        samp_plain = sfs["plain"].create_sampler(seed_base, WALKERS, dP)
+        plain_value, _, _ = timed_jobs(samp_plain, max(1, min(args.steps, 2)), 1)
+        samp_plain.release()
 
     # dominant kernel: bare stretch launches of a burn-in, events on the launching stream
     n_probe = 256
@@ -973,7 +977,7 @@ def main():
                          "fp32_tflops": flop_launch / t_launch / 1e12},
             "cpu_baseline": cpu,
             "forms": {"tensor": value, "gemm_fp32_simt": gemm_value, "plain_fp32": plain_value,
-                      "speedup_vs_plain": value / plain_value},
+                      "speedup_vs_plain": value / plain_value if plain_value else None},
             "logfn_err_vs_fp64": err,
             "autotune": tune,
             "clocks": clocks.summary(),
