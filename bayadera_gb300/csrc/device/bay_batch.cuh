@@ -16,8 +16,8 @@
 //            chunk).  wpc and the chunk size are chosen per member so that every item
 //            carries about the same work, which balances members whose data differ by
 //            orders of magnitude;
-//   accept:  CTA = (member, 256-walker tile): partials summed in chunk order, FP64 log
-//            accept, write-back; accu: accepted count per member, per-CTA per-dim sums.
+//   accept:  CTA = (member, 256-walker tile): partials summed in chunk order, log-space
+//            accept (bay_accept_log), write-back; accu: accepted count per member, per-CTA per-dim sums.
 // Counter and key words per member are those of a single sampler with the member's seed,
 // so a member's trajectory is the trajectory that sampler would take (up to the order of
 // the log-density sums).
@@ -95,7 +95,7 @@ struct bay_batch_params {
     unsigned int pad;
 };
 
-// log u <= (dim - 1) log z + beta (ly - lx), decided as in FP64 (bay_accept_log); a
+// log u <= (dim - 1) log z + beta (ly - lx) in fp32 with bay_log_det (bay_accept_log); a
 // non-finite proposal is rejected
 __device__ __forceinline__ bool bay_batch_accept(float u2, float z, float ly, float lx,
                                                  float beta, unsigned int dim) {

@@ -8,7 +8,8 @@
 // bay_u01: the reference's u01fpt_oo_32_24 (cuda/rng/uniform-sampler.cu:11-13),
 // (0.5 + (i >> 9)) * 2^-23, an exactly representable value in (0, 1).
 //
-// bay_accept_log: the stretch move's accept test, shared by every kernel form.
+// bay_accept_log: the stretch move's accept test, shared by every kernel form, with
+// bay_log_det, a logarithm whose bits a CPU restatement reproduces.
 // bay_grid_sync: a bounded grid barrier for persistent cooperative launches.
 //
 // This header is compiled both by nvcc (into libbayadera_gb300.so) and by NVRTC
@@ -46,32 +47,43 @@ __device__ __forceinline__ float bay_u01(unsigned int i) {
     return __fmul_rn(__fadd_rn(0.5f, (float)(i >> 9)), 1.1920928955078125E-7f);
 }
 
+// Natural logarithm of a positive normal float in fp32, every operation rounded on its own
+// (no fast-math approximation, no FP64), so that a CPU restatement with the same
+// operations gives the same bits.  x = m 2^e with m in [sqrt(1/2), sqrt(2)); log m =
+// 2 atanh(s), s = (m - 1) / (m + 1), |s| <= 0.1716, by its series to s^11 (the first
+// omitted term is below 2^-28 of the result); e ln 2 with ln 2 split into a 16-bit head
+// and a tail.  About 1 ulp.
+__device__ __forceinline__ float bay_log_det(float x) {
+    const unsigned int b = __float_as_uint(x);
+    int e = (int)(b >> 23) - 127;
+    float m = __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421354f) {
+        m = __fmul_rn(m, 0.5f);
+        e += 1;
+    }
+    const float f = __fsub_rn(m, 1.0f);
+    const float s = __fdiv_rn(f, __fadd_rn(2.0f, f));
+    const float w = __fmul_rn(s, s);
+    float p = __fmaf_rn(w, 0.181818187f, 0.222222224f);      // 2/11, 2/9
+    p = __fmaf_rn(w, p, 0.285714298f);                         // 2/7
+    p = __fmaf_rn(w, p, 0.400000006f);                         // 2/5
+    p = __fmaf_rn(w, p, 0.666666687f);                         // 2/3
+    const float lm = __fmaf_rn(__fmul_rn(s, w), p, __fadd_rn(s, s));
+    const float fe = (float)e;
+    return __fmaf_rn(fe, 0.693145752f, __fmaf_rn(fe, 1.42860677e-06f, lm));
+}
+
 // The stretch move's Metropolis test (Goodman & Weare 2010, eq. 7) in log space:
 // accept iff log u <= dm1 log z + beta (ly - lx), dm1 = dimension - 1; a non-finite
-// proposal density is rejected.  The decision is that of the test in FP64 with FP64 logs.
-// An fp32 evaluation with the fast logs decides whenever its two sides differ by more than
-// a bound on its error; inside that band (a few walkers in 10^5) the FP64 logs decide.  So
-// the decision does not depend on the fast logs' rounding (a CPU restatement with FP64 logs
-// reproduces it), and the common path has no FP64 arithmetic.
-//   fp32 errors: __logf at most 2^-21.41 absolute on [0.5, 2] and 3 ulp elsewhere, i.e.
-//   below 2^-21.41 (1 + |log|); ly - lx and the product with beta each rounded once, below
-//   2^-23 |beta| (|ly| + |lx|); the fma and the subtraction of tol below 2^-23 of |rhs| and
-//   tol.  tol is at least twice their sum.  Non-finite sides make the band test false
-//   (inf - inf), so those cases go to the FP64 comparison too.
+// proposal density is rejected.  fp32 throughout with bay_log_det, each operation rounded
+// on its own: the decision is a fixed function of (u, z, ly, lx, beta), which the CPU
+// restatement reproduces bit for bit, and it needs neither fast-math logs nor FP64.
 __device__ __forceinline__ bool bay_accept_log(float u2, float z, float ly, float lx, float beta,
                                                unsigned int dm1) {
     if (!isfinite(ly)) return false;
-    const float fd = (float)dm1;
-    const float lz = __logf(z);
-    const float lhs = __logf(u2);
-    const float dl = beta * (ly - lx);
-    const float rhs = fmaf(fd, lz, dl);
-    const float tol = 0x1p-20f * (1.0f + fabsf(lhs) + fd * (1.0f + fabsf(lz)) + fabsf(rhs))
-        + 0x1p-21f * fabsf(beta) * (fabsf(ly) + fabsf(lx));
-    if (lhs < rhs - tol) return true;
-    if (lhs > rhs + tol) return false;
-    const double dl64 = (double)beta * ((double)ly - (double)lx);
-    return log((double)u2) <= (double)dm1 * log((double)z) + dl64;
+    const float dl = __fmul_rn(beta, __fsub_rn(ly, lx));
+    const float rhs = __fmaf_rn((float)dm1, bay_log_det(z), dl);
+    return bay_log_det(u2) <= rhs;
 }
 
 // Grid barrier k (k = 1, 2, ... within a launch) of a cooperative launch (every CTA

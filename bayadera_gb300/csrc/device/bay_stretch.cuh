@@ -25,8 +25,8 @@
 //     BAY_ROW_LEN, BAY_PREP_LEN, BAY_WPC (walkers per CTA)
 //   BAY_CTA        threads per CTA
 //   BAY_ACCEPT_REF 1: accept if u <= z^(D-1) exp(beta dl) in fp32 (the reference's
-//                  formula); 0 (default): log u <= (D-1) log z + beta dl, decided as in
-//                  FP64 (bay_accept_log).
+//                  formula); 0 (default): log u <= (D-1) log z + beta dl in fp32 with
+//                  the deterministic logarithm bay_log_det (bay_accept_log).
 //   BAY_STRETCH_REF 1: the stretch factor's 1/a by the compiler's fast division (the
 //                  reference's build flavour, -use_fast_math); 0 (default): IEEE 1/a.
 //                  Both keep the operation order the golden trajectories pin.

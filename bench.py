@@ -232,7 +232,7 @@ def cpu_port(threads, walkers=CPU_WALKERS):
     O.use_speed_build(True)
     P, _ = precision_matrix()
     r = O.Stretch("mvn_precision", DIM, walkers, P.reshape(-1), seed=SEED, threads=threads,
-                  flags=O.ACCEPT_LOG64)
+                  flags=O.ACCEPT_LOG)
     return O, r
 
 

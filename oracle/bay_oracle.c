@@ -527,7 +527,7 @@ void bo_logfn_all(const char* name, uint64_t walkers, uint32_t dim, uint32_t dat
  * (read out of bounds, or racing with the moving half, in the reference) read as 0 here
  * and in the library's compat kernels;
  * Y_i = S_ji + z (X_ki - S_ji) fused; accept if u2 <= z^(D-1) exp(beta (f(Y) - f(X_k)))
- * (fp32, as the reference), or in log space in FP64 with BO_ACCEPT_LOG64. */
+ * (fp32, as the reference), or in log space with BO_ACCEPT_LOG (the library's test). */
 /* Walker k's draws and proposal: z, u2 and Y (D floats). */
 static void stretch_propose_one(const bo_stretch_args* A, uint32_t k, float* Y, float* z_out,
                                 float* u2_out) {
@@ -560,17 +560,44 @@ static void stretch_propose_one(const bo_stretch_args* A, uint32_t k, float* Y, 
     *u2_out = u[2];
 }
 
+/* The library kernels' logarithm (bay_log_det), restated with the same operations, each
+ * rounded on its own (this build has -ffp-contract=off): x = m 2^e, m in [sqrt(1/2),
+ * sqrt(2)), log m = 2 atanh(s) with s = (m - 1)/(m + 1) by its series to s^11, plus e ln 2
+ * with ln 2 in two parts.  Same bits as the kernels for positive normal x. */
+float bo_log_det(float x) {
+    uint32_t b;
+    memcpy(&b, &x, sizeof b);
+    int e = (int)(b >> 23) - 127;
+    const uint32_t mb = (b & 0x007fffffu) | 0x3f800000u;
+    float m;
+    memcpy(&m, &mb, sizeof m);
+    if (m > 1.41421354f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float f = m - 1.0f;
+    const float s = f / (2.0f + f);
+    const float w = s * s;
+    float p = fmaf(w, 0.181818187f, 0.222222224f);
+    p = fmaf(w, p, 0.285714298f);
+    p = fmaf(w, p, 0.400000006f);
+    p = fmaf(w, p, 0.666666687f);
+    const float lm = fmaf(s * w, p, s + s);
+    const float fe = (float)e;
+    return fmaf(fe, 0.693145752f, fmaf(fe, 1.42860677e-06f, lm));
+}
+
 /* Walker k's accept test given its proposal's log density ly; on accept Y and ly replace
- * the walker's position and log density.  Returns the decision. */
+ * the walker's position and log density.  Returns the decision.  BO_ACCEPT_LOG: the
+ * library's default test, log u <= (D-1) log z + beta (ly - lx) in fp32 with bo_log_det;
+ * else the reference's u <= z^(D-1) exp(beta (ly - lx)). */
 static int stretch_accept_one(const bo_stretch_args* A, uint32_t k, const float* Y, float z,
                               float u2, float ly) {
     const uint32_t D = A->dim;
     int accepted;
-    if (A->flags & BO_ACCEPT_LOG64) {
-        const double lx = A->logfn_X[k];
-        accepted = isfinite(ly)
-            && (log((double)u2)
-                <= (double)(D - 1) * log((double)z) + (double)A->beta * ((double)ly - lx));
+    if (A->flags & BO_ACCEPT_LOG) {
+        const float dl = A->beta * (ly - A->logfn_X[k]);
+        accepted = isfinite(ly) && bo_log_det(u2) <= fmaf((float)(D - 1), bo_log_det(z), dl);
     } else {
         const float q = isfinite(ly)
             ? powf(z, (float)(D - 1)) * expf(A->beta * (ly - A->logfn_X[k])) : 0.0f;

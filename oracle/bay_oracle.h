@@ -72,7 +72,8 @@ void bo_logfn_all(const char* name, uint64_t walkers, uint32_t dim, uint32_t dat
 /* ---------------- stretch move ---------------- */
 enum {
     BO_PARTNER_ELEMENT = 1u << 0, /* reference Q1: j0 = (uint)(u*K*DIM) element offset */
-    BO_ACCEPT_LOG64    = 1u << 1, /* accept if log(u) <= (D-1)log z + beta*dlogfn in FP64 */
+    BO_ACCEPT_LOG      = 1u << 1, /* accept if log u <= (D-1) log z + beta dlogfn: the
+                                     library's fp32 test with its logarithm (bo_log_det) */
 };
 
 typedef struct {
@@ -95,6 +96,8 @@ typedef struct {
     int threads;
 } bo_stretch_args;
 
+/* The library kernels' fp32 logarithm, restated bit for bit (positive normal x). */
+float bo_log_det(float x);
 /* One half-step: stretch_move for k in [0, K) (nvidia-gtx-mcmc-stretch.cu:35-99). */
 void bo_stretch_half(const bo_stretch_args* a);
 /* The same half-step in two parts, for checking a kernel whose model density is evaluated

@@ -24,10 +24,10 @@ CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11"
 # is built on x86-64 here and on the GPU hosts' Arm cores), so no -march=native.
 LIB_FAST = os.path.join(HERE, "libbay_oracle_fast.so")
 CFLAGS_FAST = ["-O3", "-ffast-math", "-funroll-loops", "-fopenmp", "-fPIC", "-shared",
-               "-std=c11", "-DBO_SPEED"]
+               "-std=c11", "-DBO_SPEED", "-fno-finite-math-only"]
 
 PARTNER_ELEMENT = 1
-ACCEPT_LOG64 = 2
+ACCEPT_LOG = 2
 HIST_START1 = 1
 HIST_ZERO_LIMITS = 2
 
@@ -102,6 +102,8 @@ def lib():
         L.bo_logfn_all.argtypes = [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                    f32p, f32p, f32p, C.c_int]
         L.bo_stretch_half.argtypes = [C.POINTER(StretchArgs)]
+        L.bo_log_det.argtypes = [C.c_float]
+        L.bo_log_det.restype = C.c_float
         L.bo_stretch_propose.argtypes = [C.POINTER(StretchArgs), f32p, f32p, f32p]
         L.bo_stretch_accept.argtypes = [C.POINTER(StretchArgs), f32p, f32p, f32p, f32p]
         L.bo_accu_stats.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, f32p, u8p,
@@ -158,6 +160,11 @@ def sample_direct(kind, n, params, seed):
     else:
         raise ValueError(kind)
     return out
+
+
+def log_det(x):
+    """The library kernels' fp32 logarithm (bay_log_det), as the oracle restates it."""
+    return float(lib().bo_log_det(float(x)))
 
 
 # ------------------------------------------------------------------ models

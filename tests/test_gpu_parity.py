@@ -125,7 +125,7 @@ def _step_consistency(factory, oracle, model, oname, params, data_len, dim, W, s
     for t in range(steps):
         pos, lf, rng = s.export_state()
         r = oracle.Stretch(oname, dim, W, params, data_len=data_len, seed=int(rng[0]),
-                           flags=oracle.ACCEPT_LOG64)
+                           flags=oracle.ACCEPT_LOG)
         r.xs[:] = pos.reshape(-1)
         r.logfn[:] = lf
         r.bare_counter = int(rng[2])
@@ -229,7 +229,7 @@ def test_gemm_step_consistency_mvn50(factory, M, oracle):
     for t in range(4):
         pos, lf, rng_state = s.export_state()
         r = oracle.Stretch("mvn_precision", D, W, P.reshape(-1), seed=int(rng_state[0]),
-                           flags=oracle.ACCEPT_LOG64)
+                           flags=oracle.ACCEPT_LOG)
         r.xs[:] = pos.reshape(-1)
         r.logfn[:] = lf
         r.bare_counter = int(rng_state[2])

@@ -180,3 +180,20 @@ def test_beta_binomial_posterior_and_evidence(golden):
     diff = post - beta_log(conj, x)
     assert np.linalg.norm(diff - g["log_ratio"]) / math.sqrt(x.size) <= g["log_ratio_tol"]
     assert np.mean(np.exp(loglik)) == pytest.approx(g["evidence"], rel=1e-5)
+
+
+def test_log_det_accuracy(oracle):
+    """The accept test's fp32 logarithm (the kernels' bay_log_det, restated by the oracle
+    with the same operations): within 2 ulp of the correctly rounded log on the accept
+    test's domain -- uniforms (0.5 + i) 2^-23 and stretch factors in [1/8, 8]."""
+    import numpy as np
+    rng = np.random.default_rng(1)
+    xs = np.concatenate([(0.5 + rng.integers(0, 1 << 23, 20000)) * 2.0 ** -23,
+                         np.exp(rng.uniform(np.log(0.125), np.log(8.0), 20000)),
+                         [2.0 ** -24, 0.5, 1.0, 1.41421354, 1.4142137, 2.0, 8.0]]).astype(np.float32)
+    got = np.array([oracle.log_det(x) for x in xs], np.float32)
+    want = np.log(xs.astype(np.float64))
+    ulp = np.spacing(np.abs(want).astype(np.float32)).astype(np.float64)
+    err = np.abs(got.astype(np.float64) - want)
+    assert np.all(err <= 2 * ulp + 1e-45), float(np.max(err / ulp))
+    assert oracle.log_det(1.0) == 0.0
