@@ -1534,18 +1534,27 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     bool go = true;
     for (unsigned int si = 0; si < nsteps && go; ++si) {
     for (unsigned int half = h_lo; half < h_hi && go; ++half) {
-    if (PERSIST && (si | (half - h_lo)) != 0u)
-        go = bay_grid_barrier(P.ctl, gridDim.x, 2u * si + (half - h_lo), P.gbar_extra);
-    if (!go) break;
     const unsigned int step_off = P.step_off + si;
     const unsigned int step = step0 + step_off;
     float* X = P.xs + (LOGFN_ONLY ? 0 : (size_t)half * P.K * DIM);
     const float* S = P.xs + (size_t)(1u - half) * P.K * DIM;
+    // persistent: the group's first tile of this half-step loads its draws, own rows and
+    // log densities before the grid barrier.  The tile-to-group map is fixed, so only this
+    // group wrote those rows and densities (two half-steps back, ordered by its end-of-tile
+    // barrier); during the half-step the barrier closes, other CTAs only read them.
+    if (PERSIST && tile0 < ntiles) {
+        const unsigned int nt0 = nk - tile0 * BAY_TR_W < BAY_TR_W ? nk - tile0 * BAY_TR_W : BAY_TR_W;
+        if (!LOGFN_ONLY) proposals(tile0, half, step);
+        own_rows(X + (size_t)tile0 * BAY_TR_W * DIM, nt0);
+    }
+    if (PERSIST && (si | (half - h_lo)) != 0u)
+        go = bay_grid_barrier(P.ctl, gridDim.x, 2u * si + (half - h_lo), P.gbar_extra);
+    if (!go) break;
     for (unsigned int tile = tile0; tile < ntiles; tile += tstride) {
     const unsigned int k0 = tile * BAY_TR_W;
     const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
     float* const Xt = X + (size_t)k0 * DIM;
-    if (PERSIST) {
+    if (PERSIST && tile != tile0) {
         if (!LOGFN_ONLY) proposals(tile, half, step);
         own_rows(Xt, nt);
     }

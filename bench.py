@@ -453,7 +453,7 @@ def measure_config(name, steps, warmup, rows=0, forms=None, quick=False, factory
         forms = tuple(x for x in forms if x != "gemm")
     err = None
     # the fast form's kernel shape, chosen by the library's autotuner on this workload
-    tune = f.autotune(wl["model"], W, wl["params"], **kinds[wl["fast"]])
+    tune = tuned(lambda: f.autotune(wl["model"], W, wl["params"], **kinds[wl["fast"]]))
     for form in forms:
         shape = tune["shape"] if form == wl["fast"] else {}
         sf = f.mcmc_factory(wl["model"], **kinds[form], **shape)
@@ -466,7 +466,7 @@ def measure_config(name, steps, warmup, rows=0, forms=None, quick=False, factory
             # data exceeds the uint32 data length of the reference's model ABI).
             plain_rows = wl["plain_rows"]
             params = torch.cat([params[: plain_rows * wl["row_len"]], params[-wl["hyper_len"]:]])
-        s = sf.create_sampler(11, W, params)
+        s = graphs(sf.create_sampler(11, W, params))
         fast = form == wl["fast"]
         n_steps = steps if fast else 1
         B = wl["burn"] if fast else wl.get("plain_burn", wl["burn"])
@@ -557,6 +557,8 @@ def run_config(args):
     for k in ("plain_fp32", "speedup_vs_plain", "plain_fp32_note"):
         if k in rec:
             line[k] = rec[k]
+    if NO_GRAPHS:
+        line["config"]["graphs"] = "off (--no-graphs: kernels launched one by one)"
     print(json.dumps(line))
     return 0
 
@@ -583,10 +585,10 @@ def c4_members(M, n=512, seed=0):
     return out
 
 
-def measure_c4(steps, warmup, members=512):
+def measure_c4(steps, warmup, members=512, plain=True):
     """The 512-model batch: whole jobs (init, 1,000 burn-in and 2,000 accu steps of every
     member) timed with the L2 flushed before each, the plain single-model form on a sample
-    of the members; returns the config's record."""
+    of the members (unless plain is False); returns the config's record."""
     import torch
     from bayadera_gb300 import _native
     from bayadera_gb300 import models as M
@@ -601,8 +603,8 @@ def measure_c4(steps, warmup, members=512):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     f = GB300BayaderaFactory(device=0, wgs=1024, stream=stream.cuda_stream)
     fam = f.mcmc_factory(M.hierarchical_rows_batch_model(128), form="batch")
-    tune = fam.autotune_batch(mem)          # the work lists' shape, by timing (untimed here)
-    b = fam.create_batch(mem, tune["shape"])
+    tune = tuned(lambda: fam.autotune_batch(mem))   # the work lists' shape, by timing (untimed)
+    b = graphs(fam.create_batch(mem, tune["shape"]))
     seeds = [7 + i for i in range(len(mem))]
 
     def job(k):
@@ -665,7 +667,7 @@ def measure_c4(steps, warmup, members=512):
     # sampler (one plain kernel per half-step, the reference's structure), run in turn;
     # the full job's time is estimated as (members / sample) x the sample's time
     rng = np.random.default_rng(1)
-    sample = sorted(rng.choice(len(mem), size=16, replace=False).tolist())
+    sample = sorted(rng.choice(len(mem), size=16, replace=False).tolist()) if plain else []
     PB, PR = 50, 100
     compiled, t_plain = {}, 0.0
     for i in sample:
@@ -673,7 +675,7 @@ def measure_c4(steps, warmup, members=512):
         if m["dim"] not in compiled:
             compiled[m["dim"]] = f.mcmc_factory(M.hierarchical_rows_model(m["dim"] - 2),
                                                 form="plain")
-        s = compiled[m["dim"]].create_sampler(m["seed"], m["walkers"], m["params"])
+        s = graphs(compiled[m["dim"]].create_sampler(m["seed"], m["walkers"], m["params"]))
         s.init_position_normal(seeds[i], 0.0, 1.0)
         s.burn_in(5, 2.0)
         torch.cuda.synchronize()
@@ -689,8 +691,8 @@ def measure_c4(steps, warmup, members=512):
     for sf in compiled.values():
         sf.release()
     f.release()
-    t_plain_full = t_plain * len(mem) / len(sample)
-    plain_value = float(np.sum(W)) * (BURN4 + RUN4) / t_plain_full
+    plain_value = (float(np.sum(W)) * (BURN4 + RUN4) / (t_plain * len(mem) / len(sample))
+                   if sample else None)
     achieved = flop_step / t_step / 1e12
     rates = res["acceptance_rates"]
     return {"workload": "%d Gaussian hierarchical models, J log-U[2,128], n_j log-U[10,1000], "
@@ -713,7 +715,8 @@ def measure_c4(steps, warmup, members=512):
                          "ms_per_ensemble_step": 1e3 * t_step,
                          "flop_per_ensemble_step": flop_step},
             "logfn_err_vs_fp64": err, "autotune": tune,
-            "plain_fp32": plain_value, "speedup_vs_plain": value / plain_value,
+            "plain_fp32": plain_value,
+            "speedup_vs_plain": value / plain_value if plain_value else None,
             "plain_fp32_note": "%d of %d members, %d+%d steps each, time scaled to the full "
                                "job" % (len(sample), len(mem), PB, PR),
             "acceptance_rate_min": float(rates.min()), "acceptance_rate_max": float(rates.max())}
@@ -725,7 +728,8 @@ def run_c4(args):
     __graft_entry__.build()
     torch.cuda.set_device(0)
     with ClockSampler(0) as clocks:
-        rec = measure_c4(args.steps, args.warmup, args.members)
+        rec = measure_c4(args.steps, args.warmup, args.members,
+                         plain=not args.forms or "plain" in args.forms.split(","))
     line = {"metric": "walker-steps/s", "value": rec["value"], "unit": "walker-steps/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": rec["ms_per_job"], "higher_is_better": True, "scaling": "weak",
@@ -740,6 +744,8 @@ def run_c4(args):
                       "plain_sample": rec["plain_fp32_note"]},
             "clocks": clocks.summary()}
     line["config"]["l2"] = "flushed between timed jobs"
+    if NO_GRAPHS:
+        line["config"]["graphs"] = "off (--no-graphs: kernels launched one by one)"
     print(json.dumps(line))
     return 0
 
@@ -764,6 +770,26 @@ def measure_configs():
 
 
 # ------------------------------------------------------------------ GPU arm
+SHAPE = None   # --shape: a kernel shape given on the command line instead of the autotuner's
+NO_GRAPHS = False   # --no-graphs: every kernel launched on its own (for profiles)
+
+
+def graphs(sampler):
+    """The sampler or batch, with CUDA-graph chunks switched off under --no-graphs (ncu
+    profiles kernels launched on their own, not the kernel nodes of these graphs)."""
+    if NO_GRAPHS:
+        sampler.set_graphs(False)
+    return sampler
+
+
+def tuned(run_tuner):
+    """The autotuner's record for the fast form, or, with --shape, the given shape (the
+    tuner then does not run: a profile of one shape captures no tuning launches)."""
+    if SHAPE is not None:
+        return {"shape": dict(SHAPE), "given": True}
+    return run_tuner()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -785,7 +811,16 @@ def main():
     ap.add_argument("--forms", default="",
                     help="with --config: comma-separated subset of the forms to run "
                          "(tensor, gemm, tiled, plain), e.g. for a profile of one form")
+    ap.add_argument("--shape", default="",
+                    help="JSON kernel shape for the fast form, e.g. '{\"tc_groups\": 1}', "
+                         "used instead of the autotuner's choice (for profiles of one shape)")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch every kernel on its own instead of in CUDA-graph chunks (for "
+                         "ncu, which profiles no kernel node of these graphs)")
     args = ap.parse_args()
+    global SHAPE, NO_GRAPHS
+    SHAPE = json.loads(args.shape) if args.shape else None
+    NO_GRAPHS = args.no_graphs
     if args.impl == "reference":
         return run_reference(args)
     if args.config == "c4":
@@ -817,7 +852,7 @@ def main():
     model = M.mvn_precision_model(DIM)
     # the resident tensor-core kernels' shape (tile groups per CTA), chosen by the library's
     # autotuner on this workload before anything is timed
-    tune = f.autotune(model, WALKERS, dP, form="gemm", tensor=True)
+    tune = tuned(lambda: f.autotune(model, WALKERS, dP, form="gemm", tensor=True))
     sfs = {"tensor": f.mcmc_factory(model, form="gemm", tensor=True, **tune["shape"]),
            "gemm": f.mcmc_factory(model, form="gemm"),
            "plain": f.mcmc_factory(model, form="plain")}
@@ -864,7 +899,7 @@ def main():
 
     # headline: the GEMM form on the tensor cores (64-walker tiles, x'Px as a split-bf16
     # tcgen05 product against the resident precision matrix)
-    samp = sfs["tensor"].create_sampler(seed_base, WALKERS, dP)
+    samp = graphs(sfs["tensor"].create_sampler(seed_base, WALKERS, dP))
     launches0 = _native.launch_count()
     with ClockSampler(local) as clocks:
         value, t_total, results = timed_jobs(samp, args.steps, args.warmup)
@@ -879,12 +914,12 @@ def main():
     only = set(args.forms.split(",")) if args.forms else {"tensor", "gemm", "plain"}
     if "gemm" in only:
         # the fp32 SIMT GEMM form (64-walker tiles, register-blocked x'Px from shared memory)
-        samp_gemm = sfs["gemm"].create_sampler(seed_base, WALKERS, dP)
+        samp_gemm = graphs(sfs["gemm"].create_sampler(seed_base, WALKERS, dP))
         gemm_value, _, _ = timed_jobs(samp_gemm, max(1, min(args.steps, 2)), 1)
         samp_gemm.release()
     if "plain" in only:
         # the plain FP32 form (one thread per walker, the reference's kernel structure)
-        samp_plain = sfs["plain"].create_sampler(seed_base, WALKERS, dP)
+        samp_plain = graphs(sfs["plain"].create_sampler(seed_base, WALKERS, dP))
         plain_value, _, _ = timed_jobs(samp_plain, max(1, min(args.steps, 2)), 1)
         samp_plain.release()
 
@@ -912,7 +947,7 @@ def main():
     for k in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s2 = sfs["tensor"].create_sampler(seed_base + 31 * k, WALKERS, P.reshape(-1))
+        s2 = graphs(sfs["tensor"].create_sampler(seed_base + 31 * k, WALKERS, P.reshape(-1)))
         res, mean, var, hist = job(s2, seed_base + 31 * k)
         s2.release()
         e2e_times.append(time.perf_counter() - t0)
@@ -985,6 +1020,8 @@ def main():
         }
         if configs is not None:
             line["configs"] = configs
+        if NO_GRAPHS:
+            line["config"]["graphs"] = "off (--no-graphs: kernels launched one by one)"
         print(json.dumps(line))
     if samp is not None:
         samp.release()

@@ -401,7 +401,8 @@ typedef struct bay_batch_shape {
     uint32_t walkers_per_item;  /* default 64 */
     uint32_t chunk_floats;      /* default 4096 */
     uint32_t walkers_per_thread; /* 1, 2 or 4 walkers per thread of the row-term kernel, which
-                                    then shares each staged row between them; default 1 */
+                                    then shares each staged row between them; default 1.  A
+                                    member with fewer walkers per item gets padded slots */
 } bay_batch_shape;
 int bay_batch_create_shaped(bay_model* model, const bay_batch_member* members, uint32_t n,
                             const bay_batch_shape* shape, bay_batch** out);
