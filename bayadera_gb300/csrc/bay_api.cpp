@@ -267,8 +267,8 @@ size_t tile_smem_bytes(uint32_t row_len, uint64_t data_len) {
 // the barriers and flags, and 1 KB to align the operands to the 128-byte swizzle's
 // 1024-byte period.  Largest G (fewer re-reads of the matrix), then up to 6 stages.
 constexpr size_t kTcSmemMax = 232448;  // opt-in dynamic shared memory per CTA, sm_100 family
-constexpr uint32_t kTrWalkers = 64;
-constexpr uint32_t kTrGroups = 4;   // tile groups (256 threads each) per persistent CTA      // walkers per CTA of the resident tensor-core form
+constexpr uint32_t kTrWalkers = 64;  // walkers per tile of the resident tensor-core form
+constexpr uint32_t kTrGroups = 4;    // tile groups (256 threads each) per persistent CTA
 // want_g / want_s (0 = free) ask for a shape; false when no shape fits (or the asked one
 // does not).
 bool tc_plan(uint32_t features, uint32_t aux_len, uint32_t* G, uint32_t* S, size_t* smem,
@@ -389,6 +389,8 @@ struct bay_sampler {
     bool own_params = false;
     uint64_t n_params = 0, data_len = 0;
     float* part = nullptr;  // accu per-CTA sums of one chunk: kChunk x 2 x grid() x D
+    unsigned int* flow = nullptr;   // tcr persistent: per-tile half-step flags [2][tiles] and
+                                    // per-half-step gather counts [2 kChunk + 2]
     float* means = nullptr;
     uint64_t means_cap = 0;
     float* stage = nullptr;  // W*D floats: AoS staging
@@ -428,7 +430,8 @@ struct bay_sampler {
                    "cudaMemcpy(status)");
         cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
         if (st) fail(BAY_ERR_DEVICE, std::string("a kernel gave up waiting for ") +
-                                         ((st & 4u) ? "the other CTAs of its launch (grid barrier)"
+                                         ((st & 4u) ? "the other CTAs of its launch (grid barrier "
+                                                      "or half-step dependency)"
                                           : (st & 2u) ? "its tensor-core pipeline" : "its shared-memory copy") +
                                          " (device status " + std::to_string(st) + ")");
     }
@@ -529,6 +532,8 @@ struct bay_sampler {
         p.s_bl = s_bl;
         p.tc_fp = tc_fp;
         p.gbar_extra = gbar_extra;
+        p.pad_flow = 0;
+        p.flow = flow;
         return p;
     }
 
@@ -593,7 +598,9 @@ struct bay_sampler {
 
     // m <= kChunk steps: the kernel pairs with step offsets 0..m-1, the per-step means
     // of the accu steps (from the per-CTA sums), then the device step counter += m.
-    // persistent tcr: clear the grid barrier's words, then one cooperative launch of m steps
+    // persistent tcr: clear the abandon flag, the tiles' half-step flags and the gather
+    // counts, then one cooperative launch of m steps
+    size_t flow_words() const { return 2ull * ((K + kTrWalkers - 1) / kTrWalkers) + 2ull * kChunk + 2; }
     void launch_persistent(bool accu, uint32_t m, cudaStream_t st) {
         static_assert(offsetof(bay_ctl, gbar_count) == 128 && offsetof(bay_ctl, abort) == 256,
                       "grid barrier words of bay_ctl");
@@ -601,6 +608,7 @@ struct bay_sampler {
                                    offsetof(bay_ctl, abort) + sizeof(unsigned int) - offsetof(bay_ctl, gbar_count),
                                    st),
                    "memset(grid barrier)");
+        cuda_check(cudaMemsetAsync(flow, 0, sizeof(unsigned int) * flow_words(), st), "memset(flow)");
         if (st == ctx->stream) bay::count_launches(1);
         bay_stretch_params p = make_params(0, 0);
         void* args[] = {&p, &m};
@@ -1296,8 +1304,10 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                     cuda_check(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, c->device),
                                "cudaDeviceGetAttribute(SMs)");
                     // one CTA per SM: its TMEM columns are the only ones a resident CTA holds
-                    if (per_sm >= 1)
+                    if (per_sm >= 1) {
                         s->tr_grid = (uint32_t)std::min<uint64_t>(s->grid(), (uint64_t)n_sm);
+                        s->flow = (unsigned int*)c->alloc(sizeof(unsigned int) * s->flow_words());
+                    }
                 }
                 const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
                 const uint32_t kc = (m->gemm_features + 63) / 64;
@@ -1381,6 +1391,7 @@ int bay_sampler_release(bay_sampler* s) {
         c->release(s->counts);
         c->release(s->mix);
         c->release(s->gemm_lay);
+        c->release(s->flow);
         for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
         for (unsigned short* q : {s->tc_xh, s->tc_xl, s->s_bh, s->s_bl}) c->release(q);
         if (s->own_params) c->release((void*)s->params);

@@ -776,7 +776,7 @@ NO_GRAPHS = False   # --no-graphs: every kernel launched on its own (for profile
 
 def graphs(sampler):
     """The sampler or batch, with CUDA-graph chunks switched off under --no-graphs (ncu
-    profiles kernels launched on their own, not the kernel nodes of these graphs)."""
+    profiled kernels launched on their own, but none of these graphs' kernel nodes)."""
     if NO_GRAPHS:
         sampler.set_graphs(False)
     return sampler
@@ -816,7 +816,7 @@ def main():
                          "used instead of the autotuner's choice (for profiles of one shape)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every kernel on its own instead of in CUDA-graph chunks (for "
-                         "ncu, which profiles no kernel node of these graphs)")
+                         "ncu, which profiled none of these graphs' kernel nodes)")
     args = ap.parse_args()
     global SHAPE, NO_GRAPHS
     SHAPE = json.loads(args.shape) if args.shape else None
