@@ -389,8 +389,6 @@ struct bay_sampler {
     bool own_params = false;
     uint64_t n_params = 0, data_len = 0;
     float* part = nullptr;  // accu per-CTA sums of one chunk: kChunk x 2 x grid() x D
-    unsigned int* flow = nullptr;   // tcr persistent: per-tile half-step flags [2][tiles] and
-                                    // per-half-step gather counts [2 kChunk + 2]
     float* means = nullptr;
     uint64_t means_cap = 0;
     float* stage = nullptr;  // W*D floats: AoS staging
@@ -430,8 +428,7 @@ struct bay_sampler {
                    "cudaMemcpy(status)");
         cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
         if (st) fail(BAY_ERR_DEVICE, std::string("a kernel gave up waiting for ") +
-                                         ((st & 4u) ? "the other CTAs of its launch (grid barrier "
-                                                      "or half-step dependency)"
+                                         ((st & 4u) ? "the other CTAs of its launch (grid barrier)"
                                           : (st & 2u) ? "its tensor-core pipeline" : "its shared-memory copy") +
                                          " (device status " + std::to_string(st) + ")");
     }
@@ -532,8 +529,6 @@ struct bay_sampler {
         p.s_bl = s_bl;
         p.tc_fp = tc_fp;
         p.gbar_extra = gbar_extra;
-        p.pad_flow = 0;
-        p.flow = flow;
         return p;
     }
 
@@ -598,9 +593,7 @@ struct bay_sampler {
 
     // m <= kChunk steps: the kernel pairs with step offsets 0..m-1, the per-step means
     // of the accu steps (from the per-CTA sums), then the device step counter += m.
-    // persistent tcr: clear the abandon flag, the tiles' half-step flags and the gather
-    // counts, then one cooperative launch of m steps
-    size_t flow_words() const { return 2ull * ((K + kTrWalkers - 1) / kTrWalkers) + 2ull * kChunk + 2; }
+    // persistent tcr: clear the grid barrier's words, then one cooperative launch of m steps
     void launch_persistent(bool accu, uint32_t m, cudaStream_t st) {
         static_assert(offsetof(bay_ctl, gbar_count) == 128 && offsetof(bay_ctl, abort) == 256,
                       "grid barrier words of bay_ctl");
@@ -608,7 +601,6 @@ struct bay_sampler {
                                    offsetof(bay_ctl, abort) + sizeof(unsigned int) - offsetof(bay_ctl, gbar_count),
                                    st),
                    "memset(grid barrier)");
-        cuda_check(cudaMemsetAsync(flow, 0, sizeof(unsigned int) * flow_words(), st), "memset(flow)");
         if (st == ctx->stream) bay::count_launches(1);
         bay_stretch_params p = make_params(0, 0);
         void* args[] = {&p, &m};
@@ -1304,10 +1296,8 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
                     cuda_check(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, c->device),
                                "cudaDeviceGetAttribute(SMs)");
                     // one CTA per SM: its TMEM columns are the only ones a resident CTA holds
-                    if (per_sm >= 1) {
+                    if (per_sm >= 1)
                         s->tr_grid = (uint32_t)std::min<uint64_t>(s->grid(), (uint64_t)n_sm);
-                        s->flow = (unsigned int*)c->alloc(sizeof(unsigned int) * s->flow_words());
-                    }
                 }
                 const uint32_t auxs = m->gemm_aux_len ? m->gemm_aux_len : 1u;
                 const uint32_t kc = (m->gemm_features + 63) / 64;
@@ -1391,7 +1381,6 @@ int bay_sampler_release(bay_sampler* s) {
         c->release(s->counts);
         c->release(s->mix);
         c->release(s->gemm_lay);
-        c->release(s->flow);
         for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
         for (unsigned short* q : {s->tc_xh, s->tc_xl, s->s_bh, s->s_bl}) c->release(q);
         if (s->own_params) c->release((void*)s->params);

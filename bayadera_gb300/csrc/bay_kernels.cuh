@@ -54,8 +54,6 @@ struct bay_stretch_params {
     unsigned short* s_bl;
     unsigned int tc_fp;
     unsigned int gbar_extra;
-    unsigned int pad_flow;
-    unsigned int* flow;
 };
 
 enum {

@@ -65,7 +65,7 @@ struct bay_ctl {
     unsigned long long accepted;    // accu: accepted proposals since the last reset
     unsigned int status;            // nonzero: a device-detected error
     unsigned int pad0[21];
-    unsigned int gbar_count;        // grid barrier of persistent forms (byte 128): arrivals
+    unsigned int gbar_count;        // grid barrier of the persistent form (byte 128): arrivals
     unsigned int pad1[31];
     unsigned int abort;             //   abandon flag (byte 256); both cleared before each launch
     unsigned int pad2[31];
@@ -108,13 +108,8 @@ struct bay_stretch_params {
     unsigned short* s_bh;
     unsigned short* s_bl;
     unsigned int tc_fp;
-    unsigned int gbar_extra;        // persistent form: added to the targets of its half-step
-                                    // waits (0; 1 makes them run out, for tests)
-    unsigned int pad_flow;
-    // persistent form: [2][tiles] the last half-step of the launch (from 1) whose positions
-    // each tile of each half has written, then [2 steps + 2] per half-step of the launch the
-    // tiles that finished reading their partner rows; zero before each launch
-    unsigned int* flow;
+    unsigned int gbar_extra;        // persistent form: arrivals its grid barriers wait for beyond
+                                    // the grid (0; 1 makes them run out, for tests)
 };
 
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
@@ -1238,8 +1233,8 @@ __device__ __forceinline__ void bay_mma_n(unsigned int d, unsigned long long a, 
 // 8 consecutive floats (dims 8u .. 8u + 7) of a walker row: float4 loads when rows are
 // 16-byte aligned (DIM % 4 == 0), float2 when 8-byte aligned, else scalar; zero past DIM
 // or when !ok (no access at all).  In the persistent form other CTAs rewrote the rows
-// since this SM last read them: the acquire of the half-step wait, followed by the group
-// barrier, orders these loads after those writes.
+// since this SM last read them: the grid barrier's acquire orders these loads after those
+// writes.
 __device__ __forceinline__ void bay_tr_ld8(const float* row, unsigned int u, bool ok, float (&v)[8]) {
     const unsigned int d0 = 8u * u;
 #pragma unroll
@@ -1298,41 +1293,44 @@ __device__ __forceinline__ void bay_tr_put_a(unsigned int s_a, unsigned int w, u
 // a raised abort ends every wait at once.  Returns false when the launch is being
 // abandoned.  The count and the abort word are cleared before each launch.  `extra`
 // arrivals beyond the grid (nonzero only in tests) make every barrier run out.
-// Persistent form, half-step dependencies without a grid barrier.  A tile that wrote its
-// positions of half-step n publishes n in its flag (release); a tile whose partners it
-// draws waits for their tiles' flags (acquire) -- at most 64 tiles, not the whole grid.
-// A tile about to overwrite its rows first waits until every tile of the previous
-// half-step has finished reading them (a per-half-step count).  Waits are bounded like
-// the tensor-core pipeline's: after BAY_TC_WAIT_NS a thread raises the abandon flag and
-// status bit 4, and a raised flag ends every wait.
-__device__ __forceinline__ bool bay_flow_wait(const unsigned int* w, unsigned int target,
-                                              bay_ctl* ctl) {
-    volatile unsigned int* ab = &ctl->abort;
-    unsigned long long t0 = 0;
-    for (unsigned int it = 0;; ++it) {
-        unsigned int c;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(w) : "memory");
-        if (c >= target) return true;
-        if (it == 0u) t0 = bay_globaltimer();
-        __nanosleep(32);
-        if ((it & 63u) == 63u) {
-            if (*ab) return false;
-            if (bay_globaltimer() - t0 > BAY_TC_WAIT_NS) {
-                *ab = 1u;
-                atomicOr(&ctl->status, 4u);
-                return false;
+__device__ __forceinline__ bool bay_grid_barrier(bay_ctl* ctl, unsigned int nblocks, unsigned int k,
+                                                 unsigned int extra) {
+    __shared__ unsigned int s_go;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int go = 1u;
+        volatile unsigned int* ab = &ctl->abort;
+        if (*ab) {
+            go = 0u;
+        } else {
+            const unsigned int target = k * nblocks + extra;
+            __threadfence();                               // the CTA's writes before its arrival
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&ctl->gbar_count) : "memory");
+            unsigned long long t0 = bay_globaltimer();
+            for (unsigned int it = 0;; ++it) {
+                unsigned int c;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(&ctl->gbar_count) : "memory");
+                if (c >= target) break;
+                __nanosleep(32);
+                if ((it & 63u) == 63u) {
+                    if (*ab) {
+                        go = 0u;
+                        break;
+                    }
+                    if (bay_globaltimer() - t0 > BAY_TC_WAIT_NS) {
+                        *ab = 1u;
+                        atomicOr(&ctl->status, 4u);
+                        go = 0u;
+                        break;
+                    }
+                }
             }
+            __threadfence();
         }
+        s_go = go;
     }
-}
-// after a group barrier: the group's memory operations before it, then the flag / count
-__device__ __forceinline__ void bay_flow_publish(unsigned int* w, unsigned int v) {
-    __threadfence();
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(w), "r"(v) : "memory");
-}
-__device__ __forceinline__ void bay_flow_count(unsigned int* w) {
-    __threadfence();
-    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(w) : "memory");
+    __syncthreads();
+    return s_go != 0u;
 }
 
 // Named barrier of one 256-thread tile group (ids 1..4; id 0 is the CTA's __syncthreads)
@@ -1403,13 +1401,11 @@ __device__ __forceinline__ void bay_tr_sums_pass2(unsigned int tid, const float*
 // PERSIST = false: one half-step (P.half, P.step_off), tile blockIdx.x (G = 1), launched
 // with programmatic dependent launch.  PERSIST = true: a cooperative launch of m steps
 // (both halves each, step offsets P.step_off .. + m - 1) over a grid of co-resident CTAs
-// whose groups take tiles (g * gridDim.x + blockIdx.x) + k * gridDim.x * G of every
-// half-step; instead of a grid barrier between half-steps, a tile waits only for the tiles
-// its partners live in and, before it overwrites its rows, for the previous half-step's
-// readers (bay_flow_wait); barriers, TMEM and the image are set up once.  Every tile
-// computes what the per-launch form computes (same statistics slots), so the two forms
-// give identical results.  A group whose bounded wait gives up raises ctl->abort, which
-// ends every other group's waits, and the launch stops.
+// whose groups take tiles (g * gridDim.x + blockIdx.x) + k * gridDim.x * G of every half-step, with
+// a grid barrier between half-steps; barriers, TMEM and the image are set up once.  Every
+// tile computes what the per-launch form computes (same statistics slots), so the two
+// forms give identical results.  A group whose bounded wait gives up raises ctl->abort
+// and goes on to the next grid barrier, where the whole launch stops.
 template <bool ACCU, bool LOGFN_ONLY, bool PERSIST, unsigned int G>
 __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, unsigned int m) {
     // Shared memory: [matrix image][group 0: A hi atoms, lo atoms, Yw, red][group 1 ...].
@@ -1432,7 +1428,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     __shared__ float sHalf[G][BAY_TR_W][2];
     __shared__ unsigned char sAcc[G][BAY_TR_W];
     __shared__ __align__(8) unsigned long long sBar[1 + G];
-    __shared__ unsigned int sTmem, sOk[G], sWar[G];
+    __shared__ unsigned int sTmem, sOk[G];
 
     const unsigned int kind = ACCU ? 1u : 0u;
     const unsigned int g = G == 1u ? 0u : threadIdx.x >> 8;                // tile group
@@ -1542,25 +1538,25 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
         asm volatile("griddepcontrol.wait;" ::: "memory");
         asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     }
-    unsigned int* const flags = P.flow;                    // persistent: [2][ntiles]
-    unsigned int* const gcnt = P.flow + 2u * ntiles;       // persistent: [2 nsteps + 2]
     bool go = true;
     for (unsigned int si = 0; si < nsteps && go; ++si) {
     for (unsigned int half = h_lo; half < h_hi && go; ++half) {
-    const unsigned int n = 2u * si + (half - h_lo) + 1u;   // half-step of the launch
     const unsigned int step_off = P.step_off + si;
     const unsigned int step = step0 + step_off;
     float* X = P.xs + (LOGFN_ONLY ? 0 : (size_t)half * P.K * DIM);
     const float* S = P.xs + (size_t)(1u - half) * P.K * DIM;
     // persistent: the group's first tile of this half-step loads its draws, own rows and
-    // log densities before any wait.  The tile-to-group map is fixed, so only this group
-    // wrote those rows and densities (two half-steps back, ordered by its end-of-tile
-    // barrier); since then other tiles have only read them.
+    // log densities before the grid barrier.  The tile-to-group map is fixed, so only this
+    // group wrote those rows and densities (two half-steps back, ordered by its end-of-tile
+    // barrier); during the half-step the barrier closes, other CTAs only read them.
     if (PERSIST && tile0 < ntiles) {
         const unsigned int nt0 = nk - tile0 * BAY_TR_W < BAY_TR_W ? nk - tile0 * BAY_TR_W : BAY_TR_W;
         if (!LOGFN_ONLY) proposals(tile0, half, step);
         own_rows(X + (size_t)tile0 * BAY_TR_W * DIM, nt0);
     }
+    if (PERSIST && (si | (half - h_lo)) != 0u)
+        go = bay_grid_barrier(P.ctl, gridDim.x, 2u * si + (half - h_lo), P.gbar_extra);
+    if (!go) break;
     for (unsigned int tile = tile0; tile < ntiles; tile += tstride) {
     const unsigned int k0 = tile * BAY_TR_W;
     const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
@@ -1568,17 +1564,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     if (PERSIST && tile != tile0) {
         if (!LOGFN_ONLY) proposals(tile, half, step);
         own_rows(Xt, nt);
-    }
-    if (PERSIST && (n > 1u || P.gbar_extra != 0u)) {
-        // the partner rows: final once the tiles holding them published half-step n - 1
-        bool w_ok = true;
-        if (tid < nt)
-            w_ok = bay_flow_wait(&flags[(1u - half) * ntiles + sJ[g][tid] / BAY_TR_W],
-                                 n - 1u + P.gbar_extra, P.ctl);
-        if (!bay_gsync_and(g, w_ok)) {
-            go = false;
-            break;
-        }
     }
     bay_gsync(g);
     // 3. Y of the tile (walker-major rows of odd stride) from (walker, 8-dim unit) items:
@@ -1685,14 +1670,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
         }
         bay_mma_commit(bar_mma);   // also arrives with nothing issued (a failed wait)
         sOk[g] = ok;
-        if (PERSIST) {
-            // this tile's reads of the partner half are done (the group barrier before the
-            // MMAs); then, before its rows are overwritten, every tile of half-step n - 1
-            // must have finished reading them
-            bay_flow_count(&gcnt[n]);
-            sWar[g] = (n > 1u || P.gbar_extra != 0u)
-                ? (bay_flow_wait(&gcnt[n - 1u], ntiles + P.gbar_extra, P.ctl) ? 1u : 0u) : 1u;
-        }
     }
     if (tid < BAY_TR_W) {
         float pr[BAY_PREP_LEN];
@@ -1724,8 +1701,7 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     mma_par ^= 1u;
     const bool img_done = bay_tc_wait(bar_img, 0u, nullptr, status);
     // one verdict for the whole CTA (a wait that gave up in any thread fails the tile)
-    const bool ok = bay_gsync_and(g, mma_done && img_done) && sOk[g] != 0u &&
-                    (!PERSIST || sWar[g] != 0u);
+    const bool ok = bay_gsync_and(g, mma_done && img_done) && sOk[g] != 0u;
     bay_tc_fence_after();
     // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
     //    rows [NP/2 * (w / 4), + NP/2) in 8-column loads; the two halves then combine
@@ -1842,11 +1818,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
                 }
             }
         }
-        if (PERSIST) {
-            // the tile's half-step n is written: publish it to the tiles drawing partners here
-            bay_gsync(g);
-            if (tid == 0 && ok) bay_flow_publish(&flags[half * ntiles + tile], n);
-        }
         if (ACCU) {
             if (tid == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
             if (PERSIST && P.means_cap != 0) {
@@ -1875,10 +1846,9 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
         bay_gsync(g);
     }
     if (!ok) {
-        // a bounded wait gave up: no more tiles; the persistent form raises the abandon
-        // flag, which ends the other tiles' waits for this one
+        // a bounded wait gave up: no more tiles; the persistent form raises the abort flag
+        // and still meets the next grid barrier, which then stops the whole launch
         if (PERSIST && tid == 0) *(volatile unsigned int*)&P.ctl->abort = 1u;
-        go = false;
         break;
     }
     }   // tiles

@@ -537,9 +537,9 @@ class GB300Stretch:
         N.call("bay_sampler_set_persistent", self.handle, 1 if enabled else 0)
 
     def arm_barrier_timeout(self, enabled):
-        """Testing the device failure path: the persistent form's half-step waits want one
-        half-step more than any tile publishes, run out after their bounded wait and set
-        the status word (the next status check raises)."""
+        """Testing the device failure path: the persistent form's grid barriers wait for one
+        CTA more than the launch has, run out after their bounded wait and set the status
+        word (the next status check raises)."""
         N.call("bay_sampler_test_barrier_timeout", self.handle, 1 if enabled else 0)
 
     # ---------------------------------------------------------------- MCMC

@@ -325,10 +325,10 @@ int bay_sampler_set_graphs(bay_sampler* s, int enabled);
  * faster on GB300).  Both give the same results; other forms ignore it. */
 int bay_sampler_set_persistent(bay_sampler* s, int enabled);
 /* Testing the device failure path (no reference counterpart): with enabled != 0 the
- * persistent form's half-step waits want one half-step more than any tile publishes, so
- * the waiting threads give up after their bounded wait (2 s), raise the abort flag and the
- * status word, and the launch ends; the next status check returns BAY_ERR_DEVICE.  No
- * fault, trap or unbounded wait is involved. */
+ * persistent form's grid barriers wait for one more CTA than the launch has, so every CTA
+ * gives up after its bounded wait (2 s), raises the abort flag and the status word, and
+ * the launch ends; the next status check returns BAY_ERR_DEVICE.  No fault, trap or
+ * unbounded wait is involved. */
 int bay_sampler_test_barrier_timeout(bay_sampler* s, int enabled);
 
 /* ---------------------------------------------------------------- direct samplers

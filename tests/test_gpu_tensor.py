@@ -405,9 +405,8 @@ def test_tcr_run_sampler_matches_simt(factory, M, D):
 @pytest.mark.parametrize("D,W", [(50, 4096), (10, 89600), (64, 2 * (64 * 5 + 17))])
 def test_tcr_persistent_matches_per_launch(factory, M, D, W):
     """Resident tensor-core form: the persistent cooperative launch (a chunk of steps per
-    launch; each tile waits for its partners' tiles and, before it overwrites its rows, for
-    the previous half-step's readers; several tiles per group when the tiles outnumber the
-    resident groups: 700 tiles for 89,600 walkers) and one launch per
+    launch, grid barriers between half-steps, several tiles per CTA when the tiles
+    outnumber the resident CTAs: 700 tiles for 89,600 walkers) and one launch per
     half-step give bit-identical positions, log densities, per-step means and acceptance
     (a partial last tile in the third case)."""
     rng = np.random.default_rng(D)
@@ -432,12 +431,12 @@ def test_tcr_persistent_matches_per_launch(factory, M, D, W):
     assert a[3] == b[3]
 
 
-def test_tcr_dependency_wait_runs_out_and_context_recovers(factory, M):
-    """Device failure path without a fault: armed, the persistent form's half-step waits
-    want one half-step more than any tile publishes; the waiting threads give up after
-    their bounded wait (2 s), raise the abort flag and the status word, and the launch
-    ends.  The host reads the status (BAY_ERR_DEVICE, naming the half-step dependency); a
-    new sampler on the same context then runs normally."""
+def test_tcr_grid_barrier_runs_out_and_context_recovers(factory, M):
+    """Device failure path without a fault: armed, the persistent form's grid barriers wait
+    for one CTA more than the launch has; every CTA gives up after its bounded wait (2 s),
+    raises the abort flag and the status word, and the launch ends.  The host reads the
+    status (BAY_ERR_DEVICE, naming the grid barrier); a new sampler on the same context
+    then runs normally."""
     import time
     from bayadera_gb300._native import BayaderaError, BAY_ERR_DEVICE
     D, W = 10, 4096
@@ -448,7 +447,7 @@ def test_tcr_dependency_wait_runs_out_and_context_recovers(factory, M):
     s.init_position_normal(2, 0.0, 1.0)
     s.arm_barrier_timeout(True)
     t0 = time.perf_counter()
-    with pytest.raises(BayaderaError, match="half-step dependency") as e:
+    with pytest.raises(BayaderaError, match="grid barrier") as e:
         s.run_sampler(8, 2.0)
     assert e.value.code == BAY_ERR_DEVICE
     assert time.perf_counter() - t0 < 60.0
