@@ -199,6 +199,16 @@ __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P
 // (its rows split over L = 256 / TPR row groups, batches of 8 pairwise with a Kahan carry,
 // the row groups combined in xor-butterfly then warp order), so results depend on WPT only
 // through L.
+// With 4 walkers per thread and a model that also writes its row term over bay_v4
+// (BAY_TILE_TERM4), the thread's walkers are 4 tw .. 4 tw + 3 instead, stored interleaved
+// ([wpc / 4][dpad][4]: coordinate i of the four at one 16-byte address), and the term runs
+// once per row for all four -- one coordinate load where the scalar path makes four.  Each
+// walker's operations and sum order are those of the scalar path.
+#ifdef BAY_TILE_TERM4
+#define BAY_HAS_TERM4 1
+#else
+#define BAY_HAS_TERM4 0
+#endif
 template <int MODE, unsigned int WPT>  // MODE 0: move (K walkers), 2: log density of all W
 __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, unsigned int idx) {
     extern __shared__ __align__(16) float bay_bsm[];
@@ -209,7 +219,8 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
     const unsigned long long r0 = (unsigned long long)I.c * M.chunk_rows;
     const unsigned int nr = (unsigned int)(r0 + M.chunk_rows < M.rows ? M.chunk_rows : M.rows - r0);
     const unsigned int dpad = dim | 1u;   // odd walker stride: the lanes' x[j] hit distinct banks
-    float* Ys = bay_bsm;                                              // [wpc][dpad]
+    constexpr bool VEC = WPT == 4u && BAY_HAS_TERM4;
+    float* Ys = bay_bsm;                                    // [wpc][dpad] or [wpc / 4][dpad][4]
     float* Pr = Ys + ((wpc * dpad + 3u) & ~3u);                        // [wpc][BAY_PREP_LEN]
     float* Rs = Pr + ((wpc * BAY_PREP_LEN + 3u) & ~3u);                // [nr][BAY_ROW_STRIDE]
     float* red = Rs + M.chunk_rows * BAY_ROW_STRIDE;                   // [256][WPT][2]
@@ -218,11 +229,17 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
     // every load issued before any is used)
     const float* Yg = P.y + M.xs + (size_t)I.k0 * dim;
     for (unsigned int e = tid; e < wpc * dim; e += blockDim.x) {
-        const unsigned int ww = e / dim;
-        Ys[ww * dpad + (e - ww * dim)] = e < nv * dim ? Yg[e] : 0.0f;
+        const unsigned int ww = e / dim, d = e - ww * dim;
+        const float v = e < nv * dim ? Yg[e] : 0.0f;
+        if (VEC) Ys[((ww >> 2) * dpad + d) * 4u + (ww & 3u)] = v;
+        else Ys[ww * dpad + d] = v;
     }
-    for (unsigned int e = tid; e < wpc * BAY_PREP_LEN; e += blockDim.x)
-        Pr[e] = e < nv * BAY_PREP_LEN ? P.prep[((size_t)M.walker0 + I.k0) * BAY_PREP_LEN + e] : 0.0f;
+    for (unsigned int e = tid; e < wpc * BAY_PREP_LEN; e += blockDim.x) {
+        const float v = e < nv * BAY_PREP_LEN ? P.prep[((size_t)M.walker0 + I.k0) * BAY_PREP_LEN + e] : 0.0f;
+        const unsigned int ww = e / BAY_PREP_LEN, i = e - ww * BAY_PREP_LEN;
+        if (VEC) Pr[((ww >> 2) * BAY_PREP_LEN + i) * 4u + (ww & 3u)] = v;
+        else Pr[e] = v;
+    }
     const float* Rg = P.params + M.params + r0 * BAY_ROW_LEN;
     const unsigned int nf = nr * BAY_ROW_LEN;
 #pragma unroll 4
@@ -244,6 +261,50 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
         xw[j] = Ys + (tw + j * TPR) * dpad;
         pw[j] = Pr + (tw + j * TPR) * BAY_PREP_LEN;
     }
+#if BAY_HAS_TERM4
+    if constexpr (VEC) {
+        // the four walkers 4 tw .. 4 tw + 3 (zero rows past nv, their sums dropped)
+        const bay_v4* x4 = reinterpret_cast<const bay_v4*>(Ys) + tw * dpad;
+        const bay_v4* p4 = reinterpret_cast<const bay_v4*>(Pr) + tw * BAY_PREP_LEN;
+        bay_v4 s4 = {0.0f, 0.0f, 0.0f, 0.0f}, c4 = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (4u * tw < nv) {
+            unsigned int r = l;
+            for (; r + 7u * L < nr; r += 8u * L) {
+                bay_v4 t[8];
+#pragma unroll
+                for (unsigned int i = 0; i < 8u; ++i) {
+                    float rv[BAY_ROW_STRIDE];
+                    const float4* rp = reinterpret_cast<const float4*>(Rs + (r + i * L) * BAY_ROW_STRIDE);
+#pragma unroll
+                    for (int q = 0; q < BAY_ROW_STRIDE / 4; ++q) {
+                        const float4 v4 = rp[q];
+                        rv[4 * q] = v4.x;
+                        rv[4 * q + 1] = v4.y;
+                        rv[4 * q + 2] = v4.z;
+                        rv[4 * q + 3] = v4.w;
+                    }
+                    t[i] = BAY_TILE_TERM4(rv, x4, p4);
+                }
+#pragma unroll
+                for (unsigned int h = 4u; h >= 1u; h >>= 1)
+#pragma unroll
+                    for (unsigned int i = 0; i < h; ++i) t[i] = bay_v4_add_rn(t[i], t[i + h]);
+                const bay_v4 yk = bay_v4_sub_rn(t[0], c4);
+                const bay_v4 s2 = bay_v4_add_rn(s4, yk);
+                c4 = bay_v4_sub_rn(bay_v4_sub_rn(s2, s4), yk);
+                s4 = s2;
+            }
+            for (; r < nr; r += L) {
+                const bay_v4 yk = bay_v4_sub_rn(BAY_TILE_TERM4(Rs + r * BAY_ROW_STRIDE, x4, p4), c4);
+                const bay_v4 s2 = bay_v4_add_rn(s4, yk);
+                c4 = bay_v4_sub_rn(bay_v4_sub_rn(s2, s4), yk);
+                s4 = s2;
+            }
+        }
+        sum[0] = s4.x; sum[1 % WPT] = s4.y; sum[2 % WPT] = s4.z; sum[3 % WPT] = s4.w;
+        cmp[0] = c4.x; cmp[1 % WPT] = c4.y; cmp[2 % WPT] = c4.z; cmp[3 % WPT] = c4.w;
+    } else
+#endif
     if (tw < nv) {      // walkers past nv are zero rows in Ys/Pr: their sums are dropped
         unsigned int r = l;
         // batches of 8 rows summed pairwise per walker, each batch added with Kahan
@@ -310,8 +371,9 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
     }
     __syncthreads();
     if (tid < nv) {
-        // walker tid = tw' + j' TPR: its partials sit at lane tw' % 32 of the warps holding tw'
-        const unsigned int twp = tid % TPR, jp = tid / TPR;
+        // walker tid = tw' + j' TPR (4 tw' + j' on the vector path): its partials sit at lane
+        // tw' % 32 of the warps holding tw'
+        const unsigned int twp = VEC ? tid >> 2 : tid % TPR, jp = VEC ? tid & 3u : tid / TPR;
         const unsigned int stride = TPR < 32u ? 1u : TPR / 32u;   // warps between its copies
         bay_bcf a;
         a.hi = 0.0f;

@@ -135,4 +135,27 @@ __device__ __forceinline__ bool bay_grid_sync(unsigned int* count, unsigned int*
     return s_go != 0u;
 }
 
+// bay_v4: the values of four walkers, for row terms written over their number type (the
+// batched engine's 4-walker path).  Each operator applies the scalar operator lane by lane,
+// so a term gives every walker the bits its scalar form gives.
+struct __align__(16) bay_v4 {
+    float x, y, z, w;
+};
+__device__ __forceinline__ bay_v4 operator+(bay_v4 a, bay_v4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+__device__ __forceinline__ bay_v4 operator-(bay_v4 a, bay_v4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+__device__ __forceinline__ bay_v4 operator*(bay_v4 a, bay_v4 b) { return {a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w}; }
+__device__ __forceinline__ bay_v4 operator+(float a, bay_v4 b) { return {a + b.x, a + b.y, a + b.z, a + b.w}; }
+__device__ __forceinline__ bay_v4 operator-(float a, bay_v4 b) { return {a - b.x, a - b.y, a - b.z, a - b.w}; }
+__device__ __forceinline__ bay_v4 operator*(float a, bay_v4 b) { return {a * b.x, a * b.y, a * b.z, a * b.w}; }
+__device__ __forceinline__ bay_v4 operator+(bay_v4 a, float b) { return {a.x + b, a.y + b, a.z + b, a.w + b}; }
+__device__ __forceinline__ bay_v4 operator-(bay_v4 a, float b) { return {a.x - b, a.y - b, a.z - b, a.w - b}; }
+__device__ __forceinline__ bay_v4 operator*(bay_v4 a, float b) { return {a.x * b, a.y * b, a.z * b, a.w * b}; }
+// lane-wise IEEE add and subtract, never contracted (the engine's sums)
+__device__ __forceinline__ bay_v4 bay_v4_add_rn(bay_v4 a, bay_v4 b) {
+    return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w)};
+}
+__device__ __forceinline__ bay_v4 bay_v4_sub_rn(bay_v4 a, bay_v4 b) {
+    return {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z), __fsub_rn(a.w, b.w)};
+}
+
 #endif

@@ -36,3 +36,10 @@ inline REAL hrows_logpdf(const uint32_t data_len, const uint32_t hyper_len,
     return res + hrows_walker(n, params + data_len, hyper_len, dim, x);
 }
 }
+// batch form, four walkers at once: x4[i] holds coordinate i of the four walkers (one
+// 16-byte load per row for all four); the same operations as hrows_term, lane by lane
+inline bay_v4 hrows_term4(const REAL* row, const bay_v4* x4, const bay_v4* prep4) {
+    const bay_v4 d = row[0] - x4[(uint32_t)row[1]];
+    return row[2] * d * d;
+}
+#define BAY_TILE_TERM4 hrows_term4
