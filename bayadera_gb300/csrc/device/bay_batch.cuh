@@ -200,11 +200,11 @@ __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P
 // the row groups combined in xor-butterfly then warp order), so results depend on WPT only
 // through L.
 // With 4 walkers per thread and a model that also writes its row term over bay_v4
-// (BAY_TILE_TERM4), the thread's walkers are 4 tw .. 4 tw + 3 instead, stored interleaved
+// (BAY_BATCH_TERM4), the thread's walkers are 4 tw .. 4 tw + 3 instead, stored interleaved
 // ([wpc / 4][dpad][4]: coordinate i of the four at one 16-byte address), and the term runs
 // once per row for all four -- one coordinate load where the scalar path makes four.  Each
 // walker's operations and sum order are those of the scalar path.
-#ifdef BAY_TILE_TERM4
+#ifdef BAY_BATCH_TERM4
 #define BAY_HAS_TERM4 1
 #else
 #define BAY_HAS_TERM4 0
@@ -283,7 +283,7 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
                         rv[4 * q + 2] = v4.z;
                         rv[4 * q + 3] = v4.w;
                     }
-                    t[i] = BAY_TILE_TERM4(rv, x4, p4);
+                    t[i] = BAY_BATCH_TERM4(rv, x4, p4);
                 }
 #pragma unroll
                 for (unsigned int h = 4u; h >= 1u; h >>= 1)
@@ -295,7 +295,7 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
                 s4 = s2;
             }
             for (; r < nr; r += L) {
-                const bay_v4 yk = bay_v4_sub_rn(BAY_TILE_TERM4(Rs + r * BAY_ROW_STRIDE, x4, p4), c4);
+                const bay_v4 yk = bay_v4_sub_rn(BAY_BATCH_TERM4(Rs + r * BAY_ROW_STRIDE, x4, p4), c4);
                 const bay_v4 s2 = bay_v4_add_rn(s4, yk);
                 c4 = bay_v4_sub_rn(bay_v4_sub_rn(s2, s4), yk);
                 s4 = s2;

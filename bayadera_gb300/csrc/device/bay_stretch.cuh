@@ -2108,21 +2108,48 @@ __device__ __forceinline__ void bay_tile_begin(const bay_stretch_params& P, bay_
 // pairs), the copies begun by bay_tile_begin.  Every thread of the CTA calls it.  Returns
 // false (and sets the status) when a bounded wait for a copy gave up; out is then
 // incomplete.
+// With BAY_TILE_TERM4 (the model's row term over bay_v4) and BAY_WPC a multiple of 4, a
+// thread serves the four walkers 4 s .. 4 s + 3 of walker slot s = t % (BAY_WPC / 4) on row
+// group t / (BAY_WPC / 4): one row load per four walkers, four times the row groups.
+#if defined(BAY_TILE_TERM4) && (BAY_WPC % 4 == 0)
+#define BAY_TILE_VEC 1
+typedef bay_v4 bay_tval;
+#define BAY_TVAL_ZERO {0.0f, 0.0f, 0.0f, 0.0f}
+#define BAY_TVAL_ADD(a, b) bay_v4_add_rn(a, b)
+#define BAY_TVAL_SUB(a, b) bay_v4_sub_rn(a, b)
+#define BAY_TVAL_TERM(row, pv) BAY_TILE_TERM4(row, pv)
+#else
+#define BAY_TILE_VEC 0
+typedef float bay_tval;
+#define BAY_TVAL_ZERO 0.0f
+#define BAY_TVAL_ADD(a, b) __fadd_rn(a, b)
+#define BAY_TVAL_SUB(a, b) __fsub_rn(a, b)
+#define BAY_TVAL_TERM(row, pv) BAY_TILE_TERM(row, pv)
+#endif
 __device__ __forceinline__ bool bay_tiled_logfn_rows(const bay_stretch_params& P,
                                                     const float (*prep)[BAY_PREP_LEN],
                                                     bay_cf (*red)[BAY_WPC], bay_cf* out,
                                                     bay_tile_sync* sy) {
     extern __shared__ __align__(128) float bay_tsm[];
     unsigned int& sOk = sy->ok;
-    constexpr unsigned int L = BAY_CTA / BAY_WPC;       // row groups
-    const unsigned int tid = threadIdx.x, w = tid % BAY_WPC, l = tid / BAY_WPC;
+    constexpr unsigned int WV = BAY_TILE_VEC ? 4u : 1u;     // walkers per thread
+    constexpr unsigned int WS = BAY_WPC / WV;               // walker slots
+    constexpr unsigned int L = BAY_CTA / WS;                // row groups
+    const unsigned int tid = threadIdx.x, w = tid % WS, l = tid / WS;
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     const unsigned long long nch = (n_rows + BAY_TILE_CHUNK_ROWS - 1) / BAY_TILE_CHUNK_ROWS;
     const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(&sy->bar[0]);
+#if BAY_TILE_VEC
+    bay_v4 pv[BAY_PREP_LEN];
+#pragma unroll
+    for (int i = 0; i < BAY_PREP_LEN; ++i)
+        pv[i] = {prep[4u * w][i], prep[4u * w + 1u][i], prep[4u * w + 2u][i], prep[4u * w + 3u][i]};
+#else
     float pv[BAY_PREP_LEN];
 #pragma unroll
     for (int i = 0; i < BAY_PREP_LEN; ++i) pv[i] = prep[w][i];
-    float sum = 0.0f, cmp = 0.0f;
+#endif
+    bay_tval sum = BAY_TVAL_ZERO, cmp = BAY_TVAL_ZERO;
     for (unsigned long long c = 0; c < nch; ++c) {
         const unsigned int b = (unsigned int)(c & 1ull);
         float* R = bay_tsm + b * BAY_TILE_CHUNK;
@@ -2139,37 +2166,45 @@ __device__ __forceinline__ bool bay_tiled_logfn_rows(const bay_stretch_params& P
         if (sOk == 0u) break;
         unsigned int r = l;
         for (; r + 7u * L < nr; r += 8u * L) {
-            float t[8];
+            bay_tval t[8];
 #pragma unroll
-            for (unsigned int i = 0; i < 8u; ++i) t[i] = BAY_TILE_TERM(R + (r + i * L) * BAY_ROW_LEN, pv);
+            for (unsigned int i = 0; i < 8u; ++i) t[i] = BAY_TVAL_TERM(R + (r + i * L) * BAY_ROW_LEN, pv);
 #pragma unroll
             for (unsigned int h = 4u; h >= 1u; h >>= 1)
 #pragma unroll
-                for (unsigned int i = 0; i < h; ++i) t[i] = __fadd_rn(t[i], t[i + h]);
-            const float y = __fsub_rn(t[0], cmp);
-            const float s2 = __fadd_rn(sum, y);
-            cmp = __fsub_rn(__fsub_rn(s2, sum), y);
+                for (unsigned int i = 0; i < h; ++i) t[i] = BAY_TVAL_ADD(t[i], t[i + h]);
+            const bay_tval y = BAY_TVAL_SUB(t[0], cmp);
+            const bay_tval s2 = BAY_TVAL_ADD(sum, y);
+            cmp = BAY_TVAL_SUB(BAY_TVAL_SUB(s2, sum), y);
             sum = s2;
         }
         for (; r < nr; r += L) {
-            const float y = __fsub_rn(BAY_TILE_TERM(R + r * BAY_ROW_LEN, pv), cmp);
-            const float s2 = __fadd_rn(sum, y);
-            cmp = __fsub_rn(__fsub_rn(s2, sum), y);
+            const bay_tval y = BAY_TVAL_SUB(BAY_TVAL_TERM(R + r * BAY_ROW_LEN, pv), cmp);
+            const bay_tval s2 = BAY_TVAL_ADD(sum, y);
+            cmp = BAY_TVAL_SUB(BAY_TVAL_SUB(s2, sum), y);
             sum = s2;
         }
         __syncthreads();                                // buffer b is free again
         if (tid == 0 && c + 2 < nch) bay_tile_issue(P, c + 2, R, bar0 + 8u * b);
     }
     const bool ok = sOk != 0u;
-    // the lanes of a walker (lane bits above the walker bits) by an xor butterfly, then
-    // the warps in order
-    bay_cf v;
-    v.hi = sum;
-    v.lo = -cmp;
-#pragma unroll
-    for (unsigned int o = 16u; o >= BAY_WPC && o >= 1u; o >>= 1) v = bay_cadd(v, bay_cf_shfl_xor(v, o));
+    // the lanes of a walker slot (lane bits above the slot bits) by an xor butterfly, then
+    // the warps in order; walker 4 s + j of slot s at red[warp][4 s + j] (vector path)
     const unsigned int lane = tid & 31u, warp = tid >> 5;
-    if (lane < BAY_WPC) red[warp][lane] = v;
+#pragma unroll
+    for (unsigned int j = 0; j < WV; ++j) {
+        bay_cf v;
+#if BAY_TILE_VEC
+        v.hi = j == 0u ? sum.x : j == 1u ? sum.y : j == 2u ? sum.z : sum.w;
+        v.lo = -(j == 0u ? cmp.x : j == 1u ? cmp.y : j == 2u ? cmp.z : cmp.w);
+#else
+        v.hi = sum;
+        v.lo = -cmp;
+#endif
+#pragma unroll
+        for (unsigned int o = 16u; o >= WS && o >= 1u; o >>= 1) v = bay_cadd(v, bay_cf_shfl_xor(v, o));
+        if (lane < WS) red[warp][WV * lane + j] = v;
+    }
     __syncthreads();
     if (tid < BAY_WPC) {
         bay_cf s = red[0][tid];

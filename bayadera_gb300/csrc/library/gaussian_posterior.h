@@ -29,3 +29,10 @@ inline REAL gaussian_posterior_walker(const uint64_t n_rows, const REAL* h,
     return (REAL)n_rows * gaussian_log_scale(x[1]) + gaussian_posterior_prior(0, hyper_len, h, dim, x);
 }
 }
+// data-tiled form, four walkers at once (prep4[i]: prep value i of the four walkers); the
+// same operations as gaussian_posterior_term, lane by lane
+inline bay_v4 gaussian_posterior_term4(const REAL* row, const bay_v4* prep4) {
+    const bay_v4 d = row[0] - prep4[0];
+    return d * d * prep4[1];
+}
+#define BAY_TILE_TERM4 gaussian_posterior_term4

@@ -42,4 +42,4 @@ inline bay_v4 hrows_term4(const REAL* row, const bay_v4* x4, const bay_v4* prep4
     const bay_v4 d = row[0] - x4[(uint32_t)row[1]];
     return row[2] * d * d;
 }
-#define BAY_TILE_TERM4 hrows_term4
+#define BAY_BATCH_TERM4 hrows_term4
