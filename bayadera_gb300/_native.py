@@ -66,7 +66,7 @@ class ModelDesc(C.Structure):
                 ("gemm_offset", C.c_uint64), ("gemm_rows", C.c_uint64),
                 ("gemm_aux_col", C.c_uint32), ("gemm_aux_len", C.c_uint32),
                 ("tc_subtiles", C.c_uint32), ("tc_stages", C.c_uint32),
-                ("tc_groups", C.c_uint32)]
+                ("tc_groups", C.c_uint32), ("tile_slices", C.c_uint32)]
 
 
 class SamplerInfo(C.Structure):
@@ -82,7 +82,7 @@ class BatchMember(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("walkers_per_cta", C.c_uint32), ("cta_threads", C.c_uint32),
                 ("tc_subtiles", C.c_uint32), ("tc_stages", C.c_uint32),
-                ("tc_groups", C.c_uint32),
+                ("tc_groups", C.c_uint32), ("tile_slices", C.c_uint32),
                 ("candidates", C.c_uint32), ("from_cache", C.c_uint32),
                 ("us_per_step", C.c_double), ("default_us_per_step", C.c_double)]
 

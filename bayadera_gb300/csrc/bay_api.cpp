@@ -211,6 +211,7 @@ struct bay_model {
     CUlibrary lib = nullptr;
     CUkernel k_bare = nullptr, k_accu = nullptr, k_logfn = nullptr;
     uint32_t dim = 0, params_size = 0, form = 0, cta = 256, wpc = 1, flags = 0;
+    uint32_t tslices = 1;   // tiled form: row slices per walker group
     // GEMM form layout of A (see bay_model_desc)
     uint32_t gemm_features = 0, gemm_block = 0, gemm_ld = 0, gemm_aux_col = 0, gemm_aux_len = 0;
     uint32_t prep_len = 1;
@@ -389,6 +390,8 @@ struct bay_sampler {
     bool own_params = false;
     uint64_t n_params = 0, data_len = 0;
     float* part = nullptr;  // accu per-CTA sums of one chunk: kChunk x 2 x grid() x D
+    float* t_part = nullptr;         // tiled form, row slices: [K][slices] (hi, lo) partials
+    unsigned int* t_ticket = nullptr;  // tiled form, row slices: [grid()] slice tickets
     float* means = nullptr;
     uint64_t means_cap = 0;
     float* stage = nullptr;  // W*D floats: AoS staging
@@ -445,7 +448,7 @@ struct bay_sampler {
     bool tcr = false;   // tensor cores, matrix resident (one launch per half-step, or
                         // one persistent cooperative launch per chunk of steps)
     uint32_t tr_g = 1;          // tcr: tile groups per CTA of the per-launch move kernels
-    size_t smem_move = 0;       // tcr: their dynamic shared memory
+    size_t smem_move = 0;       // tcr: their dynamic shared memory; tiled: a row slice's
     bool persistent = false;    // tcr: the persistent form (when tr_smem != 0); measured
                                 // slower than programmatic dependent launches, so opt-in
     uint32_t tr_grid = 0;       // tcr: CTAs of the persistent form (all co-resident)
@@ -529,6 +532,10 @@ struct bay_sampler {
         p.s_bl = s_bl;
         p.tc_fp = tc_fp;
         p.gbar_extra = gbar_extra;
+        p.t_slices = model->form == BAY_FORM_TILED ? model->tslices : 1u;
+        p.pad_t = 0;
+        p.t_part = t_part;
+        p.t_ticket = t_ticket;
         return p;
     }
 
@@ -551,13 +558,13 @@ struct bay_sampler {
             at[0].id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
             at[0].value.programmaticStreamSerializationAllowed = 1;
             CUlaunchConfig cfg{};
-            cfg.gridDimX = tcr ? (grid() + tr_g - 1) / tr_g : grid();
+            cfg.gridDimX = tcr ? (grid() + tr_g - 1) / tr_g : grid() * model->tslices;
             cfg.gridDimY = 1;
             cfg.gridDimZ = 1;
             cfg.blockDimX = tcr ? 256 * tr_g : model->cta;
             cfg.blockDimY = 1;
             cfg.blockDimZ = 1;
-            cfg.sharedMemBytes = (unsigned)(tcr ? smem_move : smem);
+            cfg.sharedMemBytes = (unsigned)smem_move;
             cfg.hStream = (CUstream)st;
             cfg.attrs = at;
             cfg.numAttrs = pdl ? 1 : 0;
@@ -893,6 +900,7 @@ Codegen codegen(const bay_model_desc* d, uint32_t wgs) {
         wpc = d->walkers_per_cta ? d->walkers_per_cta : 8u;
         if (wpc > 32 || wpc > cta || (wpc & (wpc - 1)))
             fail(BAY_ERR_ARG, "walkers_per_cta must be a power of two, <= 32 and <= cta_threads");
+        if (d->tile_slices > 16) fail(BAY_ERR_ARG, "tile_slices must be 0..16");
         opts.push_back("-DBAY_TILED=1");
         opts.push_back("-DBAY_ROW_LEN=" + std::to_string(d->row_len));
         opts.push_back("-DBAY_PREP_LEN=" + std::to_string(pl));
@@ -996,6 +1004,7 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
         m->cta = g.cta;
         m->wpc = g.wpc;
         m->flags = d->flags;
+        if (d->form == BAY_FORM_TILED) m->tslices = d->tile_slices ? d->tile_slices : 1u;
         if (d->form == BAY_FORM_TILED) m->row_len = d->row_len;
         if (d->form == BAY_FORM_GEMM) {
             m->prep_len = d->prep_len ? d->prep_len : 1u;
@@ -1141,7 +1150,13 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
         s->D = m->dim;
         s->n_params = n_params;
         s->data_len = n_params - m->params_size;
-        if (m->form == BAY_FORM_TILED) s->smem = tile_smem_bytes(m->row_len, s->data_len);
+        if (m->form == BAY_FORM_TILED) {
+            s->smem = tile_smem_bytes(m->row_len, s->data_len);   // the log-density launch
+            // a move launch's CTA stages one row slice: (n / slices rounded up to 4) rows
+            const uint64_t n_rows = s->data_len / m->row_len, ns = m->tslices;
+            const uint64_t rps = ns > 1 ? (((n_rows + ns - 1) / ns + 3) & ~3ull) : n_rows;
+            s->smem_move = tile_smem_bytes(m->row_len, std::min(rps, n_rows) * m->row_len);
+        }
         if (m->form == BAY_FORM_GEMM) {
             const uint64_t block = m->gemm_block ? s->data_len : 0;
             const uint64_t block_len = m->gemm_block ? m->params_size : s->data_len;
@@ -1236,6 +1251,12 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
             s->logfn = (float*)c->alloc(sizeof(float) * walkers);
             s->ctl = (bay_ctl*)c->alloc(sizeof(bay_ctl));
             s->part = (float*)c->alloc(sizeof(float) * kChunk * 2 * (size_t)s->grid() * s->D);
+            if (m->form == BAY_FORM_TILED && m->tslices > 1) {
+                s->t_part = (float*)c->alloc(sizeof(float) * 2 * (size_t)s->K * m->tslices);
+                s->t_ticket = (unsigned int*)c->alloc(sizeof(unsigned int) * s->grid());
+                cuda_check(cudaMemsetAsync(s->t_ticket, 0, sizeof(unsigned int) * s->grid(), c->stream),
+                           "memset(tickets)");
+            }
             s->stats = (double*)c->alloc(sizeof(double) * 2 * s->D);
             cuda_check(cudaMemsetAsync(s->ctl, 0, sizeof(bay_ctl), c->stream), "memset");
             cuda_check(cudaMemsetAsync(s->xs, 0, sizeof(float) * (size_t)s->D * walkers, c->stream),
@@ -1340,6 +1361,8 @@ static int sampler_create(bay_model* m, uint32_t seed, uint64_t walkers, const f
             c->release(s->stats);
             c->release(s->means);
             c->release(s->gemm_lay);
+            c->release(s->t_part);
+            c->release(s->t_ticket);
             for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
             for (unsigned short* q : {s->tc_xh, s->tc_xl, s->s_bh, s->s_bl}) c->release(q);
             if (s->own_params) c->release((void*)s->params);
@@ -1381,6 +1404,8 @@ int bay_sampler_release(bay_sampler* s) {
         c->release(s->counts);
         c->release(s->mix);
         c->release(s->gemm_lay);
+        c->release(s->t_part);
+        c->release(s->t_ticket);
         for (float* q : {s->s_y, s->s_b, s->s_prep, s->s_w, s->s_zu, s->s_part}) c->release(q);
         for (unsigned short* q : {s->tc_xh, s->tc_xl, s->s_bh, s->s_bl}) c->release(q);
         if (s->own_params) c->release((void*)s->params);

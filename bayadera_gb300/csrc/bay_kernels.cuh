@@ -54,6 +54,10 @@ struct bay_stretch_params {
     unsigned short* s_bl;
     unsigned int tc_fp;
     unsigned int gbar_extra;
+    unsigned int t_slices;
+    unsigned int pad_t;
+    float* t_part;
+    unsigned int* t_ticket;
 };
 
 enum {

@@ -110,6 +110,13 @@ struct bay_stretch_params {
     unsigned int tc_fp;
     unsigned int gbar_extra;        // persistent form: arrivals its grid barriers wait for beyond
                                     // the grid (0; 1 makes them run out, for tests)
+    // data-tiled form split into t_slices row slices per walker group (1: none): each
+    // slice's CTA leaves its walkers' partial sums in t_part[k][slice] (hi, lo) and takes a
+    // ticket in t_ticket[group]; the last one combines them in slice order and decides
+    unsigned int t_slices;
+    unsigned int pad_t;
+    float* t_part;
+    unsigned int* t_ticket;
 };
 
 __device__ __forceinline__ float bay_stretch_z(float a, float u1) {
@@ -203,13 +210,14 @@ __device__ __forceinline__ float bay_cf_total(float a, bay_cf s) {
 // per-step ensemble means are reduced from these partials by a separate kernel.
 #define BAY_SUM_CHUNK 64
 __device__ void bay_accu_epilogue(const bay_stretch_params& P, bool accepted, bool valid,
-                                  const float* mine, float (*red)[BAY_SUM_CHUNK]) {
+                                  const float* mine, float (*red)[BAY_SUM_CHUNK],
+                                  unsigned int slot, unsigned int nslots) {
     const int n_acc = __syncthreads_count(accepted);
     if (threadIdx.x == 0 && n_acc) atomicAdd(&P.ctl->accepted, (unsigned long long)n_acc);
     if (P.means_cap == 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
-    float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * gridDim.x + blockIdx.x;
+    float* out = P.part + ((size_t)P.step_off * 2 + P.half) * DIM * nslots + slot;
 #pragma unroll
     for (int d0 = 0; d0 < DIM; d0 += BAY_SUM_CHUNK) {
 #pragma unroll
@@ -231,7 +239,7 @@ __device__ void bay_accu_epilogue(const bay_stretch_params& P, bool accepted, bo
                 y.lo = 0.0f;
                 s = bay_cadd(s, y);
             }
-            out[(size_t)(d0 + d) * gridDim.x] = __fadd_rn(s.hi, s.lo);
+            out[(size_t)(d0 + d) * nslots] = __fadd_rn(s.hi, s.lo);
         }
         __syncthreads();
     }
@@ -1949,7 +1957,7 @@ __device__ __forceinline__ void bay_stretch_plain(const bay_stretch_params& P) {
     }
     if (ACCU) {
         __shared__ float red[BAY_CTA / 32][BAY_SUM_CHUNK];
-        bay_accu_epilogue(P, accepted, valid, Y, red);
+        bay_accu_epilogue(P, accepted, valid, Y, red, blockIdx.x, gridDim.x);
     }
 }
 
@@ -2060,11 +2068,12 @@ __device__ __forceinline__ bool bay_tile_wait(unsigned int bar, unsigned int par
     }
 }
 
-// Chunk c of the rows -> buffer `buf` (floats): the 16-byte-aligned prefix by one bulk
-// copy completing on `bar`, issued by the calling thread.  Returns the chunk's floats.
+// Chunk c of the rows [rb, rb + n_rows) (rb a multiple of 4) -> buffer `buf` (floats): the
+// 16-byte-aligned prefix by one bulk copy completing on `bar`, issued by the calling
+// thread.  Returns the chunk's floats.
 __device__ __forceinline__ unsigned int bay_tile_issue(const bay_stretch_params& P, unsigned long long c,
-                                                       float* buf, unsigned int bar) {
-    const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
+                                                       float* buf, unsigned int bar,
+                                                       unsigned long long rb, unsigned long long n_rows) {
     const unsigned long long r0 = c * BAY_TILE_CHUNK_ROWS;
     const unsigned long long nr = n_rows - r0 < BAY_TILE_CHUNK_ROWS ? n_rows - r0 : BAY_TILE_CHUNK_ROWS;
     const unsigned int nf = (unsigned int)(nr * BAY_ROW_LEN);
@@ -2075,7 +2084,7 @@ __device__ __forceinline__ unsigned int bay_tile_issue(const bay_stretch_params&
     if (bytes)
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-            ::"r"((unsigned int)__cvta_generic_to_shared(buf)), "l"(P.params + r0 * BAY_ROW_LEN),
+            ::"r"((unsigned int)__cvta_generic_to_shared(buf)), "l"(P.params + (rb + r0) * BAY_ROW_LEN),
             "r"(bytes), "r"(bar) : "memory");
     return nf;
 }
@@ -2089,10 +2098,10 @@ struct bay_tile_sync {
 // Thread 0: the chunk barriers and the first two chunks' copies.  The data never change
 // while a sampler runs, so this may run before the launch waits for its predecessor.  The
 // CTA's threads wait on the barriers only after a __syncthreads that follows this.
-__device__ __forceinline__ void bay_tile_begin(const bay_stretch_params& P, bay_tile_sync* sy) {
+__device__ __forceinline__ void bay_tile_begin(const bay_stretch_params& P, bay_tile_sync* sy,
+                                               unsigned long long rb, unsigned long long n_rows) {
     extern __shared__ __align__(128) float bay_tsm[];
     if (threadIdx.x != 0) return;
-    const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     const unsigned long long nch = (n_rows + BAY_TILE_CHUNK_ROWS - 1) / BAY_TILE_CHUNK_ROWS;
     const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(&sy->bar[0]);
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
@@ -2100,7 +2109,8 @@ __device__ __forceinline__ void bay_tile_begin(const bay_stretch_params& P, bay_
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sy->ok = 1u;
     for (unsigned long long c = 0; c < 2 && c < nch; ++c)
-        bay_tile_issue(P, c, bay_tsm + (unsigned int)c * BAY_TILE_CHUNK, bar0 + 8u * (unsigned int)c);
+        bay_tile_issue(P, c, bay_tsm + (unsigned int)c * BAY_TILE_CHUNK, bar0 + 8u * (unsigned int)c,
+                       rb, n_rows);
 }
 
 // Sum over all data rows of BAY_TILE_TERM(row, prep of walker w) for the CTA's walkers
@@ -2129,14 +2139,14 @@ typedef float bay_tval;
 __device__ __forceinline__ bool bay_tiled_logfn_rows(const bay_stretch_params& P,
                                                     const float (*prep)[BAY_PREP_LEN],
                                                     bay_cf (*red)[BAY_WPC], bay_cf* out,
-                                                    bay_tile_sync* sy) {
+                                                    bay_tile_sync* sy, unsigned long long rb,
+                                                    unsigned long long n_rows) {
     extern __shared__ __align__(128) float bay_tsm[];
     unsigned int& sOk = sy->ok;
     constexpr unsigned int WV = BAY_TILE_VEC ? 4u : 1u;     // walkers per thread
     constexpr unsigned int WS = BAY_WPC / WV;               // walker slots
     constexpr unsigned int L = BAY_CTA / WS;                // row groups
     const unsigned int tid = threadIdx.x, w = tid % WS, l = tid / WS;
-    const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     const unsigned long long nch = (n_rows + BAY_TILE_CHUNK_ROWS - 1) / BAY_TILE_CHUNK_ROWS;
     const unsigned int bar0 = (unsigned int)__cvta_generic_to_shared(&sy->bar[0]);
 #if BAY_TILE_VEC
@@ -2160,7 +2170,7 @@ __device__ __forceinline__ bool bay_tiled_logfn_rows(const bay_stretch_params& P
         const bool done = bay_tile_wait(bar0 + 8u * b, (unsigned int)((c >> 1) & 1ull), &P.ctl->status);
         if (!done) sOk = 0u;
         if (nb < nf) {   // the chunk's last floats past its 16-byte-aligned prefix
-            for (unsigned int e = nb + tid; e < nf; e += BAY_CTA) R[e] = P.params[r0 * BAY_ROW_LEN + e];
+            for (unsigned int e = nb + tid; e < nf; e += BAY_CTA) R[e] = P.params[(rb + r0) * BAY_ROW_LEN + e];
         }
         __syncthreads();
         if (sOk == 0u) break;
@@ -2185,7 +2195,7 @@ __device__ __forceinline__ bool bay_tiled_logfn_rows(const bay_stretch_params& P
             sum = s2;
         }
         __syncthreads();                                // buffer b is free again
-        if (tid == 0 && c + 2 < nch) bay_tile_issue(P, c + 2, R, bar0 + 8u * b);
+        if (tid == 0 && c + 2 < nch) bay_tile_issue(P, c + 2, R, bar0 + 8u * b, rb, n_rows);
     }
     const bool ok = sOk != 0u;
     // the lanes of a walker slot (lane bits above the slot bits) by an xor butterfly, then
@@ -2232,10 +2242,16 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
     float* X = P.xs + (size_t)P.half * P.K * DIM;
     const float* S = P.xs + (size_t)(1u - P.half) * P.K * DIM;
     const float* hyper = P.params + P.data_len;
-    const unsigned int k0 = blockIdx.x * BAY_WPC;
+    // walker group g and row slice sl (slice-major CTAs); slices start on 4-row boundaries
+    const unsigned int NS = P.t_slices, groups = gridDim.x / NS;
+    const unsigned int g = blockIdx.x % groups, sl = blockIdx.x / groups;
+    const unsigned int k0 = g * BAY_WPC;
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
+    const unsigned long long rps = NS > 1u ? (((n_rows + NS - 1u) / NS + 3ull) & ~3ull) : n_rows;
+    const unsigned long long rb = (unsigned long long)sl * rps < n_rows ? (unsigned long long)sl * rps : n_rows;
+    const unsigned long long rn = n_rows - rb < rps ? n_rows - rb : rps;
     __shared__ bay_tile_sync sSync;
-    bay_tile_begin(P, &sSync);
+    bay_tile_begin(P, &sSync, rb, rn);
     // Launched with programmatic dependent launch: the draws, the walker's own row and log
     // density (this half last moved two launches back, final once the previous launch began
     // its work, which it did only after waiting for its own predecessor) come before the
@@ -2284,10 +2300,40 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
         }
     }
     __syncthreads();
-    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum, &sSync);
+    bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum, &sSync, rb, rn);
     bool accepted = false;
     const unsigned int t = threadIdx.x, k = k0 + t;
     const bool valid = t < BAY_WPC && k < P.K;
+    if (NS > 1u) {
+        // leave this slice's partials (NaN after a failed copy: the walker is then
+        // rejected), take the group's ticket; the last slice combines them in slice order
+        __shared__ unsigned int sLast;
+        float2* part = reinterpret_cast<float2*>(P.t_part);
+        if (valid) part[(size_t)k * NS + sl] = ok ? make_float2(sSum[t].hi, sSum[t].lo)
+                                                 : make_float2(__int_as_float(0x7fc00000), 0.0f);
+        __threadfence();
+        __syncthreads();
+        if (t == 0) sLast = atomicAdd(&P.t_ticket[g], 1u) == NS - 1u ? 1u : 0u;
+        __syncthreads();
+        if (sLast == 0u) return;
+        __threadfence();
+        if (t == 0) P.t_ticket[g] = 0u;             // for the next launch
+        if (valid) {
+            bay_cf a;
+            a.hi = 0.0f;
+            a.lo = 0.0f;
+            for (unsigned int q = 0; q < NS; ++q) {
+                const float2 v = __ldcg(&part[(size_t)k * NS + q]);
+                bay_cf b;
+                b.hi = v.x;
+                b.lo = v.y;
+                a = bay_cadd(a, b);
+            }
+            sSum[t] = a;
+        }
+        ok = true;
+        __syncthreads();
+    }
     float mine[DIM];
     if (valid) {
         if (ok) {
@@ -2305,7 +2351,7 @@ __device__ __forceinline__ void bay_stretch_tiled(const bay_stretch_params& P) {
             for (int i = 0; i < DIM; ++i) mine[i] = accepted ? sY[t][i] : X[(size_t)k * DIM + i];
         }
     }
-    if (ACCU) bay_accu_epilogue(P, accepted, valid, mine, red1);
+    if (ACCU) bay_accu_epilogue(P, accepted, valid, mine, red1, g, groups);
 }
 
 extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_stretch_bare(bay_stretch_params P) {
@@ -2325,7 +2371,7 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
     const unsigned long long n_rows = P.data_len / BAY_ROW_LEN;
     const unsigned int k0 = blockIdx.x * BAY_WPC;
     __shared__ bay_tile_sync sSync;
-    bay_tile_begin(P, &sSync);
+    bay_tile_begin(P, &sSync, 0ull, n_rows);
     if (threadIdx.x < BAY_WPC) {
         const unsigned int t = threadIdx.x, k = k0 + t;
         if (k < P.W) {
@@ -2344,7 +2390,7 @@ extern "C" __global__ void __launch_bounds__(BAY_CTA) bay_logfn_all(bay_stretch_
         }
     }
     __syncthreads();
-    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum, &sSync);
+    const bool ok = bay_tiled_logfn_rows(P, sPrep, sRed, sSum, &sSync, 0ull, n_rows);
     const unsigned int t = threadIdx.x, k = k0 + t;
     if (ok && t < BAY_WPC && k < P.W) P.logfn[k] = bay_cf_total(sW[t], sSum[t]);
 }

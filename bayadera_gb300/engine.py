@@ -93,9 +93,9 @@ class GB300BayaderaFactory:
 
     def autotune(self, model, walkers, params, form=None, tensor=False, positions=None):
         """bay_autotune: the fastest kernel shape of the model's form on this workload (the
-        tiled form's walkers per CTA and CTA threads, the streamed tensor-core form's
-        sub-tiles and stages), timed on the device; pass the result's shape keys to
-        mcmc_factory."""
+        tiled form's walkers per CTA, CTA threads and row slices, the streamed tensor-core
+        form's sub-tiles and stages, the resident one's tile groups), timed on the device;
+        pass the result's shape keys to mcmc_factory."""
         d, keep = model_desc(model, form, tensor=tensor)
         r = N.TuneResult()
         dp = _dev_ptr(params)
@@ -113,6 +113,8 @@ class GB300BayaderaFactory:
         shape = {}
         if r.walkers_per_cta:
             shape.update(walkers_per_cta=r.walkers_per_cta, cta_threads=r.cta_threads)
+        if r.tile_slices > 1:
+            shape.update(tile_slices=r.tile_slices)
         if r.tc_subtiles:
             shape.update(tc_subtiles=r.tc_subtiles, tc_stages=r.tc_stages)
         if r.tc_groups:
@@ -122,15 +124,18 @@ class GB300BayaderaFactory:
 
     def mcmc_factory(self, model, form=None, accept_ref=False, walkers_per_cta=0,
                      cta_threads=0, streaming=False, tensor=False, stretch_ref=False,
-                     partner_element=False, tc_subtiles=0, tc_stages=0, tc_groups=0):
+                     partner_element=False, tc_subtiles=0, tc_stages=0, tc_groups=0,
+                     tile_slices=0):
         """EngineFactory/mcmc-factory: compile the model's fused stretch kernels.  GEMM form:
         streaming=True streams the matrix even when it fits in shared memory; tensor=True
         streams it through the tensor cores (split bf16, fp32 accumulation).  Reference
         compatibility: accept_ref (fp32 accept formula), stretch_ref (the stretch factor's
-        fast-math expression), partner_element (the element-offset partner, quirk Q1)."""
+        fast-math expression), partner_element (the element-offset partner, quirk Q1).
+        Kernel shapes (0: the library's choice): walkers_per_cta, cta_threads, tile_slices
+        (tiled form); tc_subtiles, tc_stages, tc_groups (tensor-core GEMM form)."""
         return GB300StretchFactory(self, model, form, accept_ref, walkers_per_cta, cta_threads,
                                    streaming, tensor, stretch_ref, partner_element, tc_subtiles,
-                                   tc_stages, tc_groups)
+                                   tc_stages, tc_groups, tile_slices)
 
     def acor(self, data_matrix):
         return self.acor_engine.acor(data_matrix)
@@ -187,7 +192,7 @@ class GB300BayaderaFactory:
 
 def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_threads=0,
                streaming=False, tensor=False, stretch_ref=False, partner_element=False,
-               tc_subtiles=0, tc_stages=0, tc_groups=0):
+               tc_subtiles=0, tc_stages=0, tc_groups=0, tile_slices=0):
     """bay_model_desc of a DeviceDistributionModel; form 'plain' | 'tiled' | None (tiled
     when the model has a tiled form)."""
     if form is None:
@@ -224,6 +229,7 @@ def model_desc(model, form=None, accept_ref=False, walkers_per_cta=0, cta_thread
         d.row_len = t["row_len"]
         d.prep_len = t["prep_len"]
         d.walkers_per_cta = walkers_per_cta
+        d.tile_slices = tile_slices
     elif form == "batch":
         bt = model.batch
         if not bt:
@@ -322,23 +328,25 @@ class GB300DensityEngine:
 
 def check_model(model, form=None, wgs=1024, accept_ref=False, tensor=False, stretch_ref=False,
                 partner_element=False, walkers_per_cta=0, cta_threads=0, tc_subtiles=0,
-                tc_stages=0, tc_groups=0):
+                tc_stages=0, tc_groups=0, tile_slices=0):
     """Compile-check a model's fused kernels with NVRTC (no device needed)."""
     d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, tensor=tensor,
                          stretch_ref=stretch_ref, partner_element=partner_element,
-                         tc_subtiles=tc_subtiles, tc_stages=tc_stages, tc_groups=tc_groups)
+                         tc_subtiles=tc_subtiles, tc_stages=tc_stages, tc_groups=tc_groups,
+                         tile_slices=tile_slices)
     N.call("bay_model_check", C.byref(d), wgs)
 
 
 class GB300StretchFactory:
     def __init__(self, factory, model, form=None, accept_ref=False, walkers_per_cta=0,
                  cta_threads=0, streaming=False, tensor=False, stretch_ref=False,
-                 partner_element=False, tc_subtiles=0, tc_stages=0, tc_groups=0):
+                 partner_element=False, tc_subtiles=0, tc_stages=0, tc_groups=0,
+                 tile_slices=0):
         self.factory = factory
         self.model = model
         d, keep = model_desc(model, form, accept_ref, walkers_per_cta, cta_threads, streaming,
                              tensor, stretch_ref, partner_element, tc_subtiles, tc_stages,
-                             tc_groups)
+                             tc_groups, tile_slices)
         h = C.c_void_p()
         N.call("bay_model_compile", factory.ctx, C.byref(d), C.byref(h))
         self.handle = h

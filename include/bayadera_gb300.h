@@ -172,6 +172,11 @@ typedef struct bay_model_desc {
      * move kernels (1 or 2: one matrix copy and one tensor-memory allocation per group or
      * per pair); 0 = library choice (bay_autotune picks it). */
     uint32_t tc_groups;
+    /* BAY_FORM_TILED: row slices per walker group (1..16): each slice's CTA sums its rows,
+     * the group's last CTA combines the slices in order and decides.  More CTAs when the
+     * walkers are few; the sums' order depends on it.  0 = library choice (1; bay_autotune
+     * picks it). */
+    uint32_t tile_slices;
 } bay_model_desc;
 
 int bay_model_compile(bay_ctx* ctx, const bay_model_desc* desc, bay_model** out);
@@ -452,6 +457,7 @@ typedef struct bay_tune_result {
     uint32_t tc_subtiles;         /* streamed tensor-core GEMM form */
     uint32_t tc_stages;           /* streamed tensor-core GEMM form */
     uint32_t tc_groups;           /* tensor-core GEMM form, matrix resident */
+    uint32_t tile_slices;         /* BAY_FORM_TILED */
     uint32_t candidates;          /* shapes timed */
     uint32_t from_cache;
     double us_per_step;           /* the chosen shape: microseconds per ensemble step */

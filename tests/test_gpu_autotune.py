@@ -64,6 +64,38 @@ def test_tiled_shapes_match_fp64(factory, M, n):
         sf.release()
 
 
+@pytest.mark.parametrize("n", [10000, 30001])
+def test_tiled_row_slices(factory, M, n):
+    """The tiled form split into row slices (each slice's CTA sums its rows, the group's
+    last CTA combines them in slice order): log densities of the moved walkers within 2e-6
+    relative of FP64 for 2, 4 and 8 slices (30,001 rows: ragged slices over several staged
+    chunks); the same seed gives the same bits twice (the combine order does not depend
+    on which CTA finishes last); the run's per-step means agree with the mean of the
+    positions it ends on."""
+    params = _c1_params(n)
+    W = 2048
+    for sl in (2, 4, 8):
+        runs = []
+        for rep in range(2):
+            sf = factory.mcmc_factory(M.gaussian_posterior_model(), form="tiled", walkers_per_cta=8,
+                                      cta_threads=128, tile_slices=sl)
+            s = sf.create_sampler(9, W, params)
+            s.init_position(10, [2.0, 4.0, 1.0, 3.0])
+            s.burn_in(6, 2.0)
+            r = s.run_sampler(5, 2.0, return_means=True)
+            pos = s.positions().T.astype(np.float64)
+            want = _fp64_c1(params, pos)
+            err = np.abs(s.logfn() - want) / np.abs(want)
+            assert err.max() < 2e-6, (sl, err.max())
+            np.testing.assert_allclose(r["means"][:, -1], s.mean(), rtol=1e-5, atol=1e-6)
+            assert 0.3 < r["acceptance_rate"] < 0.95
+            runs.append((s.positions().copy(), s.logfn().copy()))
+            s.release()
+            sf.release()
+        np.testing.assert_array_equal(runs[0][0], runs[1][0])
+        np.testing.assert_array_equal(runs[0][1], runs[1][1])
+
+
 def test_resident_tile_groups_bit_identical(factory, M):
     """Resident tensor-core form, 50-D target: one or two tile groups per CTA give the same
     positions, log densities, per-step means and acceptance (a partial last tile)."""
@@ -130,6 +162,7 @@ def test_autotune_tiled_and_cache(factory, M):
           % (r["shape"], r["us_per_step"], r["default_us_per_step"], r["candidates"]))
     assert r["candidates"] >= 2 and not r["from_cache"]
     assert r["us_per_step"] <= r["default_us_per_step"]
+    assert r["shape"].get("tile_slices", 1) in (1, 2, 4, 8)
     assert (r["shape"]["walkers_per_cta"], r["shape"]["cta_threads"]) in (
         (8, 256), (2, 256), (4, 256), (4, 512), (4, 128), (8, 128), (16, 256), (32, 256),
         (8, 512), (16, 512), (32, 512), (32, 1024))
