@@ -268,6 +268,7 @@ size_t tile_smem_bytes(uint32_t row_len, uint64_t data_len) {
 // the barriers and flags, and 1 KB to align the operands to the 128-byte swizzle's
 // 1024-byte period.  Largest G (fewer re-reads of the matrix), then up to 6 stages.
 constexpr size_t kTcSmemMax = 232448;  // opt-in dynamic shared memory per CTA, sm_100 family
+constexpr size_t kBatchSmemMax = 160 * 1024;   // batched rows kernels: dynamic shared memory, at most
 constexpr uint32_t kTrWalkers = 64;  // walkers per tile of the resident tensor-core form
 constexpr uint32_t kTrGroups = 4;    // tile groups (256 threads each) per persistent CTA
 // want_g / want_s (0 = free) ask for a shape; false when no shape fits (or the asked one
@@ -1048,6 +1049,13 @@ int bay_model_compile(bay_ctx* c, const bay_model_desc* d, bay_model** out) {
                     for (int q = 0; q < 3; ++q)
                         cu_check(g_cu.LibraryGetKernel(&m->k_brun[i][q], m->lib, br[i][q]),
                                  "GetKernel(batch run)");
+                // row chunks of up to kBatchSmemMax bytes of shared memory (opt-in above 48 KB)
+                CUdevice dev = (CUdevice)c->device;
+                for (int q = 0; q < 3; ++q)
+                    for (CUkernel k : {m->k_gr_wpt[q][0], m->k_gr_wpt[q][1], m->k_brun[0][q], m->k_brun[1][q]})
+                        cu_check(g_cu.KernelSetAttribute(CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                         (int)kBatchSmemMax, k, dev),
+                                 "cuKernelSetAttribute(smem)");
                 cu_check(g_cu.LibraryGetKernel(&m->k_bmeans, m->lib, "bay_batch_means"), "GetKernel(means)");
                 m->row_len = d->row_len;
                 m->prep_len = d->prep_len ? d->prep_len : 1u;

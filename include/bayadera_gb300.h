@@ -399,12 +399,12 @@ int bay_batch_create(bay_model* model, const bay_batch_member* members, uint32_t
  * rows_per_thread sets a work item's row chunk (about 256 x rows_per_thread / walkers
  * rows), walkers_per_item caps the walkers of one item (a power of two <= 64; fewer when a
  * member's dimension or walker count asks for it), chunk_floats caps the staged floats of
- * a chunk (64..4096).  Results agree with any shape up to the order of the row sums.
+ * a chunk (64..16384).  Results agree with any shape up to the order of the row sums.
  * bay_batch_autotune picks a shape by timing. */
 typedef struct bay_batch_shape {
     uint32_t rows_per_thread;   /* default 128 */
     uint32_t walkers_per_item;  /* default 64 */
-    uint32_t chunk_floats;      /* default 4096 */
+    uint32_t chunk_floats;      /* default 4096, at most 16384 */
     uint32_t walkers_per_thread; /* 1, 2 or 4 walkers per thread of the row-term kernel, which
                                     then shares each staged row between them; default 1.  A
                                     member with fewer walkers per item gets padded slots */
