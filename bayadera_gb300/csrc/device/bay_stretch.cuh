@@ -1711,6 +1711,21 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     // one verdict for the whole CTA (a wait that gave up in any thread fails the tile)
     const bool ok = bay_gsync_and(g, mma_done && img_done) && sOk[g] != 0u;
     bay_tc_fence_after();
+    // One launch per half-step (FAST): the epilogue's warps 0 and 1 decide their walkers
+    // themselves once warps 4 and 5 have handed over the other half of the rows (a 128-
+    // thread named barrier), and write back their own rows; no group barrier follows.
+    // Meanwhile warps 2, 3, 6 and 7 finish the previous half-step's statistics (pass 1
+    // ended before the barrier above).
+    constexpr bool FAST = !PERSIST && !LOGFN_ONLY;
+    const unsigned int hand_id = 1u + G + g;        // named barriers 1..G are the groups'
+    if (FAST && prev_stats && BAY_TR_NG > 1u && (warp & 2u)) {
+        for (unsigned int d = (warp >> 2) * 64u + (warp & 1u) * 32u + lane; d < DIM; d += 128u) {
+            float a = 0.0f;
+#pragma unroll
+            for (unsigned int wg = 0; wg < BAY_TR_NG; ++wg) a = __fadd_rn(a, red2[wg * DIM + d]);
+            prev_out[(size_t)d * ntiles] = a;
+        }
+    }
     // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
     //    rows [NP/2 * (w / 4), + NP/2) in 8-column loads; the two halves then combine
     if (32u * (warp & 3u) < BAY_TR_W) {
@@ -1747,13 +1762,55 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
                 sum = t;
             }
         }
-        if (h) {                                        // second half of the rows
+        if (FAST) {
+            if (h) {                                    // hand the second half over
+                sHalf[g][wl][0] = sum;
+                sHalf[g][wl][1] = -cmp;
+                asm volatile("bar.arrive %0, 128;" ::"r"(hand_id) : "memory");
+            } else {
+                asm volatile("bar.sync %0, 128;" ::"r"(hand_id) : "memory");
+                // 7. accept walker wl, write back its row and log density
+                bool acc = false;
+                if (wl < nt && ok) {
+                    const unsigned int k = k0 + wl;
+                    bay_cf t, a, b;
+                    t.hi = sW[g][wl];
+                    t.lo = 0.0f;
+                    a.hi = sum;
+                    a.lo = -cmp;
+                    b.hi = sHalf[g][wl][0];
+                    b.lo = sHalf[g][wl][1];
+                    t = bay_cadd(t, bay_cadd(a, b));
+                    const float ly = __fadd_rn(t.hi, t.lo);
+                    acc = bay_accept(sU2[g][wl], sZ[g][wl], ly, sLx[g][wl], beta);
+                    if (acc) {
+                        P.logfn[(size_t)half * P.K + k] = ly;
+                        const float* yr = &Yw[wl * BAY_TR_DPAD];
+#pragma unroll 1
+                        for (unsigned int u = 0; u < NU; ++u) {
+                            float y[8];
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) y[i] = 8u * u + i < DIM ? yr[8u * u + i] : 0.0f;
+                            bay_tr_st8(Xt + (size_t)wl * DIM, u, y);
+                        }
+                    }
+                }
+                if (ACCU) {
+                    const unsigned int bal = __ballot_sync(0xffffffffu, acc);
+                    if (lane == 0 && bal) atomicAdd(&P.ctl->accepted, (unsigned long long)__popc(bal));
+                }
+            }
+        } else if (h) {                                 // second half of the rows
             sHalf[g][wl][0] = sum;
             sHalf[g][wl][1] = -cmp;
         } else {                                        // first half: red[wl], red[W + wl]
             red[wl] = sum;
             red[BAY_TR_W + wl] = -cmp;
         }
+    }
+    if (FAST) {
+        if (!ok) break;
+        continue;                                       // the tile is done (one per launch)
     }
     bay_tc_fence_before();
     bay_gsync(g);
