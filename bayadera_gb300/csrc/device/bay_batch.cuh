@@ -228,11 +228,22 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
     // stage the item's walkers, their prep values and its chunk of rows (coalesced,
     // every load issued before any is used)
     const float* Yg = P.y + M.xs + (size_t)I.k0 * dim;
-    for (unsigned int e = tid; e < wpc * dim; e += blockDim.x) {
-        const unsigned int ww = e / dim, d = e - ww * dim;
-        const float v = e < nv * dim ? Yg[e] : 0.0f;
-        if (VEC) Ys[((ww >> 2) * dpad + d) * 4u + (ww & 3u)] = v;
-        else Ys[ww * dpad + d] = v;
+    {
+        // warp by warp, no division by the runtime dimension: one walker per warp pass
+        // (lanes over its coordinates), or on the vector path four walkers per pass (lanes
+        // over (coordinate, walker): consecutive shared-memory words, four row segments)
+        const unsigned int lane = tid & 31u, nw = blockDim.x >> 5;
+        if (VEC) {
+            for (unsigned int G = tid >> 5; G < (wpc >> 2); G += nw)
+                for (unsigned int e = lane; e < 4u * dim; e += 32u) {
+                    const unsigned int d = e >> 2, ww = 4u * G + (e & 3u);
+                    Ys[(G * dpad + d) * 4u + (e & 3u)] = ww < nv ? Yg[(size_t)ww * dim + d] : 0.0f;
+                }
+        } else {
+            for (unsigned int ww = tid >> 5; ww < wpc; ww += nw)
+                for (unsigned int d = lane; d < dim; d += 32u)
+                    Ys[ww * dpad + d] = ww < nv ? Yg[(size_t)ww * dim + d] : 0.0f;
+        }
     }
     for (unsigned int e = tid; e < wpc * BAY_PREP_LEN; e += blockDim.x) {
         const float v = e < nv * BAY_PREP_LEN ? P.prep[((size_t)M.walker0 + I.k0) * BAY_PREP_LEN + e] : 0.0f;
@@ -241,11 +252,18 @@ __device__ __forceinline__ void bay_batch_rows_impl(const bay_batch_params& P, u
         else Pr[e] = v;
     }
     const float* Rg = P.params + M.params + r0 * BAY_ROW_LEN;
-    const unsigned int nf = nr * BAY_ROW_LEN;
-#pragma unroll 4
-    for (unsigned int e = tid; e < nf; e += blockDim.x) {
-        const unsigned int rr = e / BAY_ROW_LEN;
-        Rs[rr * BAY_ROW_STRIDE + (e - rr * BAY_ROW_LEN)] = __ldg(Rg + e);
+    // a row per thread: its BAY_ROW_LEN floats (adjacent lanes, adjacent rows: every byte
+    // of the loaded sectors used), stored as 16-byte words (padding zero)
+#pragma unroll 2
+    for (unsigned int rr = tid; rr < nr; rr += blockDim.x) {
+        const float* src = Rg + (size_t)rr * BAY_ROW_LEN;
+        float v[BAY_ROW_STRIDE];
+#pragma unroll
+        for (int i = 0; i < BAY_ROW_STRIDE; ++i) v[i] = i < BAY_ROW_LEN ? __ldg(src + i) : 0.0f;
+#pragma unroll
+        for (int q = 0; q < BAY_ROW_STRIDE / 4; ++q)
+            *reinterpret_cast<float4*>(Rs + rr * BAY_ROW_STRIDE + 4 * q) =
+                make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
     }
     __syncthreads();
     // walkers fastest: a warp's lanes are up to 32 walkers on the same row (a broadcast)
