@@ -96,6 +96,28 @@ def test_tiled_row_slices(factory, M, n):
         np.testing.assert_array_equal(runs[0][1], runs[1][1])
 
 
+@pytest.mark.parametrize("n", [0, 3, 257])
+def test_tiled_row_slices_few_rows(factory, M, n):
+    """Row slices with fewer rows than slices x 4 (empty slices; no data at all): the log
+    densities are the prior (n = 0) or the few rows' sum, within 2e-6 relative of FP64,
+    for 1 and 8 slices."""
+    rng = np.random.default_rng(n)
+    params = np.concatenate([rng.normal(3.0, 2.0, n).astype(np.float32),
+                             np.array([0.0, 10.0, 0.0, 20.0], np.float32)])
+    for sl in (1, 8):
+        sf = factory.mcmc_factory(M.gaussian_posterior_model(), form="tiled", walkers_per_cta=8,
+                                  cta_threads=256, tile_slices=sl)
+        s = sf.create_sampler(5, 512, params)
+        s.init_position(6, [2.0, 4.0, 1.0, 3.0])
+        s.burn_in(4, 2.0)
+        pos = s.positions().T.astype(np.float64)
+        want = _fp64_c1(params, pos)
+        err = np.abs(s.logfn() - want) / np.abs(want)
+        assert err.max() < 2e-6, (n, sl, err.max())
+        s.release()
+        sf.release()
+
+
 def test_resident_tile_groups_bit_identical(factory, M):
     """Resident tensor-core form, 50-D target: one or two tile groups per CTA give the same
     positions, log densities, per-step means and acceptance (a partial last tile)."""
