@@ -1545,16 +1545,6 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
         }
         asm volatile("griddepcontrol.wait;" ::: "memory");
         asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-        // accu: the previous half-step's rows of this tile (final now), which the
-        // statistics sum while the MMAs run, prefetched into L1 a 128-byte line per thread
-        if (ACCU && P.means_cap != 0 && (P.half == 1u || P.step_off > 0u) && tile0 < ntiles) {
-            const unsigned int k0 = tile0 * BAY_TR_W;
-            const unsigned int nt = nk - k0 < BAY_TR_W ? nk - k0 : BAY_TR_W;
-            const float* rows = P.xs + (size_t)(1u - P.half) * P.K * DIM + (size_t)k0 * DIM;
-            const unsigned int n_lines = (nt * DIM * 4u + 127u) / 128u;
-            for (unsigned int i = tid; i < n_lines; i += 256u)
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(rows + 32u * i) : "memory");
-        }
     }
     bool go = true;
     for (unsigned int si = 0; si < nsteps && go; ++si) {
