@@ -1700,7 +1700,8 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     float* const prev_out = prev_stats
         ? P.part + ((size_t)(half == 1u ? step_off : step_off - 1u) * 2 + (1u - half)) * DIM * ntiles + tile
         : nullptr;
-    if (prev_stats)
+    // (one launch per half-step: the statistics run on the warps idle in the epilogue)
+    if (prev_stats && PERSIST)
         bay_tr_sums_pass1(P.xs + (size_t)(1u - half) * P.K * DIM + (size_t)k0 * DIM, nt, tid,
                           red2, prev_out, ntiles);
     // every thread waits for the MMAs (bounded; the commit arrives even if none were issued)
@@ -1718,12 +1719,31 @@ __device__ __forceinline__ void bay_stretch_tcr(const bay_stretch_params& P, uns
     // ended before the barrier above).
     constexpr bool FAST = !PERSIST && !LOGFN_ONLY;
     const unsigned int hand_id = 1u + G + g;        // named barriers 1..G are the groups'
-    if (FAST && prev_stats && BAY_TR_NG > 1u && (warp & 2u)) {
-        for (unsigned int d = (warp >> 2) * 64u + (warp & 1u) * 32u + lane; d < DIM; d += 128u) {
-            float a = 0.0f;
+    if (FAST && prev_stats && (warp & 2u)) {
+        // warps 2, 3, 6, 7 (128 threads, idle in the epilogue): both passes of the previous
+        // half-step's statistics, the same slots and order as bay_tr_sums_pass1 / pass2,
+        // with a 128-thread named barrier between them
+        const unsigned int i0 = (warp >> 2) * 64u + (warp & 1u) * 32u + lane;
+        const float* rows = P.xs + (size_t)(1u - half) * P.K * DIM + (size_t)k0 * DIM;
+        for (unsigned int t = i0; t < BAY_TR_NG * DIM; t += 128u) {
+            const unsigned int wg = t / DIM, d = t - wg * DIM;
+            float v = 0.0f;
 #pragma unroll
-            for (unsigned int wg = 0; wg < BAY_TR_NG; ++wg) a = __fadd_rn(a, red2[wg * DIM + d]);
-            prev_out[(size_t)d * ntiles] = a;
+            for (unsigned int i = 0; i < BAY_TR_WG; ++i) {
+                const unsigned int w = wg * BAY_TR_WG + i;
+                if (w < nt) v = __fadd_rn(v, rows[(size_t)w * DIM + d]);
+            }
+            if (BAY_TR_NG == 1u) prev_out[(size_t)d * ntiles] = v;
+            else red2[t] = v;
+        }
+        if (BAY_TR_NG > 1u) {
+            asm volatile("bar.sync %0, 128;" ::"r"(1u + 2u * G + g) : "memory");
+            for (unsigned int d = i0; d < DIM; d += 128u) {
+                float a = 0.0f;
+#pragma unroll
+                for (unsigned int wg = 0; wg < BAY_TR_NG; ++wg) a = __fadd_rn(a, red2[wg * DIM + d]);
+                prev_out[(size_t)d * ntiles] = a;
+            }
         }
     }
     // 6. epilogue: warps 0, 1, 4, 5 read TMEM lanes 32 (w % 4) .. + 31 (walkers 0..63),
