@@ -137,6 +137,15 @@ __device__ __forceinline__ unsigned int bay_partner(float u0, unsigned int K) {
     return j < K ? j : K - 1;
 }
 
+// e / dim for e < 2^24 from a float reciprocal, corrected to the exact quotient (the float
+// product is within 1 of it): a few instructions instead of an integer division.
+__device__ __forceinline__ unsigned int bay_div_dim(unsigned int e, unsigned int dim, float inv_dim) {
+    unsigned int q = __float2uint_rz(__fmul_rn((float)e, inv_dim));
+    if (q * dim > e) --q;
+    else if ((q + 1u) * dim <= e) ++q;
+    return q;
+}
+
 template <int MODE>  // 0 bare, 1 accu, 2 log density of the current positions (all W)
 __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P, unsigned int idx) {
     __shared__ float sZ[256];
@@ -165,15 +174,20 @@ __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P
     }
     __syncthreads();
     // the tile's proposals: one contiguous block of nt * dim floats, element-wise
-    float* Y = P.y + M.xs + (size_t)T.k0 * dim;
-    const float* X = P.xs + M.xs + (MODE == 2 ? 0 : (size_t)P.half * M.K * dim) + (size_t)T.k0 * dim;
-    const float* S = P.xs + M.xs + (size_t)(1u - P.half) * M.K * dim;
+    // (plain loads, not the read-only path: the persistent launch rewrites the positions
+    // between its phases; the proposals are a separate buffer, hence __restrict__)
+    float* __restrict__ Y = P.y + M.xs + (size_t)T.k0 * dim;
+    const float* __restrict__ X = P.xs + M.xs + (MODE == 2 ? 0 : (size_t)P.half * M.K * dim) + (size_t)T.k0 * dim;
+    const float* __restrict__ S = P.xs + M.xs + (size_t)(1u - P.half) * M.K * dim;
     const unsigned int ne = nt * dim;
+    const float inv_dim = __frcp_rn((float)dim);
+    // unrolled so that several elements' loads are in flight
+#pragma unroll 4
     for (unsigned int e = tid; e < ne; e += blockDim.x) {
         if (MODE == 2) {
             Y[e] = X[e];
         } else {
-            const unsigned int w = e / dim, d = e - w * dim;
+            const unsigned int w = bay_div_dim(e, dim, inv_dim), d = e - w * dim;
             const float s = S[(size_t)sJ[w] * dim + d];
             Y[e] = __fmaf_rn(sZ[w], __fsub_rn(X[e], s), s);
         }
@@ -422,11 +436,14 @@ __device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P,
         bay_bcf s;
         s.hi = P.wterm[wk];
         s.lo = 0.0f;
-        const float* pp = P.part + M.part + 2 * (size_t)k * M.chunks;
+        const float2* pp = reinterpret_cast<const float2*>(P.part + M.part) + (size_t)k * M.chunks;
+        // in chunk order; unrolled so that several partials' loads are in flight
+#pragma unroll 4
         for (unsigned int c = 0; c < M.chunks; ++c) {
+            const float2 v = pp[c];
             bay_bcf p;
-            p.hi = pp[2 * c];
-            p.lo = pp[2 * c + 1];
+            p.hi = v.x;
+            p.lo = v.y;
             s = bay_bcadd(s, p);
         }
         const float ly = __fadd_rn(s.hi, s.lo);
@@ -436,13 +453,22 @@ __device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P,
             const size_t lk = (size_t)M.walker0 + (size_t)P.half * M.K + k;
             accepted = bay_batch_accept(P.zu[2 * wk + 1], P.zu[2 * wk], ly, P.logfn[lk],
                                         MODE == 1 ? 1.0f : P.ctl->beta, dim);
-            if (accepted) {
-                float* X = P.xs + M.xs + ((size_t)P.half * M.K + k) * dim;
-                const float* y = P.y + M.xs + (size_t)k * dim;
-                for (unsigned int d = 0; d < dim; ++d) X[d] = y[d];
-                P.logfn[lk] = ly;
-            }
+            if (accepted) P.logfn[lk] = ly;
         }
+    }
+    if (MODE == 2) return;
+    // the accepted walkers' rows, element-wise over the tile (coalesced, many in flight)
+    __shared__ unsigned char sAcc[256];
+    sAcc[tid] = accepted ? 1 : 0;
+    __syncthreads();
+    {
+        const unsigned int nt = nk - T.k0 < blockDim.x ? nk - T.k0 : blockDim.x;
+        float* __restrict__ Xt = P.xs + M.xs + ((size_t)P.half * M.K + T.k0) * dim;
+        const float* __restrict__ Yt = P.y + M.xs + (size_t)T.k0 * dim;
+        const float inv_dim = __frcp_rn((float)dim);
+#pragma unroll 4
+        for (unsigned int e = tid; e < nt * dim; e += blockDim.x)
+            if (sAcc[bay_div_dim(e, dim, inv_dim)]) Xt[e] = Yt[e];
     }
     if (MODE != 1) return;
     // accu: the member's accepted count and this CTA's per-dim sums of the moved walkers
@@ -457,6 +483,8 @@ __device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P,
         bay_bcf s;
         s.hi = 0.0f;
         s.lo = 0.0f;
+        // in walker order; unrolled so that several rows' loads are in flight
+#pragma unroll 8
         for (unsigned int w = 0; w < nt; ++w) {
             bay_bcf y;
             y.hi = Xc[(size_t)w * dim + d];

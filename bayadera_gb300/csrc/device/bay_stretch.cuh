@@ -744,6 +744,8 @@ __device__ __forceinline__ void bay_gemm_accept_impl(const bay_stretch_params& P
         bay_cf s;
         s.hi = 0.0f;
         s.lo = 0.0f;
+        // in walker order; unrolled so that several rows' loads are in flight
+#pragma unroll 8
         for (unsigned int w = 0; w < nv; ++w) {
             bay_cf y;
             y.hi = Xc[(size_t)w * DIM + d];
