@@ -14,7 +14,8 @@ inline REAL hrows_walker(const uint64_t n_rows, const REAL* h, const uint32_t hy
     const REAL mu = x[J], lt = x[J + 1];
     const REAL c = -0.5f * expf(-2.0f * lt);
     REAL s = 0.0f;
-    for (uint32_t j = 0; j < J; ++j) {
+#pragma unroll 8
+    for (uint32_t j = 0; j < J; ++j) {     // (unrolled: several coordinates' loads in flight)
         const REAL d = x[j] - mu;
         s = fmaf(d * d, c, s);
     }
