@@ -181,15 +181,28 @@ __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P
     const float* __restrict__ S = P.xs + M.xs + (size_t)(1u - P.half) * M.K * dim;
     const unsigned int ne = nt * dim;
     const float inv_dim = __frcp_rn((float)dim);
-    // unrolled so that several elements' loads are in flight
-#pragma unroll 4
-    for (unsigned int e = tid; e < ne; e += blockDim.x) {
-        if (MODE == 2) {
-            Y[e] = X[e];
-        } else {
-            const unsigned int w = bay_div_dim(e, dim, inv_dim), d = e - w * dim;
-            const float s = S[(size_t)sJ[w] * dim + d];
-            Y[e] = __fmaf_rn(sZ[w], __fsub_rn(X[e], s), s);
+    // 8 elements per thread per pass, all their loads issued before any is used
+    for (unsigned int e0 = tid; e0 < ne; e0 += 8u * blockDim.x) {
+        float xv[8], sv[8], zv[8];
+#pragma unroll
+        for (unsigned int i = 0; i < 8u; ++i) {
+            const unsigned int e = e0 + i * blockDim.x;
+            xv[i] = 0.0f;
+            sv[i] = 0.0f;
+            zv[i] = 0.0f;
+            if (e < ne) {
+                xv[i] = X[e];
+                if (MODE != 2) {
+                    const unsigned int w = bay_div_dim(e, dim, inv_dim), d = e - w * dim;
+                    sv[i] = S[(size_t)sJ[w] * dim + d];
+                    zv[i] = sZ[w];
+                }
+            }
+        }
+#pragma unroll
+        for (unsigned int i = 0; i < 8u; ++i) {
+            const unsigned int e = e0 + i * blockDim.x;
+            if (e < ne) Y[e] = MODE == 2 ? xv[i] : __fmaf_rn(zv[i], __fsub_rn(xv[i], sv[i]), sv[i]);
         }
     }
     __syncthreads();
