@@ -483,6 +483,9 @@ __device__ __forceinline__ void bay_batch_accept_impl(const bay_batch_params& P,
         for (unsigned int e = tid; e < nt * dim; e += blockDim.x)
             if (sAcc[bay_div_dim(e, dim, inv_dim)]) Xt[e] = Yt[e];
     }
+    // the persistent launch runs the next tile's accept in this CTA: sAcc is rewritten
+    // there only after every thread has read it here
+    __syncthreads();
     if (MODE != 1) return;
     // accu: the member's accepted count and this CTA's per-dim sums of the moved walkers
     const int n_acc = __syncthreads_count(accepted);

@@ -633,23 +633,31 @@ def measure_c4(steps, warmup, members=512, plain=True):
             ts.append(e0.elapsed_time(e1) / 1e3)
         return ts, _native.launch_count() - l0, r
 
+    def fp64_errors():
+        """FP64 error of the members' log densities after the last job (8 members, 64
+        walkers each)"""
+        errs = []
+        pos_all, lf_all = b.positions(), b.logfn()
+        for i in np.linspace(0, len(mem) - 1, 8).astype(int):
+            m = mem[i]
+            idx = np.linspace(0, m["walkers"] - 1, 64).astype(np.int64)
+            errs.append(_err(lf_all[i][idx], fp64_hrows(m["params"], m["rows"], pos_all[i][idx])))
+        return {"max_abs": max(e["max_abs"] for e in errs),
+                "median_abs": float(np.median([e["median_abs"] for e in errs])),
+                "max_rel": max(e["max_rel"] for e in errs),
+                "walkers": sum(e["walkers"] for e in errs), "members": 8}
+
+    # each launch mode's jobs, each checked against FP64 after its last job
     t_launch, l_launch, res_launch = timed(False)
+    err_launch = fp64_errors()
     t_persist, l_persist, res_persist = timed(True)
+    err_persist = fp64_errors()
     persistent = sum(t_persist) < sum(t_launch)
     times, launches, res = ((t_persist, l_persist, res_persist) if persistent
                             else (t_launch, l_launch, res_launch))
     b.set_persistent(persistent)
-    # FP64 error of the members' log densities after the last job (8 members, 64 walkers)
-    errs = []
-    pos_all, lf_all = b.positions(), b.logfn()
-    for i in np.linspace(0, len(mem) - 1, 8).astype(int):
-        m = mem[i]
-        idx = np.linspace(0, m["walkers"] - 1, 64).astype(np.int64)
-        errs.append(_err(lf_all[i][idx], fp64_hrows(m["params"], m["rows"], pos_all[i][idx])))
-    err = {"max_abs": max(e["max_abs"] for e in errs),
-           "median_abs": float(np.median([e["median_abs"] for e in errs])),
-           "max_rel": max(e["max_rel"] for e in errs), "walkers": sum(e["walkers"] for e in errs),
-           "members": 8}
+    err = dict(err_persist if persistent else err_launch)
+    err["other_launch_mode_max_rel"] = (err_launch if persistent else err_persist)["max_rel"]
     # time per ensemble step of the whole batch
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)

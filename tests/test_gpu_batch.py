@@ -197,6 +197,37 @@ def test_batch_persistent_matches_per_launch(family, M, shape):
         np.testing.assert_array_equal(x, y)
 
 
+def test_batch_persistent_many_tiles_per_cta(family, M):
+    """The persistent launch with several tiles and work items per CTA (900 small members:
+    900 accept tiles against at most one CTA per SM and a few per SM by occupancy), where a
+    phase's next tile reuses the CTA's shared memory: identical to three launches per
+    half-step, and every log density within 2e-5 relative of FP64."""
+    import bench
+    rng = np.random.default_rng(9)
+    mem = []
+    for i in range(900):
+        J = int(rng.integers(2, 6))
+        mem.append(_member(M, rng, J, 5, 12, 256, 500 + i))
+    out = {}
+    for persist in (False, True):
+        b = family.create_batch(mem, {"rows_per_thread": 32, "walkers_per_item": 64,
+                                      "walkers_per_thread": 4})
+        b.set_persistent(persist)
+        b.init_position_normal([7 + i for i in range(len(mem))], 0.0, 1.0)
+        b.burn_in(20, 2.0)
+        b.run_sampler(12, 2.0)
+        out[persist] = ([p.copy() for p in b.positions()], [l.copy() for l in b.logfn()])
+        b.release()
+    for x, y in zip(out[False][0], out[True][0]):
+        np.testing.assert_array_equal(x, y)
+    for x, y in zip(out[False][1], out[True][1]):
+        np.testing.assert_array_equal(x, y)
+    for i in range(0, 900, 97):
+        m, pos, lf = mem[i], out[True][0][i], out[True][1][i]
+        want = bench.fp64_hrows(m["params"], m["rows"], pos.astype(np.float64))
+        assert np.all(np.abs(lf - want) <= 2e-5 * np.abs(want) + 1e-3), i
+
+
 def test_batch_grid_barrier_runs_out_and_context_recovers(family, M):
     """Device failure path without a fault: armed, the persistent launch's grid barriers
     wait for one CTA more than the launch has; every CTA gives up after its bounded wait
