@@ -92,10 +92,7 @@ struct bay_batch_params {
     unsigned int n_tiles, n_items;  // move tiles and rows work items (the persistent launch)
     unsigned int gbar_extra;        // persistent launch: extra arrivals its barriers wait for
                                     // (0; 1 makes them run out, for tests)
-    unsigned int prop_round;        // propose: walkers per round of proposals staged in
-                                    // shared memory (rows of prop_dpad floats)
-    unsigned int prop_dpad;
-    unsigned int pad2;
+    unsigned int pad;
 };
 
 // log u <= (dim - 1) log z + beta (ly - lx) in fp32 with bay_log_det (bay_accept_log); a
@@ -182,59 +179,43 @@ __device__ __forceinline__ void bay_batch_propose_impl(const bay_batch_params& P
     float* __restrict__ Y = P.y + M.xs + (size_t)T.k0 * dim;
     const float* __restrict__ X = P.xs + M.xs + (MODE == 2 ? 0 : (size_t)P.half * M.K * dim) + (size_t)T.k0 * dim;
     const float* __restrict__ S = P.xs + M.xs + (size_t)(1u - P.half) * M.K * dim;
+    const unsigned int ne = nt * dim;
     const float inv_dim = __frcp_rn((float)dim);
-    const float* hyper = P.params + M.params + M.rows * BAY_ROW_LEN;
-    // rounds of R walkers: their proposals to device memory and to shared memory (rows of
-    // prop_dpad floats), then each walker's prep and walker term from its staged row
-    extern __shared__ __align__(16) float bay_bsm[];
-    const unsigned int R = P.prop_round, dp = P.prop_dpad;
-    for (unsigned int w0 = 0; w0 < nt; w0 += R) {
-        const unsigned int nr = nt - w0 < R ? nt - w0 : R;
-        const unsigned int eb = w0 * dim, ne = nr * dim;
-        // 8 elements per thread per pass, all their loads issued before any is used
-        for (unsigned int e0 = tid; e0 < ne; e0 += 8u * blockDim.x) {
-            float xv[8], sv[8], zv[8];
-            unsigned int wv[8];
+    // 8 elements per thread per pass, all their loads issued before any is used
+    for (unsigned int e0 = tid; e0 < ne; e0 += 8u * blockDim.x) {
+        float xv[8], sv[8], zv[8];
 #pragma unroll
-            for (unsigned int i = 0; i < 8u; ++i) {
-                const unsigned int e = e0 + i * blockDim.x;
-                xv[i] = 0.0f;
-                sv[i] = 0.0f;
-                zv[i] = 0.0f;
-                wv[i] = 0u;
-                if (e < ne) {
-                    wv[i] = bay_div_dim(e, dim, inv_dim);
-                    xv[i] = X[eb + e];
-                    if (MODE != 2) {
-                        const unsigned int d = e - wv[i] * dim;
-                        sv[i] = S[(size_t)sJ[w0 + wv[i]] * dim + d];
-                        zv[i] = sZ[w0 + wv[i]];
-                    }
-                }
-            }
-#pragma unroll
-            for (unsigned int i = 0; i < 8u; ++i) {
-                const unsigned int e = e0 + i * blockDim.x;
-                if (e < ne) {
-                    const float v = MODE == 2 ? xv[i] : __fmaf_rn(zv[i], __fsub_rn(xv[i], sv[i]), sv[i]);
-                    Y[eb + e] = v;
-                    bay_bsm[wv[i] * dp + (e - wv[i] * dim)] = v;
+        for (unsigned int i = 0; i < 8u; ++i) {
+            const unsigned int e = e0 + i * blockDim.x;
+            xv[i] = 0.0f;
+            sv[i] = 0.0f;
+            zv[i] = 0.0f;
+            if (e < ne) {
+                xv[i] = X[e];
+                if (MODE != 2) {
+                    const unsigned int w = bay_div_dim(e, dim, inv_dim), d = e - w * dim;
+                    sv[i] = S[(size_t)sJ[w] * dim + d];
+                    zv[i] = sZ[w];
                 }
             }
         }
-        __syncthreads();
-        if (tid < nr) {
-            const unsigned int kk = T.k0 + w0 + tid;
-            const float* y = bay_bsm + tid * dp;
-            float pr[BAY_PREP_LEN];
 #pragma unroll
-            for (int i = 0; i < BAY_PREP_LEN; ++i) pr[i] = 0.0f;
-            BAY_TILE_PREP(hyper, M.hyper_len, dim, y, pr);
-#pragma unroll
-            for (int i = 0; i < BAY_PREP_LEN; ++i) P.prep[((size_t)M.walker0 + kk) * BAY_PREP_LEN + i] = pr[i];
-            P.wterm[(size_t)M.walker0 + kk] = BAY_TILE_WALKER(M.rows, hyper, M.hyper_len, dim, y);
+        for (unsigned int i = 0; i < 8u; ++i) {
+            const unsigned int e = e0 + i * blockDim.x;
+            if (e < ne) Y[e] = MODE == 2 ? xv[i] : __fmaf_rn(zv[i], __fsub_rn(xv[i], sv[i]), sv[i]);
         }
-        __syncthreads();                 // the next round rewrites the staged rows
+    }
+    __syncthreads();
+    if (tid < nt) {
+        const float* y = Y + (size_t)tid * dim;
+        const float* hyper = P.params + M.params + M.rows * BAY_ROW_LEN;
+        float pr[BAY_PREP_LEN];
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) pr[i] = 0.0f;
+        BAY_TILE_PREP(hyper, M.hyper_len, dim, y, pr);
+#pragma unroll
+        for (int i = 0; i < BAY_PREP_LEN; ++i) P.prep[((size_t)M.walker0 + k) * BAY_PREP_LEN + i] = pr[i];
+        P.wterm[(size_t)M.walker0 + k] = BAY_TILE_WALKER(M.rows, hyper, M.hyper_len, dim, y);
     }
 }
 
