@@ -165,6 +165,9 @@ def test_model_check_autotuner_shapes(native):
     for bad in ((3, 256), (64, 256), (32, 16)):
         with pytest.raises(native.IllegalArgument):
             _check(post, "tiled", walkers_per_cta=bad[0], cta_threads=bad[1])
+    _check(post, "tiled", tile_slices=16)          # row slices: a launch parameter, 1..16
+    with pytest.raises(native.IllegalArgument, match="tile_slices"):
+        _check(post, "tiled", tile_slices=17)
     lg = M.logistic_model(64)
     for g, st in ((2, 2), (2, 3), (2, 4), (1, 2), (1, 6)):
         _check(lg, "gemm", tensor=True, tc_subtiles=g, tc_stages=st)
