@@ -1,4 +1,6 @@
-"""Integer arithmetic of the batched kernels, emulated in float32 on the CPU.
+"""Index arithmetic of the kernels, emulated on the CPU.
+
+The data-tiled form's row slices partition the rows exactly (test at the end).
 
 bay_div_dim (csrc/device/bay_batch.cuh) finds the walker of a tile element, e / dim, from a
 float reciprocal instead of an integer division: q = trunc(fl(e) * rcp_rn(dim)), then one
@@ -37,3 +39,33 @@ def test_div_dim_exhaustive_small_tiles():
     for dim in range(2, 258):
         e = np.arange(0, 256 * dim, dtype=np.uint32)
         np.testing.assert_array_equal(_div_dim(e, dim), e // np.uint32(dim))
+
+
+def _slices(n, ns):
+    """The data-tiled form's row slices (bay_stretch_tiled): slice sl of ns covers rows
+    [rb, rb + rn)."""
+    rps = (((n + ns - 1) // ns + 3) & ~3) if ns > 1 else n
+    out = []
+    for sl in range(ns):
+        rb = min(sl * rps, n)
+        out.append((rb, min(n - rb, rps)))
+    return rps, out
+
+
+def test_tile_slices_cover_every_row_once():
+    """Every row count up to 5,000 (and some large ones) and every slice count 1..16: the
+    slices are disjoint, cover [0, n) in order, start on a multiple of 4 rows (16-byte TMA
+    starts for any row length), and none is longer than the host's shared-memory plan
+    (min(rps, n) rows)."""
+    ns_all = range(1, 17)
+    for n in list(range(0, 5001)) + [10000, 30001, 1000000, 2 ** 24 + 3]:
+        for ns in ns_all:
+            rps, sl = _slices(n, ns)
+            pos = 0
+            for rb, rn in sl:
+                assert rb % 4 == 0 or rn == 0, (n, ns, rb)
+                if rn:
+                    assert rb == pos, (n, ns, rb, pos)
+                    pos = rb + rn
+                assert rn <= min(rps, n)
+            assert pos == n, (n, ns, pos)
