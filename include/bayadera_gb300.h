@@ -444,11 +444,11 @@ int bay_batch_test_barrier_timeout(bay_batch* b, int enabled);
  * group size at max-block-dim-x, nvidia_gtx.clj:803-807).  bay_autotune times the
  * candidate shapes of a model description on a workload -- walkers, params (host or
  * device) and optional starting positions (dim x walkers; NULL = N(0, I)) -- over bare
- * steps with CUDA events, and returns the fastest: for BAY_FORM_TILED walkers_per_cta and
- * cta_threads, for the BAY_MODEL_GEMM_TENSOR form tc_subtiles and tc_stages (streamed) or
- * tc_groups (matrix resident) -- set them in the bay_model_desc to compile the chosen
- * shape.  Other forms have nothing to
- * tune (the defaults come back, candidates 0).  Results are cached per (model, walkers,
+ * steps with CUDA events, and returns the fastest: for BAY_FORM_TILED walkers_per_cta,
+ * cta_threads and tile_slices, for the BAY_MODEL_GEMM_TENSOR form tc_subtiles and
+ * tc_stages (streamed) or tc_groups (matrix resident) -- set them in the bay_model_desc to
+ * compile the chosen shape.  Other forms have nothing to tune (the defaults come back,
+ * candidates 0).  Results are cached per (model, walkers,
  * params size, device) for the life of the process (from_cache 1).  Shapes change only the
  * order of the log-density sums. */
 typedef struct bay_tune_result {
